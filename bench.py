@@ -1,0 +1,344 @@
+"""Benchmark of the fused-tensor hot path on GB300.
+
+Default workload (``--workload c2``): the view-heavy fused op on
+x[64,128,56,56] ~ N(0,1) and bias[128] ~ N(0,0.1): permute NCHW->NHWC,
+broadcast-add the bias, max(.,0), translate by 1 along W, then sum over the
+channel axis to [64,56,56].  ``--workload c1``: ((a*b+c).tanh).sum over three
+[1024,1024] tensors uniform in [-1,1].
+
+A step is one evaluation of the op with its inputs resident in HBM.  The value
+is algorithmic bytes / time (the bytes a single fused pass must move: every
+input read once, the output written once).  Inputs rotate over enough copies
+that the working set exceeds the 129 MB L2 between uses of one copy.
+
+``--impl reference`` times the reference's CPU implementation of the same op
+(the oracle's restatement of the generated OpenCL C, compiled with OpenMP, on
+all host cores) on a bounded sample of the workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "compute.scala_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(workload):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(workload)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the GPU is busy."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        busy = [v for v in sm if mx and v > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ workloads
+
+C2 = dict(n=64, c=128, h=56, w=56)
+C1 = dict(n=1024, m=1024)
+
+
+def c2_bytes(n, c, h, w):
+    return 4 * (n * c * h * w + c + n * h * w)
+
+
+def c1_bytes(n, m):
+    return 4 * (3 * n * m) + 4
+
+
+def build_c2(T, x, bias, n, c, h, w):
+    y = T.max(x.permute([0, 2, 3, 1]) + bias.broadcast([n, h, w, c]), T.fill(0.0, [n, h, w, c]))
+    return y.translate([0, 0, 1, 0]).split(3).reduce(lambda a, b: a + b)
+
+
+def setup(workload, d):
+    """Returns (program, list of input-buffer lists to rotate over, output buffer, bytes, description)."""
+    T = d.Tensor
+    rt = d.runtime
+    if workload == "c2":
+        n, c, h, w = C2["n"], C2["c"], C2["h"], C2["w"]
+        x = T.randomNormal([n, c, h, w], seed=0).doCache()
+        bias = (T.randomNormal([c], seed=1) * T.fill(0.1, [c])).reshape([1, 1, 1, c]).doCache()
+        s = build_c2(T, x, bias, n, c, h, w)
+        ser = d.serialize(s.closure, s.shape)
+        assert [id(p) for p in ser.params] == [id(x), id(bias)]
+        prog = rt.program(ser.text)
+        xbytes = n * c * h * w * 4
+        copies = max(2, -(-4 * L2_BYTES // xbytes))
+        sets = []
+        for _ in range(copies):
+            buf = rt.alloc(xbytes)
+            rt.random(buf, n * c * h * w, 0, True)
+            sets.append([buf, bias._cached])
+        out = rt.alloc(n * h * w * 4)
+        return dict(prog=prog, sets=sets, out=out, bytes=c2_bytes(n, c, h, w), copies=copies,
+                    keep=[x, bias], ser=ser, shape=(n, c, h, w),
+                    config={"workload": "view-heavy fused op: x[64,128,56,56] permute->+bias[128]->max0"
+                                        "->translate W+1->channel sum [64,56,56]",
+                            "x": [n, c, h, w], "bias": [c], "out": [n, h, w],
+                            "l2": "inputs rotate over %d copies of x (%.0f MB > 4x L2)" % (copies, copies * xbytes / 1e6)})
+    if workload == "c1":
+        n, m = C1["n"], C1["m"]
+        two, one = T.fill(2.0, [n, m]), T.fill(1.0, [n, m])
+        abc = [(T.random([n, m], seed=s) * two - one).doCache() for s in (0, 1, 2)]
+        expr = T.tanh(abc[0] * abc[1] + abc[2])
+        ser = d.serialize(expr.closure, expr.shape, "sum")
+        prog = rt.program(ser.text)
+        copies = max(2, -(-4 * L2_BYTES // (3 * n * m * 4)))
+        sets = []
+        for k in range(copies):
+            trip = []
+            for t in abc:
+                buf = rt.alloc(n * m * 4)
+                d.runtime.launch(rt.program(d.serialize(t.closure, t.shape).text), [t._cached], buf)
+                trip.append(buf)
+            sets.append(trip)
+        out = rt.alloc(4)
+        return dict(prog=prog, sets=sets, out=out, bytes=c1_bytes(n, m), copies=copies, keep=abc, ser=ser,
+                    shape=(n, m),
+                    config={"workload": "fused elementwise+sum: ((a*b+c).tanh).sum, a,b,c [1024,1024] U[-1,1]",
+                            "l2": "inputs rotate over %d copies of (a,b,c) (%.0f MB > 4x L2)"
+                                  % (copies, copies * 3 * n * m * 4 / 1e6)})
+    raise SystemExit("unknown workload " + workload)
+
+
+def time_device(rt, st, steps, warmup):
+    prog, sets, out = st["prog"], st["sets"], st["out"]
+    ptr_sets = [[b.device_ptr() for b in s] for s in sets]
+    out_ptr = out.device_ptr()
+    for i in range(warmup):
+        rt.launch_ptrs(prog, ptr_sets[i % len(sets)], out_ptr)
+    rt.synchronize()
+    e0 = rt.event()
+    for i in range(steps):
+        rt.launch_ptrs(prog, ptr_sets[i % len(sets)], out_ptr)
+    e1 = rt.event()
+    rt.event_wait(e1, 120 * 10 ** 9)
+    ms = rt.event_elapsed_ms(e0, e1)
+    rt.event_release(e0)
+    rt.event_release(e1)
+    return ms
+
+
+def keep_busy(rt, st, seconds):
+    """Untimed launches of the same kernel so the clock sampler sees the GPU under this load."""
+    prog, sets, out = st["prog"], st["sets"], st["out"]
+    ptr_sets = [[b.device_ptr() for b in s] for s in sets]
+    t_end = time.time() + seconds
+    i = 0
+    while time.time() < t_end:
+        for _ in range(200):
+            rt.launch_ptrs(prog, ptr_sets[i % len(sets)], out.device_ptr())
+            i += 1
+        rt.synchronize()
+
+
+def time_e2e(d, st, steps):
+    """Host buffers in, result out, through the C ABI: upload inputs, launch, download."""
+    import ctypes
+    import numpy as np
+    from compute._native import call
+    rt = d.runtime
+    inputs = st["sets"][0]
+    hosts = []
+    h2d = 0
+    for b in inputs:
+        ptr = ctypes.c_void_p()
+        call("cc_host_alloc", ctypes.c_size_t(b.nbytes), ctypes.byref(ptr))
+        arr = np.ctypeslib.as_array((ctypes.c_float * (b.nbytes // 4)).from_address(ptr.value))
+        arr[:] = rt.download(b, b.nbytes // 4)
+        hosts.append((ptr, arr))
+        h2d += b.nbytes
+    out = st["out"]
+    out_elems = st["prog"].out_elems
+    res = np.empty(out_elems, np.float32)
+    d2h = res.nbytes
+
+    def step():
+        for (ptr, arr), b in zip(hosts, inputs):
+            call("cc_buf_upload", ctypes.c_uint64(b.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(b.nbytes))
+        rt.launch(st["prog"], inputs, out)
+        call("cc_buf_download", ctypes.c_uint64(out.handle), ctypes.c_size_t(0), res.ctypes.data_as(ctypes.c_void_p),
+             ctypes.c_size_t(d2h))
+
+    for _ in range(2):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = (time.perf_counter() - t0) / steps
+    for ptr, _ in hosts:
+        call("cc_host_free", ptr)
+    return dt, h2d, d2h
+
+
+def cpu_reference(workload, budget_s=15.0, threads=None):
+    """Times the reference's CPU implementation (the oracle's C restatement of the
+    generated OpenCL C, OpenMP over all host threads) on a bounded sample."""
+    from oracle import cref
+    return cref.time_workload(workload, budget_s=budget_s, threads=threads)
+
+
+# ------------------------------------------------------------------ main
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    metric = "fused-op GB/s"
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        r = cpu_reference(args.workload)
+        line = {"impl": "reference", "metric": metric, "value": r["gbs"], "unit": "GB/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
+                "config": r["config"],
+                "cpu_baseline": {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port",
+                                 "sample": r["sample"]},
+                "e2e": {"value": r["gbs"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo", init_method="env://")
+        dist = dist_mod
+
+    from compute import Tensors
+    d = Tensors(device=local_rank)
+    rt = d.runtime
+    st = setup(args.workload, d)
+    sampler = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    rt.synchronize()
+    sampler.start()
+    ms_total = time_device(rt, st, args.steps, warmup)
+    keep_busy(rt, st, 1.5)
+    clocks = sampler.stop()
+    if dist:
+        import torch
+        t = torch.tensor([ms_total], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+        dist.barrier()
+    ms_step = ms_total / args.steps
+    gbs_step = st["bytes"] / (ms_step * 1e-3) / 1e9
+    value = gbs_step * world
+
+    e2e = None
+    if not args.no_e2e:
+        dt, h2d, d2h = time_e2e(d, st, steps=max(3, min(args.steps, 20)))
+        e2e = {"value": st["bytes"] / dt / 1e9 * world, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
+    peak, peak_kind = _peaks()
+    roofline = {"bound": "hbm", "achieved": gbs_step, "peak": peak, "unit": "GB/s", "frac": gbs_step / peak,
+                "traffic": _traffic(args.workload), "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": st["bytes"]}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            r = cpu_reference(args.workload, budget_s=12.0)
+            cpu = {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port", "sample": r["sample"]}
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": "GB/s", "cores": None, "kind": "port", "sample": "failed: %s" % e}
+    if rank == 0:
+        line = {"metric": metric, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
+                "config": dict(st["config"], parallelism="replicas" if world > 1 else "single GPU"),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+                "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,558 @@
+// IR parsing and CUDA C generation for the fused kernels.
+//
+// The generated kernels compute, per output point, exactly the statement list
+// the reference's OpenCL kernel builder emits for the same tree
+// (OpenCLKernelBuilder/src/main/scala/com/thoughtworks/compute/
+// OpenCLKernelBuilder.scala): one `const float` per operator node (:245-326,
+// :516-571), view indices as `(int)(sum of gid * coefficient + constant)` with
+// the coefficients printed by DecimalFormat (:14-32, :348-386), and an
+// out-of-range view index reading the parameter's padding (:387-411).  Around
+// that statement list sit the sm_103a skeletons: a grid-stride elementwise
+// loop (with a float4 variant when every input is read contiguously) and a
+// compensated full sum with a single-pass grid reduction.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <sstream>
+#include <utility>
+
+#include "internal.h"
+
+namespace cc {
+
+// ---------------------------------------------------------------- parsing
+
+namespace {
+
+struct Tok {
+  const char *p, *end;
+  bool eol() {
+    while (p < end && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+    return p >= end || *p == '\n';
+  }
+  std::string word() {
+    if (eol()) fail(CC_ERR_INVALID_PROGRAM, "IR: unexpected end of line");
+    const char *s = p;
+    while (p < end && *p != ' ' && *p != '\t' && *p != '\n' && *p != '\r') ++p;
+    return std::string(s, p);
+  }
+  int64_t integer() {
+    std::string w = word();
+    char *e = nullptr;
+    long long v = strtoll(w.c_str(), &e, 10);
+    if (*e) fail(CC_ERR_INVALID_PROGRAM, "IR: bad integer '" + w + "'");
+    return v;
+  }
+  double real() {
+    std::string w = word();
+    char *e = nullptr;
+    double v = strtod(w.c_str(), &e);
+    if (*e) fail(CC_ERR_INVALID_PROGRAM, "IR: bad number '" + w + "'");
+    return v;
+  }
+  uint32_t hex32() {
+    std::string w = word();
+    char *e = nullptr;
+    unsigned long v = strtoul(w.c_str(), &e, 16);
+    if (*e || w.size() != 8) fail(CC_ERR_INVALID_PROGRAM, "IR: bad float bits '" + w + "'");
+    return (uint32_t)v;
+  }
+  void next_line() {
+    if (!eol()) fail(CC_ERR_INVALID_PROGRAM, "IR: trailing tokens");
+    if (p < end) ++p;
+  }
+};
+
+const char *kUnNames[] = {"neg", "exp", "log", "tanh", "abs", "sqrt"};
+const char *kBinNames[] = {"add", "sub", "mul", "div", "mod", "min", "max"};
+
+}  // namespace
+
+Ir parse_ir(const char *text, size_t len) {
+  Ir ir;
+  Tok t{text, text + len};
+  if (t.word() != "ccir" || t.integer() != 1) fail(CC_ERR_INVALID_PROGRAM, "IR: missing 'ccir 1' header");
+  std::string kind = t.word();
+  if (kind == "ew") ir.kind = ProgramKind::Elementwise;
+  else if (kind == "sum") ir.kind = ProgramKind::Sum;
+  else fail(CC_ERR_INVALID_PROGRAM, "IR: unknown program kind '" + kind + "'");
+  t.next_line();
+  if (t.word() != "o") fail(CC_ERR_INVALID_PROGRAM, "IR: missing output shape");
+  int64_t rank = t.integer();
+  if (rank < 0 || rank > 16) fail(CC_ERR_INVALID_PROGRAM, "IR: output rank out of range");
+  for (int64_t i = 0; i < rank; ++i) {
+    int64_t d = t.integer();
+    if (d < 0) fail(CC_ERR_INVALID_PROGRAM, "IR: negative dimension");
+    ir.out_shape.push_back(d);
+  }
+  t.next_line();
+  auto node_ref = [&](int64_t v) -> int {
+    if (v < 0 || v >= (int64_t)ir.nodes.size()) fail(CC_ERR_INVALID_PROGRAM, "IR: operand refers forward or out of range");
+    return (int)v;
+  };
+  while (t.p < t.end) {
+    if (t.eol()) { t.next_line(); continue; }
+    std::string tag = t.word();
+    if (tag == "r") {
+      ir.root = node_ref(t.integer());
+      t.next_line();
+      while (t.p < t.end) {
+        if (!t.eol()) fail(CC_ERR_INVALID_PROGRAM, "IR: content after root");
+        t.next_line();
+      }
+      break;
+    }
+    IrNode n;
+    if (tag == "p") {
+      n.kind = NodeKind::Param;
+      int64_t r = t.integer();
+      if (r < 0 || r > 16) fail(CC_ERR_INVALID_PROGRAM, "IR: parameter rank out of range");
+      for (int64_t i = 0; i < r; ++i) {
+        int64_t d = t.integer();
+        if (d < 0) fail(CC_ERR_INVALID_PROGRAM, "IR: negative dimension");
+        n.dims.push_back(d);
+      }
+      n.bits = t.hex32();
+      n.param_index = ir.n_params++;
+      ir.param_nodes.push_back((int)ir.nodes.size());
+    } else if (tag == "l") {
+      n.kind = NodeKind::Literal;
+      n.bits = t.hex32();
+    } else if (tag == "x") {
+      n.kind = NodeKind::Extract;
+      n.a = node_ref(t.integer());
+      if (ir.nodes[n.a].kind != NodeKind::Param) fail(CC_ERR_INVALID_PROGRAM, "IR: extract of a non-parameter");
+      n.cols = (int)t.integer();
+      size_t rows = ir.nodes[n.a].dims.size();
+      if (n.cols < 1 || n.cols > 17) fail(CC_ERR_INVALID_PROGRAM, "IR: bad matrix columns");
+      for (size_t i = 0; i < rows * (size_t)n.cols; ++i) n.m.push_back(t.real());
+    } else if (tag == "v") {
+      n.kind = NodeKind::View;
+      n.a = node_ref(t.integer());
+      int64_t r = t.integer();
+      if (r < 0 || r > 16) fail(CC_ERR_INVALID_PROGRAM, "IR: view rank out of range");
+      for (int64_t i = 0; i < r; ++i) {
+        int64_t d = t.integer();
+        if (d < 0) fail(CC_ERR_INVALID_PROGRAM, "IR: negative dimension");
+        n.dims.push_back(d);
+      }
+      n.bits = t.hex32();
+      n.cols = (int)t.integer();
+      if (n.cols < 1 || n.cols > 17) fail(CC_ERR_INVALID_PROGRAM, "IR: bad matrix columns");
+      for (size_t i = 0; i < (size_t)r * (size_t)n.cols; ++i) n.m.push_back(t.real());
+    } else if (tag == "u") {
+      n.kind = NodeKind::Unary;
+      std::string op = t.word();
+      int k = -1;
+      for (int i = 0; i < 6; ++i) if (op == kUnNames[i]) k = i;
+      if (k < 0) fail(CC_ERR_INVALID_PROGRAM, "IR: unknown unary operator '" + op + "'");
+      n.op = (uint8_t)k;
+      n.a = node_ref(t.integer());
+    } else if (tag == "b") {
+      n.kind = NodeKind::Binary;
+      std::string op = t.word();
+      int k = -1;
+      for (int i = 0; i < 7; ++i) if (op == kBinNames[i]) k = i;
+      if (k < 0) fail(CC_ERR_INVALID_PROGRAM, "IR: unknown binary operator '" + op + "'");
+      n.op = (uint8_t)k;
+      n.a = node_ref(t.integer());
+      n.b = node_ref(t.integer());
+    } else if (tag == "t") {
+      n.kind = NodeKind::Tuple;
+      int64_t cnt = t.integer();
+      if (cnt < 1 || cnt > 4096) fail(CC_ERR_INVALID_PROGRAM, "IR: bad tuple length");
+      for (int64_t i = 0; i < cnt; ++i) n.elems.push_back(node_ref(t.integer()));
+    } else {
+      fail(CC_ERR_INVALID_PROGRAM, "IR: unknown line tag '" + tag + "'");
+    }
+    t.next_line();
+    ir.nodes.push_back(std::move(n));
+  }
+  if (ir.root < 0) fail(CC_ERR_INVALID_PROGRAM, "IR: missing root");
+  for (size_t i = 0; i < ir.nodes.size(); ++i) {
+    if (ir.nodes[i].kind == NodeKind::Tuple && (int)i != ir.root)
+      fail(CC_ERR_INVALID_PROGRAM, "IR: a tuple may only be the root");
+  }
+  if (ir.kind == ProgramKind::Sum && ir.nodes[ir.root].kind == NodeKind::Tuple)
+    fail(CC_ERR_INVALID_PROGRAM, "IR: the sum of a tuple-valued tree is not defined");
+  return ir;
+}
+
+// ---------------------------------------------------------------- literals
+
+std::string decimal_format3(double v) {
+  // Exact decimal expansion of the double, then HALF_EVEN rounding at the third
+  // fraction digit (java.text.DecimalFormat's default pattern "#,##0.###" with
+  // grouping off).
+  if (std::isnan(v)) return "NaN";
+  if (std::isinf(v)) return v > 0 ? "\xE2\x88\x9E" : "-\xE2\x88\x9E";
+  bool neg = std::signbit(v);
+  double a = std::fabs(v);
+  static thread_local char buf[1600];
+  snprintf(buf, sizeof buf, "%.1100f", a);
+  std::string s(buf);
+  size_t dot = s.find('.');
+  std::string ip = s.substr(0, dot);
+  std::string fp = s.substr(dot + 1);
+  std::string keep = fp.substr(0, 3);
+  std::string rest = fp.substr(3);
+  int cmp;  // rest vs one half
+  if (rest.empty() || rest[0] < '5') {
+    cmp = -1;
+  } else if (rest[0] > '5') {
+    cmp = 1;
+  } else {
+    cmp = (rest.find_first_not_of('0', 1) == std::string::npos) ? 0 : 1;
+  }
+  std::string digits = ip + keep;
+  bool up = cmp > 0 || (cmp == 0 && ((digits.back() - '0') % 2 == 1));
+  if (up) {
+    int i = (int)digits.size() - 1;
+    while (i >= 0) {
+      if (digits[i] == '9') { digits[i] = '0'; --i; }
+      else { digits[i]++; break; }
+    }
+    if (i < 0) digits.insert(digits.begin(), '1');
+  }
+  std::string ipart = digits.substr(0, digits.size() - 3);
+  std::string fpart = digits.substr(digits.size() - 3);
+  size_t nz = ipart.find_first_not_of('0');
+  ipart = nz == std::string::npos ? "0" : ipart.substr(nz);
+  while (!fpart.empty() && fpart.back() == '0') fpart.pop_back();
+  std::string out = (neg ? "-" : "") + ipart;
+  if (!fpart.empty()) out += "." + fpart;
+  return out;
+}
+
+// ---------------------------------------------------------------- generation
+
+namespace {
+
+// device_common.cuh, embedded at build time as a string literal.
+const char *kPrelude =
+#include "device_common.inc"
+    ;
+
+std::string lit_code(uint32_t bits) {
+  char b[48];
+  snprintf(b, sizeof b, "__int_as_float(0x%08x)", bits);
+  return b;
+}
+
+struct Frame {
+  int id;
+  std::vector<std::string> gid;   // index variable names
+  std::vector<int64_t> shape;
+};
+
+class Generator {
+ public:
+  Generator(const Ir &ir, bool contiguous_mode) : ir_(ir), contig_(contiguous_mode) {}
+
+  // Returns the name of the variable holding node `n` evaluated in frame `f`.
+  std::string gen(int n, const Frame &f, std::ostringstream &os, int ind) {
+    auto key = std::make_pair(n, f.id);
+    auto it = memo_.find(key);
+    if (it != memo_.end()) return it->second;
+    const IrNode &node = ir_.nodes[n];
+    std::string pad(ind, ' ');
+    std::string v;
+    switch (node.kind) {
+      case NodeKind::Literal:
+        v = fresh();
+        os << pad << "const float " << v << " = " << lit_code(node.bits) << ";\n";
+        break;
+      case NodeKind::Unary: {
+        std::string a = gen(node.a, f, os, ind);
+        v = fresh();
+        static const char *fn[] = {"-", "expf", "logf", "tanhf", "fabsf", "sqrtf"};
+        if (node.op == (uint8_t)UnOp::Neg)
+          os << pad << "const float " << v << " = -" << a << ";\n";
+        else
+          os << pad << "const float " << v << " = " << fn[node.op] << "(" << a << ");\n";
+        break;
+      }
+      case NodeKind::Binary: {
+        std::string a = gen(node.a, f, os, ind);
+        std::string b = gen(node.b, f, os, ind);
+        v = fresh();
+        switch ((BinOp)node.op) {
+          case BinOp::Add: os << pad << "const float " << v << " = " << a << " + " << b << ";\n"; break;
+          case BinOp::Sub: os << pad << "const float " << v << " = " << a << " - " << b << ";\n"; break;
+          case BinOp::Mul: os << pad << "const float " << v << " = " << a << " * " << b << ";\n"; break;
+          case BinOp::Div: os << pad << "const float " << v << " = " << a << " / " << b << ";\n"; break;
+          case BinOp::Mod: os << pad << "const float " << v << " = fmodf(" << a << ", " << b << ");\n"; break;
+          case BinOp::Min: os << pad << "const float " << v << " = fminf(" << a << ", " << b << ");\n"; break;
+          case BinOp::Max: os << pad << "const float " << v << " = fmaxf(" << a << ", " << b << ");\n"; break;
+        }
+        break;
+      }
+      case NodeKind::Extract: {
+        const IrNode &p = ir_.nodes[node.a];
+        if (node.cols != (int)f.shape.size() + 1)
+          fail(CC_ERR_INVALID_PROGRAM, "IR: view matrix columns do not match the frame rank");
+        v = fresh();
+        if (contig_) {
+          os << pad << "const float " << v << " = a" << p.param_index << ";\n";
+          break;
+        }
+        std::vector<std::string> idx;
+        std::string ok = index_rows(node, p.dims, f, os, ind, idx);
+        std::string off = offset_expr(p.dims, idx);
+        std::string load = "__ldg(in" + std::to_string(p.param_index) + " + " + off + ")";
+        if (p.dims.empty()) load = "__ldg(in" + std::to_string(p.param_index) + ")";
+        if (ok.empty())
+          os << pad << "const float " << v << " = " << load << ";\n";
+        else
+          os << pad << "const float " << v << " = (" << ok << ") ? " << load << " : " << lit_code(p.bits) << ";\n";
+        break;
+      }
+      case NodeKind::View: {
+        if (node.cols != (int)f.shape.size() + 1)
+          fail(CC_ERR_INVALID_PROGRAM, "IR: view matrix columns do not match the frame rank");
+        v = fresh();
+        std::vector<std::string> idx;
+        std::string ok = index_rows(node, node.dims, f, os, ind, idx);
+        Frame inner{next_frame_++, idx, node.dims};
+        os << pad << "float " << v << ";\n";
+        if (!ok.empty()) {
+          os << pad << "if (" << ok << ") {\n";
+          std::string sub = gen(node.a, inner, os, ind + 2);
+          os << pad << "  " << v << " = " << sub << ";\n";
+          os << pad << "} else {\n" << pad << "  " << v << " = " << lit_code(node.bits) << ";\n" << pad << "}\n";
+        } else {
+          os << pad << "{\n";
+          std::string sub = gen(node.a, inner, os, ind + 2);
+          os << pad << "  " << v << " = " << sub << ";\n" << pad << "}\n";
+        }
+        break;
+      }
+      case NodeKind::Param:
+        fail(CC_ERR_INVALID_PROGRAM, "IR: a parameter is used as a value without Extract");
+      case NodeKind::Tuple:
+        fail(CC_ERR_INVALID_PROGRAM, "IR: nested tuple");
+    }
+    memo_[key] = v;
+    return v;
+  }
+
+  bool uses_fp64() const { return fp64_; }
+
+ private:
+  std::string fresh() { return "_" + std::to_string(next_var_++); }
+
+  // Emits one index variable per source dimension, the way ArrayView.extract
+  // does (OpenCLKernelBuilder.scala:348-411); returns the bounds condition
+  // ("" when every row is constant-zero and no check applies).
+  std::string index_rows(const IrNode &node, const std::vector<int64_t> &dims, const Frame &f,
+                         std::ostringstream &os, int ind, std::vector<std::string> &idx) {
+    std::string pad(ind, ' ');
+    const int rows = (int)dims.size();
+    const int cols = node.cols;
+    std::string ok;
+    for (int y = 0; y < rows; ++y) {
+      std::string sum;
+      bool any = false;
+      for (int x = 0; x < cols; ++x) {
+        double s = node.m[(size_t)y * cols + x];
+        if (s == 0.0) continue;
+        std::string term;
+        if (x < cols - 1) {
+          term = (s == 1.0) ? f.gid[x] : f.gid[x] + " * " + literal(s);
+        } else {
+          term = literal(s);
+        }
+        sum += (any ? " + " : "") + term;
+        any = true;
+      }
+      std::string name = "_i" + std::to_string(next_var_++);
+      if (!any) {
+        os << pad << "const int " << name << " = 0;\n";
+        if (dims[y] == 0) ok += std::string(ok.empty() ? "" : " && ") + "false";
+      } else {
+        os << pad << "const int " << name << " = (int)(" << sum << ");\n";
+        ok += std::string(ok.empty() ? "" : " && ") + "(" + name + " >= 0) && (" + name + " < " +
+              std::to_string(dims[y]) + ")";
+      }
+      idx.push_back(name);
+    }
+    return ok;
+  }
+
+  std::string literal(double s) {
+    std::string t = decimal_format3(s);
+    if (t.find('.') != std::string::npos) fp64_ = true;
+    if (t[0] == '-') return "(" + t + ")";
+    return t;
+  }
+
+  static std::string offset_expr(const std::vector<int64_t> &dims, const std::vector<std::string> &idx) {
+    if (dims.empty()) return "0";
+    int64_t total = 1;
+    for (int64_t d : dims) total *= d;
+    bool wide = total >= (int64_t(1) << 31);
+    std::string e = wide ? "(cc_i64)" + idx[0] : idx[0];
+    for (size_t i = 1; i < dims.size(); ++i) {
+      e = "(" + e + " * " + std::to_string(dims[i]) + (wide ? "LL" : "") + " + " + idx[i] + ")";
+    }
+    return e;
+  }
+
+  const Ir &ir_;
+  bool contig_;
+  bool fp64_ = false;
+  int next_var_ = 0;
+  int next_frame_ = 1;
+  std::map<std::pair<int, int>, std::string> memo_;
+};
+
+bool is_contiguous_identity(const IrNode &x, const IrNode &p, const std::vector<int64_t> &out_shape) {
+  if (p.dims != out_shape) return false;
+  const int rows = (int)p.dims.size();
+  const int cols = x.cols;
+  if (cols != rows + 1) return false;
+  for (int y = 0; y < rows; ++y)
+    for (int c = 0; c < cols; ++c)
+      if (x.m[(size_t)y * cols + c] != (c == y ? 1.0 : 0.0)) return false;
+  return true;
+}
+
+}  // namespace
+
+Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
+  Generated g;
+  g.n_inputs = ir.n_params;
+  const IrNode &root = ir.nodes[ir.root];
+  g.tuple_len = root.kind == NodeKind::Tuple ? (int)root.elems.size() : 1;
+  int64_t domain = 1;
+  for (int64_t d : ir.out_shape) domain *= d;
+  g.domain = domain;
+  g.out_elems = ir.kind == ProgramKind::Sum ? 1 : domain * g.tuple_len;
+  const int rank = (int)ir.out_shape.size();
+
+  // Contiguous: every value reachable from the root is a literal, an operator,
+  // or an identity read of a parameter with the output's shape.
+  bool contiguous = g.tuple_len == 1 && domain > 0;
+  for (const IrNode &n : ir.nodes) {
+    if (n.kind == NodeKind::View) contiguous = false;
+    if (n.kind == NodeKind::Extract && !is_contiguous_identity(n, ir.nodes[n.a], ir.out_shape)) contiguous = false;
+  }
+  g.has_vec4 = contiguous;
+
+  std::ostringstream src;
+  src << "// generated by compute.scala_gb300 for sm_103a\n" << kPrelude << "\n";
+
+  std::string params;
+  for (int i = 0; i < ir.n_params; ++i) params += "const float *__restrict__ in" + std::to_string(i) + ", ";
+
+  // Frame 0: output coordinates decoded from the linear index.
+  Frame f0{0, {}, ir.out_shape};
+  for (int d = 0; d < rank; ++d) f0.gid.push_back("g" + std::to_string(d));
+  auto decode = [&](std::ostringstream &os, int ind) {
+    std::string pad(ind, ' ');
+    if (rank == 0) return;
+    os << pad << "cc_i64 rem_ = lin;\n";
+    for (int d = rank - 1; d >= 1; --d) {
+      os << pad << "const int g" << d << " = (int)(rem_ % " << ir.out_shape[d] << "LL);\n";
+      os << pad << "rem_ /= " << ir.out_shape[d] << "LL;\n";
+    }
+    os << pad << "const int g0 = (int)rem_;\n";
+  };
+
+  const std::string block = std::to_string(opt.block);
+  bool fp64 = false;
+
+  if (contiguous) {
+    // The point function of the contiguous form: parameter values in, result out.
+    Generator gen(ir, true);
+    std::ostringstream body;
+    std::string r = gen.gen(ir.root, f0, body, 2);
+    fp64 |= gen.uses_fp64();
+    src << "__device__ __forceinline__ float cc_point(";
+    for (int i = 0; i < ir.n_params; ++i) src << (i ? ", " : "") << "float a" << i;
+    if (ir.n_params == 0) src << "void";
+    src << ") {\n" << body.str() << "  return " << r << ";\n}\n\n";
+  }
+
+  // Generic per-point body (frame 0 at coordinates decoded from `lin`).
+  std::ostringstream generic;
+  std::vector<std::string> results;
+  {
+    Generator gen(ir, false);
+    decode(generic, 4);
+    if (root.kind == NodeKind::Tuple) {
+      for (int e : root.elems) results.push_back(gen.gen(e, f0, generic, 4));
+    } else {
+      results.push_back(gen.gen(ir.root, f0, generic, 4));
+    }
+    fp64 |= gen.uses_fp64();
+  }
+  g.uses_fp64_index = fp64;
+
+  std::string call_args;
+  auto contig_call = [&](const std::string &lane) {
+    std::string s = "cc_point(";
+    for (int i = 0; i < ir.n_params; ++i) s += (i ? ", " : "") + std::string("v") + std::to_string(i) + lane;
+    return s + ")";
+  };
+
+  if (ir.kind == ProgramKind::Elementwise) {
+    src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_ew(" << params
+        << "float *__restrict__ out, cc_i64 n) {\n"
+        << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+        << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
+        << generic.str();
+    if (g.tuple_len == 1) {
+      src << "    out[lin] = " << results[0] << ";\n";
+    } else {
+      for (int k = 0; k < g.tuple_len; ++k)
+        src << "    out[lin * " << g.tuple_len << "LL + " << k << "] = " << results[k] << ";\n";
+    }
+    src << "  }\n}\n\n";
+    if (contiguous) {
+      src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_ew_v4(" << params
+          << "float *__restrict__ out, cc_i64 n) {\n"
+          << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+          << "  const cc_i64 n4 = n >> 2;\n"
+          << "  for (cc_i64 q = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {\n";
+      for (int i = 0; i < ir.n_params; ++i)
+        src << "    const float4 v" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
+      src << "    float4 r;\n";
+      for (const char *lane : {".x", ".y", ".z", ".w"}) src << "    r" << lane << " = " << contig_call(lane) << ";\n";
+      src << "    reinterpret_cast<float4 *>(out)[q] = r;\n  }\n"
+          << "  for (cc_i64 lin = (n4 << 2) + (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n";
+      for (int i = 0; i < ir.n_params; ++i) src << "    const float v" << i << " = __ldg(in" << i << " + lin);\n";
+      src << "    out[lin] = " << contig_call("") << ";\n  }\n}\n\n";
+    }
+  } else {
+    src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum(" << params
+        << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
+        << "  float s_ = 0.0f, c_ = 0.0f;\n"
+        << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+        << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
+        << generic.str() << "    cc_acc(s_, c_, " << results[0] << ");\n  }\n"
+        << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+    if (contiguous) {
+      src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum_v4(" << params
+          << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
+          << "  float s_ = 0.0f, c_ = 0.0f;\n"
+          << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+          << "  const cc_i64 n4 = n >> 2;\n"
+          << "  for (cc_i64 q = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {\n";
+      for (int i = 0; i < ir.n_params; ++i)
+        src << "    const float4 v" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
+      for (const char *lane : {".x", ".y", ".z", ".w"}) src << "    cc_acc(s_, c_, " << contig_call(lane) << ");\n";
+      src << "  }\n"
+          << "  for (cc_i64 lin = (n4 << 2) + (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n";
+      for (int i = 0; i < ir.n_params; ++i) src << "    const float v" << i << " = __ldg(in" << i << " + lin);\n";
+      src << "    cc_acc(s_, c_, " << contig_call("") << ");\n  }\n"
+          << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+    }
+  }
+  g.source = src.str();
+  return g;
+}
+
+}  // namespace cc

@@ -1,0 +1,78 @@
+// Device helpers shared by the precompiled kernels (kernels.cu) and every
+// NVRTC-generated program (codegen.cpp embeds this file as its prelude).
+#pragma once
+
+typedef long long cc_i64;
+typedef unsigned long long cc_u64;
+
+// Error-free transformation of a + b (Knuth's TwoSum); the intrinsics are never
+// contracted into FMAs, so the error term is exact under any compile flags.
+__device__ __forceinline__ void cc_two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void cc_acc(float &s, float &c, float v) {
+  float t, e;
+  cc_two_sum(s, v, t, e);
+  s = t;
+  c = __fadd_rn(c, e);
+}
+__device__ __forceinline__ void cc_merge(float &s, float &c, float s2, float c2) {
+  float t, e;
+  cc_two_sum(s, s2, t, e);
+  s = t;
+  c = __fadd_rn(__fadd_rn(c, c2), e);
+}
+__device__ __forceinline__ void cc_warp_merge(float &s, float &c) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float s2 = __shfl_down_sync(0xffffffffu, s, o);
+    float c2 = __shfl_down_sync(0xffffffffu, c, o);
+    cc_merge(s, c, s2, c2);
+  }
+}
+// Block reduction of (s, c) pairs into thread 0, in a fixed order.
+__device__ __forceinline__ void cc_block_merge(float &s, float &c, float2 *ws) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  cc_warp_merge(s, c);
+  if (lane == 0) ws[wid] = make_float2(s, c);
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    s = lane < nw ? ws[lane].x : 0.0f;
+    c = lane < nw ? ws[lane].y : 0.0f;
+    cc_warp_merge(s, c);
+  }
+  __syncthreads();
+}
+// Single-pass grid sum: each block publishes its compensated partial; the last
+// block to finish (completion counter) combines all partials in block order, so
+// the result does not depend on which block finishes last, and resets the
+// counter for the next launch.
+__device__ __forceinline__ void cc_grid_finish(float s, float c, float2 *__restrict__ partials,
+                                               unsigned int *__restrict__ counter, float *__restrict__ out) {
+  __shared__ float2 ws[32];
+  __shared__ int last;
+  cc_block_merge(s, c, ws);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = make_float2(s, c);
+    __threadfence();
+    unsigned int ticket = atomicAdd(counter, 1u);
+    last = (ticket == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  s = 0.0f;
+  c = 0.0f;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    float2 p = __ldcg(&partials[i]);
+    cc_merge(s, c, p.x, p.y);
+  }
+  cc_block_merge(s, c, ws);
+  if (threadIdx.x == 0) {
+    out[0] = isfinite(s) ? __fadd_rn(s, c) : s;
+    *counter = 0u;
+  }
+}

@@ -1,0 +1,91 @@
+// Internal declarations shared by the runtime translation units.
+#pragma once
+
+#include <cuda.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/compute_cuda.h"
+
+namespace cc {
+
+// A failure carried to the C ABI boundary, where it becomes a status code and
+// the thread's last-error message.
+struct Error {
+  int code;
+  std::string message;
+};
+
+[[noreturn]] void fail(int code, const std::string &message);
+
+// Driver API functions the runtime uses, resolved at cc_init through
+// cudaGetDriverEntryPointByVersion (the library itself does not link libcuda).
+struct Driver {
+  bool loaded = false;
+  decltype(&::cuModuleLoadData) ModuleLoadData = nullptr;
+  decltype(&::cuModuleGetFunction) ModuleGetFunction = nullptr;
+  decltype(&::cuModuleUnload) ModuleUnload = nullptr;
+  decltype(&::cuLaunchKernel) LaunchKernel = nullptr;
+  decltype(&::cuGetErrorName) GetErrorName = nullptr;
+  decltype(&::cuGetErrorString) GetErrorString = nullptr;
+  decltype(&::cuCtxGetCurrent) CtxGetCurrent = nullptr;
+  decltype(&::cuCtxSetCurrent) CtxSetCurrent = nullptr;
+  decltype(&::cuFuncSetAttribute) FuncSetAttribute = nullptr;
+  decltype(&::cuTensorMapEncodeTiled) TensorMapEncodeTiled = nullptr;
+};
+extern Driver g_drv;
+
+// ---- IR (the alpha-converted expression tree; format documented in compute/trees.py)
+enum class NodeKind : uint8_t { Param, Literal, Extract, View, Unary, Binary, Tuple };
+enum class UnOp : uint8_t { Neg, Exp, Log, Tanh, Abs, Sqrt };
+enum class BinOp : uint8_t { Add, Sub, Mul, Div, Mod, Min, Max };
+
+struct IrNode {
+  NodeKind kind;
+  uint8_t op = 0;              // UnOp / BinOp
+  int a = -1, b = -1;          // operands; Extract: a = param node; View: a = sub node
+  std::vector<int64_t> dims;   // Param / View: the viewed tensor's shape
+  uint32_t bits = 0;           // Literal value / Param or View padding (binary32 bits)
+  int cols = 0;                // Extract / View: matrix columns (= frame rank + 1)
+  std::vector<double> m;       // Extract / View: row-major view matrix
+  std::vector<int> elems;      // Tuple
+  int param_index = -1;        // Param: kernel input number
+};
+
+enum class ProgramKind : int { Elementwise = 0, Sum = 1 };
+
+struct Ir {
+  ProgramKind kind = ProgramKind::Elementwise;
+  std::vector<int64_t> out_shape;
+  std::vector<IrNode> nodes;
+  int root = -1;
+  int n_params = 0;
+  std::vector<int> param_nodes;
+};
+
+Ir parse_ir(const char *text, size_t len);
+
+struct CodegenOptions {
+  int block = 256;
+};
+
+struct Generated {
+  std::string source;
+  bool has_vec4 = false;   // a float4 variant of the kernel exists (all inputs contiguous)
+  int tuple_len = 1;
+  int n_inputs = 0;
+  int64_t out_elems = 0;   // floats written (1 for a sum)
+  int64_t domain = 0;      // points evaluated
+  bool uses_fp64_index = false;
+};
+
+Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);
+
+// The literal text DecimalFormat gives a view coefficient (at most three
+// fraction digits, HALF_EVEN, no grouping), as OpenCLKernelBuilder.toLiteral.
+std::string decimal_format3(double v);
+
+}  // namespace cc

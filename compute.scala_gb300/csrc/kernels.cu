@@ -1,0 +1,123 @@
+// Precompiled sm_103a kernels whose code does not depend on an expression tree:
+// the random-number generators and the plain full sum of a float buffer.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace cc {
+namespace {
+
+// Thomas Wang's 32-bit integer hash, the reference's default generator
+// (Tensors/src/main/scala/com/thoughtworks/compute/Tensors.scala:106-117).
+__device__ __forceinline__ unsigned int wang_hash(unsigned int v) {
+  v = (v ^ 61u) ^ (v >> 16);
+  v *= 9u;
+  v ^= v << 4;
+  v *= 0x27d4eb2du;
+  v ^= v >> 15;
+  return v;
+}
+
+// Marsaglia xorshift32 step (Tensors.scala:402-406).
+__device__ __forceinline__ unsigned int xorshift(unsigned int s) {
+  const unsigned int t1 = s ^ (s << 13);
+  const unsigned int t2 = t1 ^ (t1 >> 17);
+  return t2 ^ (t2 << 5);
+}
+
+// hash / 2^32 as the reference writes it: the uint converts to float with
+// round-to-nearest-even, and the division by a power of two is exact.
+__device__ __forceinline__ float unit_float(unsigned int h) {
+  return __fmul_rn(__uint2float_rn(h), 2.3283064365386963e-10f);
+}
+
+// Tensors.scala:431-443: buffer[i] = hash(i ^ seed) / 4294967296.0f
+__global__ void __launch_bounds__(256) random_uniform_kernel(float *__restrict__ out, long long n,
+                                                             unsigned int seed) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    out[i] = unit_float(wang_hash((unsigned int)i ^ seed));
+  }
+}
+
+// Tensors.scala:397-429: one Box-Muller pair per work item.
+__global__ void __launch_bounds__(256) random_normal_kernel(float2 *__restrict__ out, long long pairs,
+                                                            unsigned int seed) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const float two_pi = 6.28318548202514648f;  // 2 * M_PI_F, exact in binary32
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < pairs; i += stride) {
+    const unsigned int r1 = wang_hash((unsigned int)i ^ seed);
+    const unsigned int r2 = xorshift(r1);
+    const float u1 = unit_float(r1);
+    const float u2 = unit_float(r2);
+    const float r = sqrtf(__fmul_rn(-2.0f, logf(u1)));
+    const float theta = __fmul_rn(two_pi, u2);
+    out[i] = make_float2(__fmul_rn(r, cosf(theta)), __fmul_rn(r, sinf(theta)));
+  }
+}
+
+// Plain compensated sum of a float buffer (the kind-1 program of a bare
+// parameter, precompiled): float4 loads when the address allows.
+__global__ void __launch_bounds__(256) sum_kernel(const float *__restrict__ in, long long n,
+                                                  float2 *__restrict__ partials, unsigned int *__restrict__ counter,
+                                                  float *__restrict__ out, int vec4) {
+  float s = 0.0f, c = 0.0f;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long start = 0;
+  if (vec4) {
+    const long long n4 = n >> 2;
+    const float4 *in4 = reinterpret_cast<const float4 *>(in);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
+      const float4 v = __ldg(in4 + q);
+      cc_acc(s, c, v.x);
+      cc_acc(s, c, v.y);
+      cc_acc(s, c, v.z);
+      cc_acc(s, c, v.w);
+    }
+    start = n4 << 2;
+  }
+  for (long long i = start + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    cc_acc(s, c, __ldg(in + i));
+  }
+  cc_grid_finish(s, c, partials, counter, out);
+}
+
+}  // namespace
+
+cudaError_t launch_random(float *out, long long n, unsigned int seed, int normal, int sm_count,
+                          cudaStream_t stream) {
+  const int block = 256;
+  long long work = normal ? (n + 1) / 2 : n;
+  if (work <= 0) return cudaSuccess;
+  long long grid = (work + block - 1) / block;
+  long long cap = (long long)sm_count * 16;
+  if (grid > cap) grid = cap;
+  if (normal) {
+    random_normal_kernel<<<(unsigned)grid, block, 0, stream>>>(reinterpret_cast<float2 *>(out), work, seed);
+  } else {
+    random_uniform_kernel<<<(unsigned)grid, block, 0, stream>>>(out, work, seed);
+  }
+  return cudaGetLastError();
+}
+
+int sum_grid(long long work, int sm_count) {
+  long long grid = (work + 255) / 256;
+  long long cap = (long long)sm_count * 8;
+  if (cap > kMaxSumBlocks) cap = kMaxSumBlocks;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  return (int)grid;
+}
+
+cudaError_t launch_sum(const float *in, long long n, float2 *partials, unsigned int *counter, float *out,
+                       int sm_count, cudaStream_t stream) {
+  const int vec4 = (reinterpret_cast<uintptr_t>(in) & 15u) == 0;
+  const int grid = sum_grid(vec4 ? (n >> 2) : n, sm_count);
+  sum_kernel<<<grid, 256, 0, stream>>>(in, n, partials, counter, out, vec4);
+  return cudaGetLastError();
+}
+
+}  // namespace cc

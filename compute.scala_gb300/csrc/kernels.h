@@ -1,0 +1,18 @@
+// Host-side launchers of the precompiled kernels in kernels.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace cc {
+
+// Upper bound on the blocks of one grid sum; the scratch of a sum holds this
+// many float2 partials plus one completion counter.
+constexpr int kMaxSumBlocks = 4096;
+
+cudaError_t launch_random(float *out, long long n, unsigned int seed, int normal, int sm_count,
+                          cudaStream_t stream);
+int sum_grid(long long work, int sm_count);
+cudaError_t launch_sum(const float *in, long long n, float2 *partials, unsigned int *counter, float *out,
+                       int sm_count, cudaStream_t stream);
+
+}  // namespace cc

@@ -1,0 +1,838 @@
+// The C ABI of include/compute_cuda.h: context, buffer pool, NVRTC program
+// cache, launches, reductions, random numbers and events.
+//
+// It stands where the reference's OpenCL layer stands
+// (OpenCL/src/main/scala/com/thoughtworks/compute/OpenCL.scala): one CUDA
+// stream per context instead of a pool of command queues (:423-448), a
+// size-binned pool instead of one clCreateBuffer per result (:1397-1431), NVRTC
+// to cubin instead of clBuildProgram (:885-932, :1266-1294), and bounded event
+// waits instead of driver callbacks (:1246-1263).
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "internal.h"
+#include "kernels.h"
+
+namespace cc {
+
+namespace {
+thread_local std::string t_last_error;
+}
+
+void fail(int code, const std::string &message) { throw Error{code, message}; }
+
+// Driver API entry points, resolved through the CUDA runtime at cc_init so the
+// library loads (and its GPU-free entry points work) on hosts without a driver.
+Driver g_drv;
+
+namespace {
+
+void check_cuda(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return;
+  int code = CC_ERR_CUDA;
+  if (e == cudaErrorMemoryAllocation) code = CC_ERR_OUT_OF_MEMORY;
+  fail(code, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+template <class F>
+void resolve(F &fn, const char *symbol) {
+  cudaDriverEntryPointQueryResult q;
+  void *p = nullptr;
+  cudaError_t e = cudaGetDriverEntryPointByVersion(symbol, &p, 12080, cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+    cudaGetLastError();
+    fail(CC_ERR_CUDA, std::string("driver entry point ") + symbol + " is unavailable");
+  }
+  fn = reinterpret_cast<F>(p);
+}
+
+void load_driver() {
+  if (g_drv.loaded) return;
+  resolve(g_drv.ModuleLoadData, "cuModuleLoadData");
+  resolve(g_drv.ModuleGetFunction, "cuModuleGetFunction");
+  resolve(g_drv.ModuleUnload, "cuModuleUnload");
+  resolve(g_drv.LaunchKernel, "cuLaunchKernel");
+  resolve(g_drv.GetErrorName, "cuGetErrorName");
+  resolve(g_drv.GetErrorString, "cuGetErrorString");
+  resolve(g_drv.CtxGetCurrent, "cuCtxGetCurrent");
+  resolve(g_drv.CtxSetCurrent, "cuCtxSetCurrent");
+  resolve(g_drv.FuncSetAttribute, "cuFuncSetAttribute");
+  resolve(g_drv.TensorMapEncodeTiled, "cuTensorMapEncodeTiled");
+  g_drv.loaded = true;
+}
+
+void check_cu(CUresult r, const char *what) {
+  if (r == CUDA_SUCCESS) return;
+  const char *name = nullptr, *str = nullptr;
+  if (g_drv.GetErrorName) g_drv.GetErrorName(r, &name);
+  if (g_drv.GetErrorString) g_drv.GetErrorString(r, &str);
+  int code = r == CUDA_ERROR_OUT_OF_MEMORY ? CC_ERR_OUT_OF_MEMORY : CC_ERR_CUDA;
+  fail(code, std::string(what) + ": " + (name ? name : "?") + " (" + (str ? str : "?") + ")");
+}
+
+// ---------------------------------------------------------------- buffer pool
+//
+// Blocks are binned by size class (eight classes per power of two above 4 KiB,
+// so at most 12.5% slack).  A released block goes back to its class's free
+// list; work is ordered on the context stream, so a later allocation may reuse
+// it at once.  A cap (cc_pool_set_limit) turns allocations past it into
+// CC_ERR_OUT_OF_MEMORY, the reference's MemObjectAllocationFailure.
+class Pool {
+ public:
+  static size_t size_class(size_t bytes) {
+    if (bytes <= 4096) {
+      size_t c = 256;
+      while (c < bytes) c <<= 1;
+      return c;
+    }
+    size_t p = 4096;
+    while (p < bytes) p <<= 1;       // p/2 < bytes <= p
+    size_t base = p >> 1, step = base >> 3;
+    return base + ((bytes - base + step - 1) / step) * step;
+  }
+
+  void *alloc(size_t bytes, size_t *cls_out) {
+    size_t cls = size_class(bytes == 0 ? 1 : bytes);
+    *cls_out = cls;
+    auto it = free_.find(cls);
+    if (it != free_.end() && !it->second.empty()) {
+      void *p = it->second.back();
+      it->second.pop_back();
+      cached_ -= cls;
+      in_use_ += cls;
+      ++reuses_;
+      return p;
+    }
+    if (limit_ && in_use_ + cls > limit_) {
+      fail(CC_ERR_OUT_OF_MEMORY, "buffer pool limit reached: " + std::to_string(in_use_) + " bytes in use, " +
+                                     std::to_string(cls) + " requested, limit " + std::to_string(limit_));
+    }
+    if (limit_ && in_use_ + cached_ + cls > limit_) trim();
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, cls);
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      trim();
+      e = cudaMalloc(&p, cls);
+    }
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail(CC_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(cls) + " bytes failed: " + cudaGetErrorString(e));
+    }
+    in_use_ += cls;
+    ++allocs_;
+    return p;
+  }
+
+  void release(void *p, size_t cls) {
+    in_use_ -= cls;
+    cached_ += cls;
+    free_[cls].push_back(p);
+  }
+
+  void trim() {
+    for (auto &kv : free_) {
+      for (void *p : kv.second) {
+        cudaFree(p);
+        cached_ -= kv.first;
+      }
+      kv.second.clear();
+    }
+  }
+
+  size_t in_use_ = 0, cached_ = 0, limit_ = 0;
+  uint64_t allocs_ = 0, reuses_ = 0;
+
+ private:
+  std::map<size_t, std::vector<void *>> free_;
+};
+
+struct Buffer {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  size_t cls = 0;
+  int refs = 1;
+};
+
+struct Program {
+  CUmodule module = nullptr;
+  CUfunction scalar = nullptr;  // cc_ew / cc_sum
+  CUfunction vec4 = nullptr;    // cc_ew_v4 / cc_sum_v4 (contiguous inputs)
+  ProgramKind kind = ProgramKind::Elementwise;
+  Generated gen;
+};
+
+struct Event {
+  cudaEvent_t ev = nullptr;
+};
+
+enum : uint64_t { kTagBuffer = 1, kTagProgram = 2, kTagEvent = 3 };
+
+struct Context {
+  int device = 0;
+  CUcontext cuctx = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  int sm_count = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t total_mem = 0;
+  uint32_t flags = 0;
+
+  std::recursive_mutex mu;
+  Pool pool;
+  uint64_t next_id = 1;
+  std::unordered_map<uint64_t, Buffer *> buffers;
+  std::unordered_map<uint64_t, Program *> programs;   // by handle
+  std::unordered_map<std::string, uint64_t> cache;    // IR text -> program handle
+  std::unordered_map<uint64_t, Event *> events;
+  uint64_t cache_hits = 0, cache_misses = 0;
+  std::mutex compile_mu;
+
+  // Scratch of the grid sums: kMaxSumBlocks float2 partials, then the counter.
+  void *sum_scratch = nullptr;
+  size_t sum_scratch_cls = 0;
+
+  uint64_t make_handle(uint64_t tag) { return (tag << 56) | (next_id++); }
+  float2 *partials() { return reinterpret_cast<float2 *>(sum_scratch); }
+  unsigned int *counter() {
+    return reinterpret_cast<unsigned int *>(static_cast<char *>(sum_scratch) + sizeof(float2) * kMaxSumBlocks);
+  }
+};
+
+std::mutex g_init_mu;
+Context *g_ctx = nullptr;
+
+Context &ctx() {
+  Context *c = g_ctx;
+  if (!c) fail(CC_ERR_NOT_INITIALIZED, "cc_init has not been called");
+  thread_local CUcontext bound = nullptr;
+  if (bound != c->cuctx) {
+    check_cuda(cudaSetDevice(c->device), "cudaSetDevice");
+    check_cu(g_drv.CtxSetCurrent(c->cuctx), "cuCtxSetCurrent");
+    bound = c->cuctx;
+  }
+  return *c;
+}
+
+uint64_t tag_of(uint64_t h) { return h >> 56; }
+
+Buffer &buffer_of(Context &c, cc_handle h) {
+  auto it = c.buffers.find(h);
+  if (tag_of(h) != kTagBuffer || it == c.buffers.end())
+    fail(CC_ERR_INVALID_MEM_OBJECT, "not a live buffer handle");
+  return *it->second;
+}
+
+Program &program_of(Context &c, cc_handle h) {
+  auto it = c.programs.find(h);
+  if (tag_of(h) != kTagProgram || it == c.programs.end()) fail(CC_ERR_INVALID_PROGRAM, "not a program handle");
+  return *it->second;
+}
+
+Event &event_of(Context &c, cc_handle h) {
+  auto it = c.events.find(h);
+  if (tag_of(h) != kTagEvent || it == c.events.end()) fail(CC_ERR_INVALID_EVENT, "not a live event handle");
+  return *it->second;
+}
+
+// ---------------------------------------------------------------- NVRTC
+
+std::vector<char> compile_cubin(const std::string &source, int cc_major, int cc_minor, uint32_t flags) {
+  nvrtcProgram prog;
+  nvrtcResult r = nvrtcCreateProgram(&prog, source.c_str(), "cc_program.cu", 0, nullptr, nullptr);
+  if (r != NVRTC_SUCCESS) fail(CC_ERR_BUILD_PROGRAM_FAILURE, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
+  std::string arch = "-arch=sm_" + std::to_string(cc_major) + std::to_string(cc_minor) + "a";
+  std::vector<std::string> opts = {arch, "--std=c++17", "-default-device",
+                                   (flags & CC_FLAG_FMA_CONTRACT) ? "--fmad=true" : "--fmad=false"};
+  std::vector<const char *> optp;
+  for (auto &o : opts) optp.push_back(o.c_str());
+  r = nvrtcCompileProgram(prog, (int)optp.size(), optp.data());
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    if (n) nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    fail(CC_ERR_BUILD_PROGRAM_FAILURE, "NVRTC build failure (" + arch + "):\n" + log);
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  std::vector<char> cubin(n);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  return cubin;
+}
+
+// ---------------------------------------------------------------- launches
+
+int64_t ew_grid(int64_t work, int block, int sm_count) {
+  int64_t grid = (work + block - 1) / block;
+  int64_t cap = (int64_t)sm_count * 16;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  return grid;
+}
+
+void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
+  const int block = 256;
+  const int64_t n = p.gen.domain;
+  bool aligned = (out & 15u) == 0;
+  for (uint64_t a : in) aligned = aligned && (a & 15u) == 0;
+  const bool vec = p.vec4 && aligned;
+  CUfunction f = vec ? p.vec4 : p.scalar;
+  const int64_t work = vec ? (n >> 2) : n;
+  std::vector<void *> args;
+  std::vector<uint64_t> ptrs(in);
+  for (auto &v : ptrs) args.push_back(&v);
+  uint64_t out_ptr = out;
+  int64_t nn = n;
+  uint64_t partials = 0, counter = 0;
+  unsigned grid;
+  if (p.kind == ProgramKind::Sum) {
+    partials = reinterpret_cast<uint64_t>(c.partials());
+    counter = reinterpret_cast<uint64_t>(c.counter());
+    args.push_back(&partials);
+    args.push_back(&counter);
+    grid = (unsigned)sum_grid(work, c.sm_count);
+  } else {
+    if (n == 0) return;
+    grid = (unsigned)ew_grid(work, block, c.sm_count);
+  }
+  args.push_back(&out_ptr);
+  args.push_back(&nn);
+  check_cu(g_drv.LaunchKernel(f, grid, 1, 1, block, 1, 1, 0, (CUstream)stream, args.data(), nullptr),
+           "cuLaunchKernel");
+}
+
+}  // namespace
+}  // namespace cc
+
+using namespace cc;
+
+#define CC_API_BEGIN try {
+#define CC_API_END                                            \
+  }                                                           \
+  catch (const cc::Error &e) {                                \
+    cc::t_last_error = e.message;                             \
+    return e.code;                                            \
+  }                                                           \
+  catch (const std::bad_alloc &) {                            \
+    cc::t_last_error = "host allocation failed";              \
+    return CC_ERR_OUT_OF_RESOURCES;                           \
+  }                                                           \
+  catch (const std::exception &e) {                           \
+    cc::t_last_error = e.what();                              \
+    return CC_ERR_INVALID_VALUE;                              \
+  }                                                           \
+  return CC_OK;
+
+extern "C" {
+
+int cc_last_error(char *buf, size_t len) {
+  if (!buf || len == 0) return CC_ERR_INVALID_VALUE;
+  size_t n = t_last_error.size() < len - 1 ? t_last_error.size() : len - 1;
+  memcpy(buf, t_last_error.data(), n);
+  buf[n] = '\0';
+  return CC_OK;
+}
+
+int cc_init(int device_ordinal, uint32_t flags) {
+  CC_API_BEGIN
+  std::lock_guard<std::mutex> g(g_init_mu);
+  if (g_ctx) {
+    if (g_ctx->device != device_ordinal) fail(CC_ERR_INVALID_OPERATION, "already initialised on another device");
+    g_ctx->flags = flags;
+    return CC_OK;
+  }
+  int count = 0;
+  cudaError_t ce = cudaGetDeviceCount(&count);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    fail(CC_ERR_DEVICE_NOT_FOUND, std::string("no usable CUDA device: ") + cudaGetErrorString(ce));
+  }
+  if (device_ordinal < 0 || device_ordinal >= count) fail(CC_ERR_DEVICE_NOT_FOUND, "no CUDA device " + std::to_string(device_ordinal));
+  load_driver();
+  auto c = std::make_unique<Context>();
+  c->device = device_ordinal;
+  c->flags = flags;
+  check_cuda(cudaSetDevice(device_ordinal), "cudaSetDevice");
+  check_cuda(cudaFree(nullptr), "cudaFree(0)");  // creates the primary context and makes it current
+  check_cu(g_drv.CtxGetCurrent(&c->cuctx), "cuCtxGetCurrent");
+  check_cuda(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device_ordinal), "attr");
+  check_cuda(cudaDeviceGetAttribute(&c->cc_major, cudaDevAttrComputeCapabilityMajor, device_ordinal), "attr");
+  check_cuda(cudaDeviceGetAttribute(&c->cc_minor, cudaDevAttrComputeCapabilityMinor, device_ordinal), "attr");
+  {
+    size_t free_b = 0;
+    check_cuda(cudaMemGetInfo(&free_b, &c->total_mem), "cudaMemGetInfo");
+  }
+  check_cuda(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  c->stream = c->own_stream;
+  c->sum_scratch = c->pool.alloc(sizeof(float2) * kMaxSumBlocks + 256, &c->sum_scratch_cls);
+  check_cuda(cudaMemsetAsync(c->sum_scratch, 0, sizeof(float2) * kMaxSumBlocks + 256, c->stream), "cudaMemsetAsync");
+  check_cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  g_ctx = c.release();
+  CC_API_END
+}
+
+int cc_shutdown(void) {
+  CC_API_BEGIN
+  std::lock_guard<std::mutex> g(g_init_mu);
+  Context *c = g_ctx;
+  if (!c) return CC_OK;
+  cudaSetDevice(c->device);
+  g_drv.CtxSetCurrent(c->cuctx);
+  cudaStreamSynchronize(c->stream);
+  for (auto &kv : c->programs) {
+    g_drv.ModuleUnload(kv.second->module);
+    delete kv.second;
+  }
+  for (auto &kv : c->buffers) {
+    cudaFree(kv.second->ptr);
+    delete kv.second;
+  }
+  for (auto &kv : c->events) {
+    cudaEventDestroy(kv.second->ev);
+    delete kv.second;
+  }
+  c->pool.release(c->sum_scratch, c->sum_scratch_cls);
+  c->pool.trim();
+  cudaStreamDestroy(c->own_stream);
+  g_ctx = nullptr;
+  delete c;
+  CC_API_END
+}
+
+int cc_device_info(int *sm_count, int *cc_major, int *cc_minor, size_t *total_mem) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  if (sm_count) *sm_count = c.sm_count;
+  if (cc_major) *cc_major = c.cc_major;
+  if (cc_minor) *cc_minor = c.cc_minor;
+  if (total_mem) *total_mem = c.total_mem;
+  CC_API_END
+}
+
+int cc_get_stream(uint64_t *stream) {
+  CC_API_BEGIN
+  if (!stream) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  *stream = reinterpret_cast<uint64_t>(ctx().stream);
+  CC_API_END
+}
+
+int cc_set_stream(uint64_t stream) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  // Blocks freed so far may still be read by work on the old stream.
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  c.stream = stream ? reinterpret_cast<cudaStream_t>(stream) : c.own_stream;
+  CC_API_END
+}
+
+int cc_synchronize(void) {
+  CC_API_BEGIN
+  check_cuda(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+  CC_API_END
+}
+
+// ---------------------------------------------------------------- buffers
+
+int cc_buf_alloc(size_t bytes, cc_handle *out) {
+  CC_API_BEGIN
+  if (!out) fail(CC_ERR_INVALID_VALUE, "null handle pointer");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  auto b = std::make_unique<Buffer>();
+  b->ptr = c.pool.alloc(bytes, &b->cls);
+  b->bytes = bytes;
+  uint64_t h = c.make_handle(kTagBuffer);
+  c.buffers[h] = b.release();
+  *out = h;
+  CC_API_END
+}
+
+int cc_buf_retain(cc_handle h) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  buffer_of(c, h).refs++;
+  CC_API_END
+}
+
+int cc_buf_release(cc_handle h) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Buffer &b = buffer_of(c, h);
+  if (--b.refs == 0) {
+    c.pool.release(b.ptr, b.cls);
+    delete &b;
+    c.buffers.erase(h);
+  }
+  CC_API_END
+}
+
+int cc_buf_size(cc_handle h, size_t *bytes) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (!bytes) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  *bytes = buffer_of(c, h).bytes;
+  CC_API_END
+}
+
+int cc_buf_device_ptr(cc_handle h, uint64_t *ptr) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (!ptr) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  *ptr = reinterpret_cast<uint64_t>(buffer_of(c, h).ptr);
+  CC_API_END
+}
+
+int cc_buf_upload(cc_handle h, size_t offset, const void *host, size_t bytes) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  void *dst;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    Buffer &b = buffer_of(c, h);
+    if (offset > b.bytes || bytes > b.bytes - offset) fail(CC_ERR_INVALID_VALUE, "upload range exceeds the buffer");
+    dst = static_cast<char *>(b.ptr) + offset;
+  }
+  if (bytes == 0) return CC_OK;
+  if (!host) fail(CC_ERR_INVALID_VALUE, "null host pointer");
+  check_cuda(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, c.stream), "cudaMemcpyAsync H2D");
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  CC_API_END
+}
+
+int cc_buf_download(cc_handle h, size_t offset, void *host, size_t bytes) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  void *src;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    Buffer &b = buffer_of(c, h);
+    if (offset > b.bytes || bytes > b.bytes - offset) fail(CC_ERR_INVALID_VALUE, "download range exceeds the buffer");
+    src = static_cast<char *>(b.ptr) + offset;
+  }
+  if (bytes == 0) return CC_OK;
+  if (!host) fail(CC_ERR_INVALID_VALUE, "null host pointer");
+  check_cuda(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, c.stream), "cudaMemcpyAsync D2H");
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  CC_API_END
+}
+
+int cc_host_alloc(size_t bytes, void **host) {
+  CC_API_BEGIN
+  if (!host) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  ctx();
+  check_cuda(cudaMallocHost(host, bytes ? bytes : 1), "cudaMallocHost");
+  CC_API_END
+}
+
+int cc_host_free(void *host) {
+  CC_API_BEGIN
+  ctx();
+  if (host) check_cuda(cudaFreeHost(host), "cudaFreeHost");
+  CC_API_END
+}
+
+int cc_pool_stats(size_t *in_use, size_t *cached, uint64_t *allocs, uint64_t *reuses) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (in_use) *in_use = c.pool.in_use_;
+  if (cached) *cached = c.pool.cached_;
+  if (allocs) *allocs = c.pool.allocs_;
+  if (reuses) *reuses = c.pool.reuses_;
+  CC_API_END
+}
+
+int cc_pool_set_limit(size_t bytes) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  c.pool.limit_ = bytes;
+  CC_API_END
+}
+
+int cc_pool_trim(void) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  c.pool.trim();
+  CC_API_END
+}
+
+// ---------------------------------------------------------------- programs
+
+int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
+  CC_API_BEGIN
+  if (!ir_text || !out) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Context &c = ctx();
+  std::string key(ir_text, ir_len);
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    auto it = c.cache.find(key);
+    if (it != c.cache.end()) {
+      ++c.cache_hits;
+      *out = it->second;
+      return CC_OK;
+    }
+  }
+  std::lock_guard<std::mutex> cg(c.compile_mu);
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    auto it = c.cache.find(key);
+    if (it != c.cache.end()) {
+      ++c.cache_hits;
+      *out = it->second;
+      return CC_OK;
+    }
+  }
+  Ir ir = parse_ir(ir_text, ir_len);
+  CodegenOptions opt;
+  auto p = std::make_unique<Program>();
+  p->gen = generate_cuda(ir, opt);
+  p->kind = ir.kind;
+  std::vector<char> cubin = compile_cubin(p->gen.source, c.cc_major, c.cc_minor, c.flags);
+  check_cu(g_drv.ModuleLoadData(&p->module, cubin.data()), "cuModuleLoadData");
+  const char *sname = ir.kind == ProgramKind::Sum ? "cc_sum" : "cc_ew";
+  const char *vname = ir.kind == ProgramKind::Sum ? "cc_sum_v4" : "cc_ew_v4";
+  check_cu(g_drv.ModuleGetFunction(&p->scalar, p->module, sname), "cuModuleGetFunction");
+  if (p->gen.has_vec4) check_cu(g_drv.ModuleGetFunction(&p->vec4, p->module, vname), "cuModuleGetFunction");
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  uint64_t h = c.make_handle(kTagProgram);
+  c.programs[h] = p.release();
+  c.cache[key] = h;
+  ++c.cache_misses;
+  *out = h;
+  CC_API_END
+}
+
+int cc_codegen(const char *ir_text, size_t ir_len, char *buf, size_t len, size_t *needed) {
+  CC_API_BEGIN
+  if (!ir_text) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Ir ir = parse_ir(ir_text, ir_len);
+  Generated gen = generate_cuda(ir, CodegenOptions{});
+  if (needed) *needed = gen.source.size() + 1;
+  if (buf && len) {
+    size_t n = gen.source.size() < len - 1 ? gen.source.size() : len - 1;
+    memcpy(buf, gen.source.data(), n);
+    buf[n] = '\0';
+  }
+  CC_API_END
+}
+
+int cc_compile_check(const char *ir_text, size_t ir_len, int cc_major, int cc_minor, uint32_t flags) {
+  CC_API_BEGIN
+  if (!ir_text) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Ir ir = parse_ir(ir_text, ir_len);
+  Generated gen = generate_cuda(ir, CodegenOptions{});
+  compile_cubin(gen.source, cc_major, cc_minor, flags);
+  CC_API_END
+}
+
+int cc_program_info(cc_handle h, int *kind, int *n_inputs, int64_t *out_elems, int *tuple_len) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Program &p = program_of(c, h);
+  if (kind) *kind = (int)p.kind;
+  if (n_inputs) *n_inputs = p.gen.n_inputs;
+  if (out_elems) *out_elems = p.gen.out_elems;
+  if (tuple_len) *tuple_len = p.gen.tuple_len;
+  CC_API_END
+}
+
+int cc_program_source(cc_handle h, char *buf, size_t len, size_t *needed) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Program &p = program_of(c, h);
+  const std::string &s = p.gen.source;
+  if (needed) *needed = s.size() + 1;
+  if (buf && len) {
+    size_t n = s.size() < len - 1 ? s.size() : len - 1;
+    memcpy(buf, s.data(), n);
+    buf[n] = '\0';
+  }
+  CC_API_END
+}
+
+int cc_program_cache_stats(uint64_t *hits, uint64_t *misses, uint64_t *entries) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (hits) *hits = c.cache_hits;
+  if (misses) *misses = c.cache_misses;
+  if (entries) *entries = c.cache.size();
+  CC_API_END
+}
+
+int cc_launch(cc_handle prog, const cc_handle *inputs, int n_inputs, cc_handle output) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Program &p = program_of(c, prog);
+  if (n_inputs != p.gen.n_inputs)
+    fail(CC_ERR_INVALID_KERNEL_ARGS, "program takes " + std::to_string(p.gen.n_inputs) + " inputs, got " +
+                                         std::to_string(n_inputs));
+  std::vector<uint64_t> ptrs;
+  for (int i = 0; i < n_inputs; ++i) {
+    Buffer &b = buffer_of(c, inputs[i]);
+    ptrs.push_back(reinterpret_cast<uint64_t>(b.ptr));
+  }
+  Buffer &o = buffer_of(c, output);
+  if (o.bytes < (size_t)p.gen.out_elems * sizeof(float))
+    fail(CC_ERR_INVALID_VALUE, "output buffer holds " + std::to_string(o.bytes) + " bytes, the program writes " +
+                                   std::to_string(p.gen.out_elems * sizeof(float)));
+  launch_program(c, p, ptrs, reinterpret_cast<uint64_t>(o.ptr), c.stream);
+  CC_API_END
+}
+
+int cc_launch_ptrs(cc_handle prog, const uint64_t *input_ptrs, int n_inputs, uint64_t output_ptr, uint64_t stream) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Program &p = program_of(c, prog);
+  if (n_inputs != p.gen.n_inputs) fail(CC_ERR_INVALID_KERNEL_ARGS, "wrong number of inputs");
+  if (!output_ptr || (n_inputs && !input_ptrs)) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  std::vector<uint64_t> ptrs(input_ptrs, input_ptrs + n_inputs);
+  for (uint64_t q : ptrs)
+    if (!q) fail(CC_ERR_INVALID_VALUE, "null input pointer");
+  launch_program(c, p, ptrs, output_ptr, stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream);
+  CC_API_END
+}
+
+// ---------------------------------------------------------------- sums and random numbers
+
+int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stream) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  if (!out_ptr || (n && !in_ptr)) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  // Scratch for this call from the pool: partials, then the zeroed counter.
+  size_t cls = 0;
+  const size_t bytes = sizeof(float2) * kMaxSumBlocks + 256;
+  void *scratch = c.pool.alloc(bytes, &cls);
+  auto *partials = reinterpret_cast<float2 *>(scratch);
+  auto *counter = reinterpret_cast<unsigned int *>(static_cast<char *>(scratch) + sizeof(float2) * kMaxSumBlocks);
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
+  if (e == cudaSuccess)
+    e = launch_sum(reinterpret_cast<const float *>(in_ptr), (long long)n, partials, counter,
+                   reinterpret_cast<float *>(out_ptr), c.sm_count, s);
+  if (s != c.stream && e == cudaSuccess) e = cudaStreamSynchronize(s);  // the pool is ordered on the context stream
+  c.pool.release(scratch, cls);
+  check_cuda(e, "sum launch");
+  CC_API_END
+}
+
+int cc_random(cc_handle output, size_t n, uint32_t seed, int normal) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Buffer &b = buffer_of(c, output);
+  size_t need = normal ? ((n + 1) / 2) * 2 : n;
+  if (b.bytes < need * sizeof(float)) fail(CC_ERR_INVALID_VALUE, "output buffer too small for the random numbers");
+  check_cuda(launch_random(static_cast<float *>(b.ptr), (long long)n, seed, normal, c.sm_count, c.stream),
+             "random launch");
+  CC_API_END
+}
+
+// ---------------------------------------------------------------- events
+
+int cc_event_record(cc_handle *out) {
+  CC_API_BEGIN
+  if (!out) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  auto e = std::make_unique<Event>();
+  check_cuda(cudaEventCreate(&e->ev), "cudaEventCreate");
+  cudaError_t r = cudaEventRecord(e->ev, c.stream);
+  if (r != cudaSuccess) {
+    cudaEventDestroy(e->ev);
+    check_cuda(r, "cudaEventRecord");
+  }
+  uint64_t h = c.make_handle(kTagEvent);
+  c.events[h] = e.release();
+  *out = h;
+  CC_API_END
+}
+
+int cc_event_query(cc_handle h, int *complete) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  cudaEvent_t ev;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    ev = event_of(c, h).ev;
+  }
+  cudaError_t r = cudaEventQuery(ev);
+  if (r == cudaErrorNotReady) {
+    if (complete) *complete = 0;
+    return CC_OK;
+  }
+  check_cuda(r, "cudaEventQuery");
+  if (complete) *complete = 1;
+  CC_API_END
+}
+
+int cc_event_wait(cc_handle h, uint64_t timeout_ns) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  cudaEvent_t ev;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    ev = event_of(c, h).ev;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  int spin = 0;
+  for (;;) {
+    cudaError_t r = cudaEventQuery(ev);
+    if (r == cudaSuccess) return CC_OK;
+    if (r != cudaErrorNotReady) check_cuda(r, "cudaEventQuery");
+    auto dt = std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+    if ((uint64_t)dt >= timeout_ns) fail(CC_ERR_TIMEOUT, "event not complete after " + std::to_string(timeout_ns) + " ns");
+    if (++spin > 64) std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  CC_API_END
+}
+
+int cc_event_elapsed(cc_handle start, cc_handle end, float *ms) {
+  CC_API_BEGIN
+  if (!ms) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  check_cuda(cudaEventElapsedTime(ms, event_of(c, start).ev, event_of(c, end).ev), "cudaEventElapsedTime");
+  CC_API_END
+}
+
+int cc_event_release(cc_handle h) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Event &e = event_of(c, h);
+  cudaEventDestroy(e.ev);
+  delete &e;
+  c.events.erase(h);
+  CC_API_END
+}
+
+}  // extern "C"

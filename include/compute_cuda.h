@@ -1,0 +1,147 @@
+/*
+ * compute_cuda.h -- C ABI of the GB300 (sm_103a) back-end for Compute.scala's
+ * fused-tensor path.
+ *
+ * A `cuda` device object (a sibling of Compute.scala's `gpu` and `cpu`
+ * objects) binds these entry points through JNI or Panama; the Python mirror
+ * of the Tensor API in this repository binds them through ctypes.  Every
+ * entry point replaces one member of the OpenCL layer that `Tensors` calls
+ * (paths below are inside the Compute.scala project):
+ *
+ *   OpenCL/src/main/scala/com/thoughtworks/compute/OpenCL.scala      ("OpenCL.scala")
+ *   Tensors/src/main/scala/com/thoughtworks/compute/Tensors.scala    ("Tensors.scala")
+ *
+ * Conventions
+ *   - Every function returns a status: 0 on success, otherwise a negative
+ *     code.  Codes that have an OpenCL counterpart use its value, so the
+ *     reference's `OpenCL.Exceptions.fromErrorCode` (OpenCL.scala:251-303)
+ *     maps them to the same exception types.  The message of the last failure
+ *     on the calling thread is returned by cc_last_error.
+ *   - Handles are opaque 64-bit values (0 is never a valid handle).
+ *   - All functions are thread-safe.  Work is ordered on one CUDA stream per
+ *     context (cc_get_stream / cc_set_stream).
+ *   - Completion is reported by polling or by blocking waits with a timeout;
+ *     the library never calls back into the caller from a driver thread.
+ */
+#ifndef COMPUTE_CUDA_H
+#define COMPUTE_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef uint64_t cc_handle;
+
+/* ---- status codes -------------------------------------------------------- */
+#define CC_OK                         0
+#define CC_ERR_DEVICE_NOT_FOUND      (-1)    /* CL_DEVICE_NOT_FOUND */
+#define CC_ERR_OUT_OF_MEMORY         (-4)    /* CL_MEM_OBJECT_ALLOCATION_FAILURE */
+#define CC_ERR_OUT_OF_RESOURCES      (-5)    /* CL_OUT_OF_RESOURCES */
+#define CC_ERR_BUILD_PROGRAM_FAILURE (-11)   /* CL_BUILD_PROGRAM_FAILURE; message = NVRTC log */
+#define CC_ERR_INVALID_VALUE         (-30)   /* CL_INVALID_VALUE */
+#define CC_ERR_INVALID_MEM_OBJECT    (-38)   /* CL_INVALID_MEM_OBJECT */
+#define CC_ERR_INVALID_PROGRAM       (-44)   /* CL_INVALID_PROGRAM */
+#define CC_ERR_INVALID_KERNEL_ARGS   (-52)   /* CL_INVALID_KERNEL_ARGS */
+#define CC_ERR_INVALID_EVENT         (-58)   /* CL_INVALID_EVENT */
+#define CC_ERR_INVALID_OPERATION     (-59)   /* CL_INVALID_OPERATION */
+#define CC_ERR_TIMEOUT               (-1001) /* a bounded wait ran out */
+#define CC_ERR_NOT_INITIALIZED       (-1002) /* cc_init has not succeeded */
+#define CC_ERR_CUDA                  (-1003) /* CUDA runtime/driver error; see cc_last_error */
+#define CC_ERR_DEVICE_REPORTED       (-1004) /* a kernel set its error flag (bounded wait expired) */
+
+/* ---- flags for cc_init ----------------------------------------------------- */
+#define CC_FLAG_FMA_CONTRACT   0x1u  /* let the compiler fuse a*b+c into one FMA (off: every
+                                        SSA statement rounds separately, as written) */
+#define CC_FLAG_NO_FUSION_SUM  0x2u  /* reserved */
+
+/* ---- context: replaces OpenCL.UseAllDevicesByType + context + CommandQueuePool
+ *      (OpenCL.scala:340-374, :423-448, :1375-1393) ------------------------- */
+int cc_init(int device_ordinal, uint32_t flags);
+int cc_shutdown(void);
+/* Copies the message of this thread's last failure (NUL-terminated, truncated to len). */
+int cc_last_error(char *buf, size_t len);
+/* deviceId.maxComputeUnits / deviceType (OpenCL.scala:451-470). */
+int cc_device_info(int *sm_count, int *cc_major, int *cc_minor, size_t *total_mem);
+int cc_get_stream(uint64_t *stream);            /* the context's cudaStream_t */
+int cc_set_stream(uint64_t stream);             /* order later work on a caller-owned stream */
+int cc_synchronize(void);
+
+/* ---- device buffers: replace allocateBuffer / allocateBufferFrom
+ *      (OpenCL.scala:1397-1431) and DeviceBuffer.retain/release/numberOfBytes/
+ *      toHostBuffer (OpenCL.scala:633-717).  Buffers come from a size-binned,
+ *      stream-ordered pool; the reference count mirrors retain/release. ------ */
+int cc_buf_alloc(size_t bytes, cc_handle *buf);
+int cc_buf_retain(cc_handle buf);
+int cc_buf_release(cc_handle buf);
+int cc_buf_size(cc_handle buf, size_t *bytes);
+int cc_buf_device_ptr(cc_handle buf, uint64_t *device_ptr);
+/* Host -> device copy into [offset, offset+bytes).  Returns when the host memory may be reused. */
+int cc_buf_upload(cc_handle buf, size_t offset, const void *host, size_t bytes);
+/* Device -> host copy of [offset, offset+bytes) after all work queued so far; blocking. */
+int cc_buf_download(cc_handle buf, size_t offset, void *host, size_t bytes);
+/* Page-locked host memory for fast transfers (the staging of Tensor.apply / flatArray). */
+int cc_host_alloc(size_t bytes, void **host);
+int cc_host_free(void *host);
+/* Pool accounting and an optional cap (bytes in use + cached); 0 = no cap. */
+int cc_pool_stats(size_t *in_use, size_t *cached, uint64_t *allocs, uint64_t *reuses);
+int cc_pool_set_limit(size_t bytes);
+int cc_pool_trim(void);
+
+/* ---- programs: replace createProgramWithSource + Program.build
+ *      (OpenCL.scala:885-932, :1266-1294) and the kernel cache keyed by the
+ *      alpha-converted tree (Tensors.scala:1267-1293).  `ir` is the
+ *      alpha-converted expression tree in the text form documented in
+ *      compute/trees.py; the runtime generates CUDA C for sm_103a, compiles it
+ *      with NVRTC to a cubin and caches it by the IR text.  A compile failure
+ *      returns CC_ERR_BUILD_PROGRAM_FAILURE with the NVRTC log as the message
+ *      (the reference's BuildProgramFailure, OpenCL.scala:172-181). --------- */
+int cc_program_get(const char *ir, size_t ir_len, cc_handle *program);
+/* kind: 0 = elementwise store, 1 = full sum.  out_elems = number of floats written. */
+int cc_program_info(cc_handle program, int *kind, int *n_inputs, int64_t *out_elems, int *tuple_len);
+/* The generated CUDA C source, NUL-terminated; *needed gets the size required. */
+int cc_program_source(cc_handle program, char *buf, size_t len, size_t *needed);
+int cc_program_cache_stats(uint64_t *hits, uint64_t *misses, uint64_t *entries);
+/* GPU-free checks of the same path (no cc_init needed): the CUDA C generated
+ * for `ir`, and an NVRTC compile of it for sm_<cc_major><cc_minor>a whose
+ * failure carries the NVRTC log, like cc_program_get. */
+int cc_codegen(const char *ir, size_t ir_len, char *buf, size_t len, size_t *needed);
+int cc_compile_check(const char *ir, size_t ir_len, int cc_major, int cc_minor, uint32_t flags);
+
+/* ---- launch: replaces Kernel.update + Kernel.enqueue + dispatch
+ *      (OpenCL.scala:751-844, :1298-1329) as driven by CompiledKernel.run
+ *      (Tensors.scala:1331-1381).  Inputs are in the program's parameter
+ *      order; the output must hold out_elems floats (1 for a sum). --------- */
+int cc_launch(cc_handle program, const cc_handle *inputs, int n_inputs, cc_handle output);
+/* The same on raw device pointers and a caller stream (0 = the context stream). */
+int cc_launch_ptrs(cc_handle program, const uint64_t *input_ptrs, int n_inputs, uint64_t output_ptr,
+                   uint64_t stream);
+
+/* ---- reductions: Tensor.sum -> reduce(PlusPrograms) (Tensors.scala:303-392,
+ *      :673-771).  A fused sum is a kind-1 program run by cc_launch; this is the
+ *      plain sum of n floats at a device address, written to one float at
+ *      `out`.  Scratch (block partials and a completion counter) comes from the
+ *      context's buffer pool. ------------------------------------------------ */
+int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stream);
+
+/* ---- random numbers: Tensor.random / Tensor.randomNormal with the Wang hash
+ *      (Tensors.scala:106-117, :397-524).  normal=0: uniform [0,1]; normal=1:
+ *      Box-Muller pairs (the buffer must hold n rounded up to even floats). -- */
+int cc_random(cc_handle output, size_t n, uint32_t seed, int normal);
+
+/* ---- events: replace Event.waitFor / waitForStatus / release
+ *      (OpenCL.scala:565-611, :1246-1263).  Waits are bounded and return
+ *      CC_ERR_TIMEOUT instead of hanging. ---------------------------------- */
+int cc_event_record(cc_handle *event);
+int cc_event_query(cc_handle event, int *complete);
+int cc_event_wait(cc_handle event, uint64_t timeout_ns);
+int cc_event_elapsed(cc_handle start, cc_handle end, float *ms);
+int cc_event_release(cc_handle event);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COMPUTE_CUDA_H */

@@ -1,0 +1,89 @@
+"""The C ABI library: loads without a GPU, exports every declared entry point,
+and its GPU-free entry points generate and compile the fused kernels."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from compute import _native
+from compute.runtime import codegen, compile_check
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            names += re.findall(r"^int\s+(cc_\w+)\s*\(", text, flags=re.M)
+    return names
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = _native.load()
+    names = declared_functions()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _native._SIGNATURES, "no ctypes signature for " + n
+
+
+def test_init_without_gpu_fails_cleanly():
+    lib = _native.load()
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    st = lib.cc_init(0, 0)
+    assert st == -1  # CC_ERR_DEVICE_NOT_FOUND
+    assert "CUDA" in _native.last_error() or "device" in _native.last_error()
+
+
+C2_SMALL = None
+
+
+def c2_ir():
+    from compute import Tensors
+    d = Tensors(runtime=object())
+    T = d.Tensor
+    x = T.randomNormal([2, 8, 5, 5], seed=0)
+    bias = (T.randomNormal([8], seed=1) * T.fill(0.1, [8])).reshape([1, 1, 1, 8])
+    y = T.max(x.permute([0, 2, 3, 1]) + bias.broadcast([2, 5, 5, 8]), T.fill(0.0, [2, 5, 5, 8]))
+    s = y.translate([0, 0, 1, 0]).split(3).reduce(lambda a, b: a + b)
+    return d.serialize(s.closure, s.shape).text
+
+
+def test_codegen_and_nvrtc_compile_for_sm103a():
+    ir = c2_ir()
+    src = codegen(ir)
+    assert "cc_ew" in src and "__launch_bounds__" in src
+    compile_check(ir, (10, 3))
+    compile_check(ir.replace("ccir 1 ew", "ccir 1 sum"), (10, 3))
+
+
+def test_contiguous_programs_get_a_float4_variant():
+    ir = "ccir 1 sum\no 1 100\np 1 100 00000000\nx 0 2 1 0\np 1 100 00000000\nx 2 2 1 0\nb mul 1 3\nu tanh 4\nr 5\n"
+    src = codegen(ir)
+    assert "cc_sum_v4" in src and "float4" in src
+    compile_check(ir)
+
+
+def test_invalid_ir_is_rejected():
+    with pytest.raises(_native.InvalidProgram):
+        codegen("ccir 1 ew\no 1 4\nb add 0 1\nr 0\n")
+    with pytest.raises(_native.InvalidProgram):
+        codegen("not an ir")
+    with pytest.raises(_native.InvalidProgram):
+        codegen("ccir 1 ew\no 1 4\np 1 4 00000000\nx 0 3 1 0 0\nr 1\n")  # matrix/frame mismatch
+
+
+def test_compile_failure_carries_the_nvrtc_log():
+    ir = "ccir 1 ew\no 1 4\nl 3f800000\nr 0\n"
+    with pytest.raises(_native.BuildProgramFailure) as e:
+        compile_check(ir, (1, 0))
+    assert "NVRTC" in str(e.value)
