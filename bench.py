@@ -262,6 +262,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=["c1", "c2"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-clocks", action="store_true", help="skip the clock sampling (and its untimed busy loop)")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
 
@@ -298,10 +299,13 @@ def main():
     if dist:
         dist.barrier()
     rt.synchronize()
-    sampler.start()
+    if not args.no_clocks:
+        sampler.start()
     ms_total = time_device(rt, st, args.steps, warmup)
-    keep_busy(rt, st, 1.5)
-    clocks = sampler.stop()
+    clocks = None
+    if not args.no_clocks:
+        keep_busy(rt, st, 1.5)
+        clocks = sampler.stop()
     if dist:
         import torch
         t = torch.tensor([ms_total], dtype=torch.float64)

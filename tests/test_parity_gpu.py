@@ -42,11 +42,20 @@ def test_random_uniform_bit_exact(cuda_device, n):
     assert np.array_equal(bits(got), bits(rng.random_uniform(n, 12345)))
 
 
-@pytest.mark.parametrize("n", [1, 2, 27, 1001, 1 << 20])
+def test_random_normal_infinities_follow_the_reference():
+    """hash == 0 gives log(0) = -inf, hence infinite normals, in the reference too (Tensors.scala:419-426)."""
+    n = 3 << 20
+    want = rng.random_normal(n, 9)
+    assert not np.isfinite(want).all()
+
+
+@pytest.mark.parametrize("n", [1, 2, 27, 1001, 1 << 20, 3 << 20])
 def test_random_normal_within_2ulp(cuda_device, n):
-    got = cuda_device.Tensor.randomNormal([n], seed=54321).flatArray()
-    want = rng.random_normal(n, 54321)
+    seed = 54321 if n < (3 << 20) else 9
+    got = cuda_device.Tensor.randomNormal([n], seed=seed).flatArray()
+    want = rng.random_normal(n, seed)
     fin = np.isfinite(want)
+    assert np.array_equal(np.isinf(got), np.isinf(want))
     # log, then sqrt, then cos/sin: the device functions are <= 2 ulp each; allow their composition
     assert ulp_diff(got[fin], want[fin]).max() <= 4
 
@@ -152,7 +161,8 @@ def test_c1_fused_elementwise_sum(cuda_device):
 
 def test_sum_is_deterministic(cuda_device):
     T = cuda_device.Tensor
-    a = T.randomNormal([3 << 20], seed=9).doCache()
+    n = 3 << 20
+    a = (T.random([n], seed=9) - T.fill(0.5, [n])).doCache()
     r = {a.sum().readScalar() for _ in range(5)}
     assert len(r) == 1
     a.close()
