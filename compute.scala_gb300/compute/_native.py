@@ -138,6 +138,7 @@ _SIGNATURES = {
     "cc_launch": [c_handle, ctypes.POINTER(c_handle), ctypes.c_int, c_handle],
     "cc_launch_ptrs": [c_handle, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64],
     "cc_reduce_sum_f32": [ctypes.c_uint64, c_size, ctypes.c_uint64, ctypes.c_uint64],
+    "cc_reduce_sum_f32_noalloc": [ctypes.c_uint64, c_size, ctypes.c_uint64, ctypes.c_uint64],
     "cc_random": [c_handle, c_size, ctypes.c_uint32, ctypes.c_int],
     "cc_event_record": [ctypes.POINTER(c_handle)],
     "cc_event_query": [c_handle, ctypes.POINTER(ctypes.c_int)],

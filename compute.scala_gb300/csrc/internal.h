@@ -21,6 +21,9 @@ struct Error {
 
 [[noreturn]] void fail(int code, const std::string &message);
 
+// Stores `message` as the calling thread's last error (what cc_last_error returns).
+void record_error(const std::string &message);
+
 // Driver API functions the runtime uses, resolved at cc_init through
 // cudaGetDriverEntryPointByVersion (the library itself does not link libcuda).
 struct Driver {

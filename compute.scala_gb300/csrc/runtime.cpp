@@ -33,6 +33,8 @@ thread_local std::string t_last_error;
 
 void fail(int code, const std::string &message) { throw Error{code, message}; }
 
+void record_error(const std::string &message) { t_last_error = message; }
+
 // Driver API entry points, resolved through the CUDA runtime at cc_init so the
 // library loads (and its GPU-free entry points work) on hosts without a driver.
 Driver g_drv;

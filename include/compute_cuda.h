@@ -126,6 +126,27 @@ int cc_launch_ptrs(cc_handle program, const uint64_t *input_ptrs, int n_inputs, 
  *      context's buffer pool. ------------------------------------------------ */
 int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stream);
 
+/* The same sum for callers that cannot allocate device memory.  It has no
+ * counterpart in the reference.  Some callers cannot call cudaMalloc (or
+ * cc_init, whose pool does): a host framework that has already reserved the
+ * device's memory for its own allocator and forbids side allocations, or a
+ * latency-critical caller that cannot accept cudaMalloc's device-wide
+ * synchronisation.  This entry point allocates nothing: its scratch (one
+ * compensated partial per block and a completion counter, 128 KiB + 256 B) is a
+ * fixed array in device memory that every GPU loading this library holds until
+ * the process exits.  It needs no cc_init and runs on the calling thread's
+ * current device; in_ptr and out_ptr must be on that device, and stream 0 is
+ * that device's default stream.
+ *   - n may be at most 134,217,728 floats (16384 blocks of 8192); larger n is
+ *     rejected with CC_ERR_INVALID_VALUE and nothing is launched.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Every call shares the one array, which keeps the last call's contents:
+ *     each call zeroes the counter on `stream` first, so calls ordered on one
+ *     stream are safe, but calls that can overlap on the GPU (on different
+ *     streams of one device) race and give wrong sums. */
+int cc_reduce_sum_f32_noalloc(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stream);
+
 /* ---- random numbers: Tensor.random / Tensor.randomNormal with the Wang hash
  *      (Tensors.scala:106-117, :397-524).  normal=0: uniform [0,1]; normal=1:
  *      Box-Muller pairs (the buffer must hold n rounded up to even floats). -- */

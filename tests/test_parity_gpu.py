@@ -171,7 +171,8 @@ def test_sum_is_deterministic(cuda_device):
 def test_plain_sum_entry_point(cuda_device):
     T = cuda_device.Tensor
     rt = cuda_device.runtime
-    a = T.randomNormal([(1 << 20) + 3], seed=11).doCache()
+    n = (1 << 20) + 3
+    a = (T.random([n], seed=11) - T.fill(0.5, [n])).doCache()
     ev = a._cached
     out = rt.alloc(4)
     for off in (0, 1):  # aligned (float4 loads) and misaligned (scalar loads)
