@@ -114,6 +114,8 @@ _SIGNATURES = {
     "cc_get_stream": [ctypes.POINTER(ctypes.c_uint64)],
     "cc_set_stream": [ctypes.c_uint64],
     "cc_synchronize": [],
+    "cc_config_set": [ctypes.c_char_p, ctypes.c_int64],
+    "cc_config_get": [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)],
     "cc_buf_alloc": [c_size, ctypes.POINTER(c_handle)],
     "cc_buf_retain": [c_handle],
     "cc_buf_release": [c_handle],
@@ -140,6 +142,9 @@ _SIGNATURES = {
     "cc_reduce_sum_f32": [ctypes.c_uint64, c_size, ctypes.c_uint64, ctypes.c_uint64],
     "cc_reduce_sum_f32_noalloc": [ctypes.c_uint64, c_size, ctypes.c_uint64, ctypes.c_uint64],
     "cc_random": [c_handle, c_size, ctypes.c_uint32, ctypes.c_int],
+    "cc_gemm_f32": [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                    ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64],
+    "cc_device_errors": [ctypes.POINTER(ctypes.c_int)],
     "cc_event_record": [ctypes.POINTER(c_handle)],
     "cc_event_query": [c_handle, ctypes.POINTER(ctypes.c_int)],
     "cc_event_wait": [c_handle, ctypes.c_uint64],

@@ -78,6 +78,16 @@ class NativeRuntime:
     def synchronize(self):
         call("cc_synchronize")
 
+    def config_set(self, key: str, value: int):
+        """Sets a runtime tuning knob; programs are compiled again under the new setting."""
+        call("cc_config_set", key.encode(), ctypes.c_int64(int(value)))
+        self._programs.clear()
+
+    def config_get(self, key: str) -> int:
+        v = ctypes.c_int64()
+        call("cc_config_get", key.encode(), ctypes.byref(v))
+        return v.value
+
     # -- buffers
     def alloc(self, nbytes: int) -> DeviceBuffer:
         h = c_handle()
@@ -142,6 +152,19 @@ class NativeRuntime:
     def reduce_sum_ptr(self, in_ptr: int, n: int, out_ptr: int, stream: int = 0):
         call("cc_reduce_sum_f32", ctypes.c_uint64(in_ptr), ctypes.c_size_t(int(n)), ctypes.c_uint64(out_ptr),
              ctypes.c_uint64(stream))
+
+    GEMM_EXACT, GEMM_FP32, GEMM_BF16X6 = 0, 1, 2
+
+    def gemm_ptr(self, a_ptr: int, b_ptr: int, c_ptr: int, m: int, n: int, k: int, mode: int,
+                 lda: int = None, ldb: int = None, ldc: int = None, stream: int = 0):
+        call("cc_gemm_f32", ctypes.c_uint64(a_ptr), ctypes.c_uint64(b_ptr), ctypes.c_uint64(c_ptr), int(m), int(n),
+             int(k), ctypes.c_int64(k if lda is None else lda), ctypes.c_int64(n if ldb is None else ldb),
+             ctypes.c_int64(n if ldc is None else ldc), int(mode), ctypes.c_uint64(stream))
+
+    def device_errors(self) -> int:
+        v = ctypes.c_int()
+        call("cc_device_errors", ctypes.byref(v))
+        return v.value
 
     # -- events
     def event(self) -> int:

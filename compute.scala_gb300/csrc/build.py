@@ -21,7 +21,7 @@ BUILD = os.path.normpath(os.path.join(HERE, "..", "_build"))
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SOURCES = ["runtime.cpp", "codegen.cpp"]
-DEVICE_SOURCES = ["kernels.cu", "noalloc.cu"]
+DEVICE_SOURCES = ["kernels.cu", "noalloc.cu", "gemm.cu", "gemm_tc.cu"]
 LIB_NAME = "libcomputecuda.so"
 
 

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <sstream>
 #include <utility>
@@ -247,46 +248,57 @@ struct Frame {
   std::vector<int64_t> shape;
 };
 
+// One generated statement.  Index statements are integer view arithmetic (they
+// depend only on coordinates), loads read a buffer, computes are float ops.
+enum class Cat : uint8_t { Index, Prefetch, Load, Compute };
+struct Stmt {
+  Cat cat;
+  std::string text;
+};
+
 class Generator {
  public:
-  Generator(const Ir &ir, bool contiguous_mode) : ir_(ir), contig_(contiguous_mode) {}
+  Generator(const Ir &ir, bool contiguous_mode, bool asm_loads = false, int64_t prefetch_min_bytes = -1)
+      : ir_(ir), contig_(contiguous_mode), asm_loads_(asm_loads), prefetch_min_bytes_(prefetch_min_bytes) {}
 
-  // Returns the name of the variable holding node `n` evaluated in frame `f`.
-  std::string gen(int n, const Frame &f, std::ostringstream &os, int ind) {
+  // Returns the name of the variable holding node `n` evaluated in frame `f`;
+  // the statements computing it are appended to the statement list.
+  std::string gen(int n, const Frame &f) {
     auto key = std::make_pair(n, f.id);
     auto it = memo_.find(key);
     if (it != memo_.end()) return it->second;
     const IrNode &node = ir_.nodes[n];
-    std::string pad(ind, ' ');
     std::string v;
     switch (node.kind) {
       case NodeKind::Literal:
         v = fresh();
-        os << pad << "const float " << v << " = " << lit_code(node.bits) << ";\n";
+        add(Cat::Compute, "const float " + v + " = " + lit_code(node.bits) + ";");
         break;
       case NodeKind::Unary: {
-        std::string a = gen(node.a, f, os, ind);
+        std::string a = gen(node.a, f);
         v = fresh();
         static const char *fn[] = {"-", "expf", "logf", "tanhf", "fabsf", "sqrtf"};
         if (node.op == (uint8_t)UnOp::Neg)
-          os << pad << "const float " << v << " = -" << a << ";\n";
+          add(Cat::Compute, "const float " + v + " = -" + a + ";");
         else
-          os << pad << "const float " << v << " = " << fn[node.op] << "(" << a << ");\n";
+          add(Cat::Compute, "const float " + v + " = " + fn[node.op] + "(" + a + ");");
         break;
       }
       case NodeKind::Binary: {
-        std::string a = gen(node.a, f, os, ind);
-        std::string b = gen(node.b, f, os, ind);
+        std::string a = gen(node.a, f);
+        std::string b = gen(node.b, f);
         v = fresh();
+        std::string e;
         switch ((BinOp)node.op) {
-          case BinOp::Add: os << pad << "const float " << v << " = " << a << " + " << b << ";\n"; break;
-          case BinOp::Sub: os << pad << "const float " << v << " = " << a << " - " << b << ";\n"; break;
-          case BinOp::Mul: os << pad << "const float " << v << " = " << a << " * " << b << ";\n"; break;
-          case BinOp::Div: os << pad << "const float " << v << " = " << a << " / " << b << ";\n"; break;
-          case BinOp::Mod: os << pad << "const float " << v << " = fmodf(" << a << ", " << b << ");\n"; break;
-          case BinOp::Min: os << pad << "const float " << v << " = fminf(" << a << ", " << b << ");\n"; break;
-          case BinOp::Max: os << pad << "const float " << v << " = fmaxf(" << a << ", " << b << ");\n"; break;
+          case BinOp::Add: e = a + " + " + b; break;
+          case BinOp::Sub: e = a + " - " + b; break;
+          case BinOp::Mul: e = a + " * " + b; break;
+          case BinOp::Div: e = a + " / " + b; break;
+          case BinOp::Mod: e = "fmodf(" + a + ", " + b + ")"; break;
+          case BinOp::Min: e = "fminf(" + a + ", " + b + ")"; break;
+          case BinOp::Max: e = "fmaxf(" + a + ", " + b + ")"; break;
         }
+        add(Cat::Compute, "const float " + v + " = " + e + ";");
         break;
       }
       case NodeKind::Extract: {
@@ -295,38 +307,48 @@ class Generator {
           fail(CC_ERR_INVALID_PROGRAM, "IR: view matrix columns do not match the frame rank");
         v = fresh();
         if (contig_) {
-          os << pad << "const float " << v << " = a" << p.param_index << ";\n";
+          add(Cat::Compute, "const float " + v + " = a" + std::to_string(p.param_index) + ";");
           break;
         }
         std::vector<std::string> idx;
-        std::string ok = index_rows(node, p.dims, f, os, ind, idx);
+        std::string ok = index_rows(node, p.dims, f, idx);
         std::string off = offset_expr(p.dims, idx);
-        std::string load = "__ldg(in" + std::to_string(p.param_index) + " + " + off + ")";
-        if (p.dims.empty()) load = "__ldg(in" + std::to_string(p.param_index) + ")";
-        if (ok.empty())
-          os << pad << "const float " << v << " = " << load << ";\n";
-        else
-          os << pad << "const float " << v << " = (" << ok << ") ? " << load << " : " << lit_code(p.bits) << ";\n";
+        std::string ptr = "in" + std::to_string(p.param_index) + (p.dims.empty() ? "" : " + " + off);
+        if (prefetch_min_bytes_ >= 0) {
+          int64_t bytes = 4;
+          for (int64_t d : p.dims) bytes *= d;
+          if (bytes >= prefetch_min_bytes_)
+            add(Cat::Prefetch, "cc_prefetch(" + ptr + ", " + (ok.empty() ? std::string("1") : "(" + ok + ")") + ");");
+        }
+        if (asm_loads_) {
+          // A predicated non-coherent load in volatile inline PTX: the compiler
+          // keeps these in the order emit() places them, so the lookahead holds.
+          add(Cat::Load, "float " + v + " = " + lit_code(p.bits) + "; cc_ld(" + v + ", " + ptr + ", " +
+                             (ok.empty() ? std::string("1") : "(" + ok + ")") + ");");
+        } else if (ok.empty()) {
+          add(Cat::Load, "const float " + v + " = __ldg(" + ptr + ");");
+        } else {
+          add(Cat::Load, "const float " + v + " = (" + ok + ") ? __ldg(" + ptr + ") : " + lit_code(p.bits) + ";");
+        }
         break;
       }
       case NodeKind::View: {
+        // An inline tensor evaluated at view coordinates.  Its expression is
+        // evaluated unconditionally and the padding selected afterwards: every
+        // load inside carries its own bounds check, so coordinates outside the
+        // view cannot read outside a buffer, and the code stays straight-line,
+        // so the loads of many views can be scheduled ahead together.
         if (node.cols != (int)f.shape.size() + 1)
           fail(CC_ERR_INVALID_PROGRAM, "IR: view matrix columns do not match the frame rank");
         v = fresh();
         std::vector<std::string> idx;
-        std::string ok = index_rows(node, node.dims, f, os, ind, idx);
+        std::string ok = index_rows(node, node.dims, f, idx);
         Frame inner{next_frame_++, idx, node.dims};
-        os << pad << "float " << v << ";\n";
-        if (!ok.empty()) {
-          os << pad << "if (" << ok << ") {\n";
-          std::string sub = gen(node.a, inner, os, ind + 2);
-          os << pad << "  " << v << " = " << sub << ";\n";
-          os << pad << "} else {\n" << pad << "  " << v << " = " << lit_code(node.bits) << ";\n" << pad << "}\n";
-        } else {
-          os << pad << "{\n";
-          std::string sub = gen(node.a, inner, os, ind + 2);
-          os << pad << "  " << v << " = " << sub << ";\n" << pad << "}\n";
-        }
+        std::string sub = gen(node.a, inner);
+        if (!ok.empty())
+          add(Cat::Compute, "const float " + v + " = (" + ok + ") ? " + sub + " : " + lit_code(node.bits) + ";");
+        else
+          add(Cat::Compute, "const float " + v + " = " + sub + ";");
         break;
       }
       case NodeKind::Param:
@@ -338,17 +360,49 @@ class Generator {
     return v;
   }
 
+  // Writes the statements in an order the hardware likes: all index arithmetic
+  // first, then each load `lookahead` loads ahead of the arithmetic that uses
+  // it, so a thread keeps that many independent loads in flight while the
+  // float statements still execute in the tree's order.
+  void emit(std::ostringstream &os, int ind, int lookahead) const {
+    std::string pad(ind, ' ');
+    std::vector<size_t> loads;
+    for (size_t i = 0; i < stmts_.size(); ++i) {
+      if (stmts_[i].cat == Cat::Index) os << pad << stmts_[i].text << "\n";
+      if (stmts_[i].cat == Cat::Load) loads.push_back(i);
+    }
+    for (size_t i = 0; i < stmts_.size(); ++i)
+      if (stmts_[i].cat == Cat::Prefetch) os << pad << stmts_[i].text << "\n";
+    size_t emitted = 0, seen = 0;
+    auto emit_loads_to = [&](size_t n) {
+      if (n > loads.size()) n = loads.size();
+      while (emitted < n) os << pad << stmts_[loads[emitted++]].text << "\n";
+    };
+    for (size_t i = 0; i < stmts_.size(); ++i) {
+      const Stmt &s = stmts_[i];
+      if (s.cat == Cat::Index || s.cat == Cat::Prefetch) continue;
+      if (s.cat == Cat::Load) {
+        ++seen;
+        emit_loads_to(seen);
+        continue;
+      }
+      emit_loads_to(seen + (size_t)(lookahead > 0 ? lookahead : 0));
+      os << pad << s.text << "\n";
+    }
+    emit_loads_to(loads.size());
+  }
+
   bool uses_fp64() const { return fp64_; }
 
  private:
   std::string fresh() { return "_" + std::to_string(next_var_++); }
+  void add(Cat c, std::string t) { stmts_.push_back(Stmt{c, std::move(t)}); }
 
-  // Emits one index variable per source dimension, the way ArrayView.extract
-  // does (OpenCLKernelBuilder.scala:348-411); returns the bounds condition
-  // ("" when every row is constant-zero and no check applies).
+  // One index variable per source dimension, the way ArrayView.extract
+  // computes it (OpenCLKernelBuilder.scala:348-411); returns the bounds
+  // condition ("" when every row is constant-zero and no check applies).
   std::string index_rows(const IrNode &node, const std::vector<int64_t> &dims, const Frame &f,
-                         std::ostringstream &os, int ind, std::vector<std::string> &idx) {
-    std::string pad(ind, ' ');
+                         std::vector<std::string> &idx) {
     const int rows = (int)dims.size();
     const int cols = node.cols;
     std::string ok;
@@ -369,10 +423,10 @@ class Generator {
       }
       std::string name = "_i" + std::to_string(next_var_++);
       if (!any) {
-        os << pad << "const int " << name << " = 0;\n";
+        add(Cat::Index, "const int " + name + " = 0;");
         if (dims[y] == 0) ok += std::string(ok.empty() ? "" : " && ") + "false";
       } else {
-        os << pad << "const int " << name << " = (int)(" << sum << ");\n";
+        add(Cat::Index, "const int " + name + " = (int)(" + sum + ");");
         ok += std::string(ok.empty() ? "" : " && ") + "(" + name + " >= 0) && (" + name + " < " +
               std::to_string(dims[y]) + ")";
       }
@@ -402,10 +456,13 @@ class Generator {
 
   const Ir &ir_;
   bool contig_;
+  bool asm_loads_;
+  int64_t prefetch_min_bytes_;
   bool fp64_ = false;
   int next_var_ = 0;
   int next_frame_ = 1;
   std::map<std::pair<int, int>, std::string> memo_;
+  std::vector<Stmt> stmts_;
 };
 
 bool is_contiguous_identity(const IrNode &x, const IrNode &p, const std::vector<int64_t> &out_shape) {
@@ -420,6 +477,17 @@ bool is_contiguous_identity(const IrNode &x, const IrNode &p, const std::vector<
 }
 
 }  // namespace
+
+int choose_min_blocks(int64_t domain, int block, int sm_count, int override_blocks) {
+  if (override_blocks > 0) return override_blocks;
+  if (sm_count <= 0) return 0;
+  const int64_t blocks = (domain + block - 1) / block;
+  const int64_t per_sm = (blocks + sm_count - 1) / sm_count;
+  int64_t max_per_sm = 2048 / block;
+  if (max_per_sm > 32) max_per_sm = 32;  // resident blocks per SM
+  if (per_sm <= max_per_sm) return (int)(per_sm < 1 ? 1 : per_sm);
+  return 4;
+}
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   Generated g;
@@ -462,13 +530,16 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   };
 
   const std::string block = std::to_string(opt.block);
+  // launch bounds of the generic kernels (see choose_min_blocks)
+  const std::string lb = opt.min_blocks > 0 ? block + ", " + std::to_string(opt.min_blocks) : block;
   bool fp64 = false;
 
   if (contiguous) {
     // The point function of the contiguous form: parameter values in, result out.
     Generator gen(ir, true);
     std::ostringstream body;
-    std::string r = gen.gen(ir.root, f0, body, 2);
+    std::string r = gen.gen(ir.root, f0);
+    gen.emit(body, 2, 0);
     fp64 |= gen.uses_fp64();
     src << "__device__ __forceinline__ float cc_point(";
     for (int i = 0; i < ir.n_params; ++i) src << (i ? ", " : "") << "float a" << i;
@@ -480,13 +551,14 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   std::ostringstream generic;
   std::vector<std::string> results;
   {
-    Generator gen(ir, false);
+    Generator gen(ir, false, opt.asm_loads, opt.prefetch_min_bytes);
     decode(generic, 4);
     if (root.kind == NodeKind::Tuple) {
-      for (int e : root.elems) results.push_back(gen.gen(e, f0, generic, 4));
+      for (int e : root.elems) results.push_back(gen.gen(e, f0));
     } else {
-      results.push_back(gen.gen(ir.root, f0, generic, 4));
+      results.push_back(gen.gen(ir.root, f0));
     }
+    gen.emit(generic, 4, opt.load_lookahead);
     fp64 |= gen.uses_fp64();
   }
   g.uses_fp64_index = fp64;
@@ -498,8 +570,56 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     return s + ")";
   };
 
+  // The float4 loop: each thread takes U float4 positions `stride` apart, loads
+  // all of them from every input first (U * inputs loads in flight), then
+  // computes; leftover positions and the last n % 4 floats follow one at a time.
+  const int U = opt.vec_unroll > 0 ? opt.vec_unroll : 1;
+  g.vec_unroll = U;
+  auto vec4_loop = [&](int nin, int u_count, bool store, const std::function<std::string(const std::string &)> &call) {
+    std::ostringstream o;
+    o << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+      << "  const cc_i64 n4 = n >> 2;\n"
+      << "  cc_i64 q = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x;\n"
+      << "  for (; q + " << (u_count - 1) << " * stride < n4; q += " << u_count << " * stride) {\n";
+    for (int u = 0; u < u_count; ++u)
+      for (int i = 0; i < nin; ++i)
+        o << "    const float4 v" << i << "_" << u << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q + "
+          << u << " * stride);\n";
+    for (int u = 0; u < u_count; ++u) {
+      auto lane_call = [&](const char *lane) {
+        std::string c = "cc_point(";
+        for (int i = 0; i < nin; ++i) c += (i ? ", " : "") + std::string("v") + std::to_string(i) + "_" + std::to_string(u) + lane;
+        return c + ")";
+      };
+      if (store) {
+        o << "    {\n      float4 r;\n";
+        for (const char *lane : {".x", ".y", ".z", ".w"}) o << "      r" << lane << " = " << lane_call(lane) << ";\n";
+        o << "      reinterpret_cast<float4 *>(out)[q + " << u << " * stride] = r;\n    }\n";
+      } else {
+        for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    cc_acc(s_, c_, " << lane_call(lane) << ");\n";
+      }
+    }
+    o << "  }\n  for (; q < n4; q += stride) {\n";
+    for (int i = 0; i < nin; ++i)
+      o << "    const float4 v" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
+    if (store) {
+      o << "    float4 r;\n";
+      for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    r" << lane << " = " << call(lane) << ";\n";
+      o << "    reinterpret_cast<float4 *>(out)[q] = r;\n";
+    } else {
+      for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    cc_acc(s_, c_, " << call(lane) << ");\n";
+    }
+    o << "  }\n  for (cc_i64 lin = (n4 << 2) + (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n";
+    for (int i = 0; i < nin; ++i) o << "    const float v" << i << " = __ldg(in" << i << " + lin);\n";
+    if (store)
+      o << "    out[lin] = " << call("") << ";\n  }\n";
+    else
+      o << "    cc_acc(s_, c_, " << call("") << ");\n  }\n";
+    return o.str();
+  };
+
   if (ir.kind == ProgramKind::Elementwise) {
-    src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_ew(" << params
+    src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_ew(" << params
         << "float *__restrict__ out, cc_i64 n) {\n"
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
@@ -514,20 +634,10 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     if (contiguous) {
       src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_ew_v4(" << params
           << "float *__restrict__ out, cc_i64 n) {\n"
-          << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
-          << "  const cc_i64 n4 = n >> 2;\n"
-          << "  for (cc_i64 q = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {\n";
-      for (int i = 0; i < ir.n_params; ++i)
-        src << "    const float4 v" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
-      src << "    float4 r;\n";
-      for (const char *lane : {".x", ".y", ".z", ".w"}) src << "    r" << lane << " = " << contig_call(lane) << ";\n";
-      src << "    reinterpret_cast<float4 *>(out)[q] = r;\n  }\n"
-          << "  for (cc_i64 lin = (n4 << 2) + (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n";
-      for (int i = 0; i < ir.n_params; ++i) src << "    const float v" << i << " = __ldg(in" << i << " + lin);\n";
-      src << "    out[lin] = " << contig_call("") << ";\n  }\n}\n\n";
+          << vec4_loop(ir.n_params, U, true, contig_call) << "}\n\n";
     }
   } else {
-    src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum(" << params
+    src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_sum(" << params
         << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
         << "  float s_ = 0.0f, c_ = 0.0f;\n"
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
@@ -538,16 +648,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
       src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum_v4(" << params
           << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
           << "  float s_ = 0.0f, c_ = 0.0f;\n"
-          << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
-          << "  const cc_i64 n4 = n >> 2;\n"
-          << "  for (cc_i64 q = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {\n";
-      for (int i = 0; i < ir.n_params; ++i)
-        src << "    const float4 v" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
-      for (const char *lane : {".x", ".y", ".z", ".w"}) src << "    cc_acc(s_, c_, " << contig_call(lane) << ");\n";
-      src << "  }\n"
-          << "  for (cc_i64 lin = (n4 << 2) + (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n";
-      for (int i = 0; i < ir.n_params; ++i) src << "    const float v" << i << " = __ldg(in" << i << " + lin);\n";
-      src << "    cc_acc(s_, c_, " << contig_call("") << ");\n  }\n"
+          << vec4_loop(ir.n_params, U, false, contig_call)
           << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
     }
   }

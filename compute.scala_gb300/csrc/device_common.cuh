@@ -76,3 +76,21 @@ __device__ __forceinline__ void cc_grid_finish(float s, float c, float2 *__restr
     *counter = 0u;
   }
 }
+
+// Predicated read-only load that stays where the code generator put it: the
+// value keeps its initial contents (the padding) when `ok` is false, and no
+// memory is touched then.
+__device__ __forceinline__ void cc_ld(float &v, const float *p, int ok) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %2, 0;\n @q ld.global.nc.f32 %0, [%1];\n}\n"
+      : "+f"(v)
+      : "l"(p), "r"(ok));
+}
+
+// L2 prefetch of the line holding *p, skipped when `ok` is false (so no
+// address outside a buffer is ever touched).  It needs no register, so a
+// thread can have all of its future loads' lines requested at once.
+__device__ __forceinline__ void cc_prefetch(const float *p, int ok) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %1, 0;\n @q prefetch.global.L2 [%0];\n}\n" ::"l"(p), "r"(ok));
+}

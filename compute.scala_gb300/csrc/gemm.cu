@@ -1,0 +1,201 @@
+// Contraction kernels on the CUDA cores, and the operand split for the tensor cores.
+//
+// The reference multiplies matrices as a broadcast product followed by a
+// left-fold of `split(1)` views (Tensors/src/test/scala/com/thoughtworks/
+// compute/TensorsSpec.scala:468-485, README.md:311-343):
+//   C[i][k] = ((A[i][0]*B[0][k] + A[i][1]*B[1][k]) + A[i][2]*B[2][k]) + ...
+// with every product and every sum rounded to float.
+//
+// sgemm_kernel<kExact=true> keeps exactly that order per output (the k loop is
+// sequential in every thread, products and sums rounded separately), so it is
+// bit-identical to the reference's result.  sgemm_kernel<false> is the plain
+// FP32 CUDA-core GEMM with fused multiply-adds.  split_planes_kernel prepares
+// the three-way BF16 split the tensor-core kernel (gemm_tc.cu) consumes.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gemm.h"
+
+namespace cc {
+namespace {
+
+constexpr int kTile = 128;  // block tile (rows and columns)
+constexpr int kTk = 8;      // k per smem stage
+
+// One 128x128 output tile per block of 256 threads; each thread owns an 8x8
+// sub-tile made of rows {ty*4+r, 64+ty*4+r} and columns {tx*4+c, 64+tx*4+c}.
+template <bool kExact>
+__global__ void __launch_bounds__(256) sgemm_kernel(const float *__restrict__ A, const float *__restrict__ B,
+                                                    float *__restrict__ C, int M, int N, int K, long long lda,
+                                                    long long ldb, long long ldc) {
+  __shared__ float As[2][kTk][kTile + 4];
+  __shared__ float Bs[2][kTk][kTile + 4];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int bm = blockIdx.y * kTile, bn = blockIdx.x * kTile;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+
+  // global -> register staging: A: row tid/2, k (tid%2)*4..+3; B: k-row tid/32, cols (tid%32)*4..+3
+  const int a_r = tid >> 1, a_c = (tid & 1) * 4;
+  const int b_r = tid >> 5, b_c = (tid & 31) * 4;
+  float ra[4], rb[4];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int gr = bm + a_r, gk = k0 + a_c + q;
+      ra[q] = (gr < M && gk < K) ? __ldg(A + gr * lda + gk) : 0.0f;
+      const int gk2 = k0 + b_r, gc = bn + b_c + q;
+      rb[q] = (gk2 < K && gc < N) ? __ldg(B + gk2 * ldb + gc) : 0.0f;
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      As[buf][a_c + q][a_r] = ra[q];
+      Bs[buf][b_r][b_c + q] = rb[q];
+    }
+  };
+  const int ntiles = (K + kTk - 1) / kTk;
+  load(0);
+  store(0);
+  __syncthreads();
+  for (int t = 0; t < ntiles; ++t) {
+    const int buf = t & 1;
+    if (t + 1 < ntiles) load((t + 1) * kTk);
+    const int kcount = (K - t * kTk) < kTk ? (K - t * kTk) : kTk;
+#pragma unroll
+    for (int kk = 0; kk < kTk; ++kk) {
+      if (kk < kcount) {
+        float a[8], b[8];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          a[r] = As[buf][kk][ty * 4 + r];
+          a[4 + r] = As[buf][kk][64 + ty * 4 + r];
+          b[r] = Bs[buf][kk][tx * 4 + r];
+          b[4 + r] = Bs[buf][kk][64 + tx * 4 + r];
+        }
+        const bool first = (t == 0 && kk == 0);
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            if (kExact) {
+              const float p = __fmul_rn(a[i], b[j]);
+              acc[i][j] = first ? p : __fadd_rn(acc[i][j], p);
+            } else {
+              acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+            }
+          }
+      }
+    }
+    if (t + 1 < ntiles) store(buf ^ 1);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int gr = bm + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+    if (gr >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int gc = bn + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+      if (gc < N) C[gr * ldc + gc] = acc[i][j];
+    }
+  }
+}
+
+// x = hi + mid + lo with each part a bfloat16 (round-to-nearest): three 8-bit
+// significands cover float's 24, and each residual is exact in float.
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
+  h = __float2bfloat16_rn(x);
+  const float r1 = __fsub_rn(x, __bfloat162float(h));
+  m = __float2bfloat16_rn(r1);
+  const float r2 = __fsub_rn(r1, __bfloat162float(m));
+  l = __float2bfloat16_rn(r2);
+}
+
+// src: rows x cols floats, row-major with leading dimension ld (or, when
+// transpose, the matrix is read as its transpose: element (r, c) = src[c*ld + r]).
+// dst: three planes of prows x pcols bf16, row-major, zero outside rows x cols.
+__global__ void __launch_bounds__(256) split_planes_kernel(const float *__restrict__ src, long long ld, int rows,
+                                                           int cols, int transpose, __nv_bfloat16 *__restrict__ dst,
+                                                           int prows, int pcols) {
+  const long long plane = (long long)prows * pcols;
+  const long long total = plane;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const int r = (int)(i / pcols), c = (int)(i % pcols);
+    float x = 0.0f;
+    if (r < rows && c < cols) x = transpose ? __ldg(src + (long long)c * ld + r) : __ldg(src + (long long)r * ld + c);
+    __nv_bfloat16 h, m, l;
+    split3(x, h, m, l);
+    dst[i] = h;
+    dst[plane + i] = m;
+    dst[2 * plane + i] = l;
+  }
+}
+
+// Transposing split through shared memory so both the fp32 reads and the bf16
+// writes are coalesced: a 32x32 tile of src (rows = K, cols = N) becomes a
+// 32x32 tile of the planes (rows = N, cols = K).
+__global__ void __launch_bounds__(256) split_planes_t_kernel(const float *__restrict__ src, long long ld, int krows,
+                                                             int ncols, __nv_bfloat16 *__restrict__ dst, int prows,
+                                                             int pcols) {
+  __shared__ float tile[32][33];
+  const long long plane = (long long)prows * pcols;
+  const int k0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int k = k0 + r, n = n0 + tx;
+    tile[r][tx] = (k < krows && n < ncols) ? __ldg(src + (long long)k * ld + n) : 0.0f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int n = n0 + r, k = k0 + tx;
+    if (n < prows && k < pcols) {
+      __nv_bfloat16 h, m, l;
+      split3(tile[tx][r], h, m, l);
+      const long long o = (long long)n * pcols + k;
+      dst[o] = h;
+      dst[plane + o] = m;
+      dst[2 * plane + o] = l;
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_sgemm(const float *A, const float *B, float *C, int M, int N, int K, long long lda, long long ldb,
+                         long long ldc, bool exact, cudaStream_t stream) {
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  if (K <= 0) return cudaErrorInvalidValue;
+  dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
+  if (exact)
+    sgemm_kernel<true><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, lda, ldb, ldc);
+  else
+    sgemm_kernel<false><<<grid, 256, 0, stream>>>(A, B, C, M, N, K, lda, ldb, ldc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split_a(const float *A, long long lda, int M, int K, __nv_bfloat16 *planes, int Mp, int Kp,
+                           int sm_count, cudaStream_t stream) {
+  long long total = (long long)Mp * Kp;
+  long long grid = (total + 255) / 256;
+  if (grid > (long long)sm_count * 16) grid = (long long)sm_count * 16;
+  split_planes_kernel<<<(unsigned)grid, 256, 0, stream>>>(A, lda, M, K, 0, planes, Mp, Kp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split_bt(const float *B, long long ldb, int K, int N, __nv_bfloat16 *planes, int Np, int Kp,
+                            cudaStream_t stream) {
+  dim3 grid((Kp + 31) / 32, (Np + 31) / 32);
+  split_planes_t_kernel<<<grid, 256, 0, stream>>>(B, ldb, K, N, planes, Np, Kp);
+  return cudaGetLastError();
+}
+
+}  // namespace cc

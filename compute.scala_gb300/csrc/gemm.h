@@ -1,0 +1,33 @@
+// Host-side launchers of the contraction kernels (gemm.cu, gemm_tc.cu).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace cc {
+
+// C[M,N] = A[M,K] * B[K,N] on the CUDA cores.  exact: each output is the
+// sequential left fold over k of separately rounded products (the reference's
+// broadcast+split+reduce order); otherwise fused multiply-adds.
+cudaError_t launch_sgemm(const float *A, const float *B, float *C, int M, int N, int K, long long lda, long long ldb,
+                         long long ldc, bool exact, cudaStream_t stream);
+
+// Three bf16 planes (hi, mid, lo) of A[M,K] as Mp x Kp row-major, zero padded.
+cudaError_t launch_split_a(const float *A, long long lda, int M, int K, __nv_bfloat16 *planes, int Mp, int Kp,
+                           int sm_count, cudaStream_t stream);
+// Three bf16 planes of B^T (Np x Kp row-major) from B[K,N], zero padded.
+cudaError_t launch_split_bt(const float *B, long long ldb, int K, int N, __nv_bfloat16 *planes, int Np, int Kp,
+                            cudaStream_t stream);
+
+// Tile sizes of the tensor-core kernel: planes are padded to these multiples
+// (kTcBN covers both tile widths).
+constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 32;
+// Tile width (B^T box rows) of a kernel variant: 0 = 128 columns with two
+// accumulator pairs (the epilogue overlaps the next tile), 1 = 256 columns with one.
+int gemm_tc_box_n(int variant);
+// maps: A planes 0..2 (box 32 x 128), B^T planes 0..2 (box 32 x gemm_tc_box_n), 64-byte swizzle.
+cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
+                               int sm_count, int *err, int variant, cudaStream_t stream);
+
+}  // namespace cc

@@ -1,0 +1,390 @@
+// Split-BF16 contraction on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// C = A * B for float A[M,K], B[K,N].  Each operand is split into three
+// bfloat16 planes (x = hi + mid + lo, gemm.cu) and C accumulates, in FP32 in
+// tensor memory, the six products whose order of magnitude is at least
+// 2^-16 of the leading one: hi*hi, hi*mid, mid*hi, mid*mid, hi*lo, lo*hi.  The
+// dropped products (mid*lo, lo*mid, lo*lo) are below 2^-24 relative.  hi*hi
+// accumulates in one TMEM accumulator and the five small products in a second
+// one, added once in the epilogue: adding a product 2^-8 smaller into the big
+// accumulator would cost up to an ulp of it each time.
+//
+// Kernel structure (one CTA per SM, persistent over 128 x BN output tiles):
+//   warp 0      TMA producer: per k-block of 32, loads the 3 A planes (128x32)
+//               and the 3 B^T planes (BNx32) into a shared-memory ring of
+//               STAGES, 64-byte swizzled, completing on the stage's "full"
+//               mbarrier;
+//   warp 1      allocates 512 TMEM columns (ACC_BUFS pairs of BN-column FP32
+//               accumulators), and one thread issues the 12 tcgen05.mma (6
+//               products x 2 k-steps of 16) per stage, committing to the stage's
+//               "empty" mbarrier and, after a tile's last stage, to the
+//               accumulator pair's "full";
+//   warps 2..5  epilogue: tcgen05.ld both accumulators (each warp reads its own
+//               32-lane quarter of TMEM), add, store to C, release the pair.
+// Every mbarrier wait gives up after kWaitNs of %globaltimer time: it records
+// an error code in *err, raises the CTA's abort flag, and all roles leave their
+// loops, so the CTA still frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gemm.h"
+
+namespace cc {
+namespace {
+
+constexpr int BM = 128, BK = 32;  // BK bf16 = 64 bytes = one 64-byte swizzle row
+constexpr int kAPlaneBytes = BM * BK * 2;  // 8 KiB
+constexpr int kTmemCols = 512;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s
+constexpr int kThreads = 192;
+
+template <int BN, int STAGES, int ACC_BUFS>
+struct TcCfg {
+  static_assert(ACC_BUFS * 2 * BN == kTmemCols, "two accumulators per buffer fill TMEM");
+  static constexpr int kBPlaneBytes = BN * BK * 2;
+  static constexpr int kStageBytes = 3 * kAPlaneBytes + 3 * kBPlaneBytes;
+  // Shared memory after the stage ring (offsets from the 1 KiB-aligned base):
+  // full[STAGES], empty[STAGES], acc_full[ACC_BUFS], acc_empty[ACC_BUFS], drain.
+  static constexpr int kBarOffset = STAGES * kStageBytes;
+  static constexpr int kNumBars = 2 * STAGES + 2 * ACC_BUFS + 1;
+  static constexpr int kTmemSlotOffset = kBarOffset + kNumBars * 8;
+  static constexpr int kAbortOffset = kTmemSlotOffset + 4;
+  static constexpr int kSmemBytes = kAbortOffset + 4 + 1024;  // + slack to align the base to 1 KiB
+  // Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, M=128, N=BN.
+  static constexpr uint32_t kIdesc =
+      (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  static_assert(kSmemBytes <= 232448, "shared memory");
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false (and the error recorded, the abort flag raised) on timeout
+// or when another role has already aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err,
+                                          int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (globaltimer() - t0 > kWaitNs) {
+      atomicCAS(err, 0, code);
+      *abort_flag = 1;
+      return false;
+    }
+    __nanosleep(64);
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+
+// tcgen05 shared-memory descriptor: K-major operand, 64-byte swizzle, 8-row
+// groups 512 bytes apart (SBO), version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);        // start address, 16-byte units
+  d |= (uint64_t)(16u >> 4) << 16;                // leading byte offset (unused for this layout)
+  d |= (uint64_t)(512u >> 4) << 32;               // stride byte offset
+  d |= (uint64_t)1 << 46;                         // descriptor version
+  d |= (uint64_t)4 << 61;                         // SWIZZLE_64B
+  return d;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// The six (A plane, B plane) products, largest first.
+__device__ __constant__ int kProdA[6] = {0, 0, 1, 1, 0, 2};
+__device__ __constant__ int kProdB[6] = {0, 1, 0, 1, 2, 0};
+
+template <int BN, int STAGES, int ACC_BUFS>
+__global__ void __launch_bounds__(kThreads, 1)
+    gemm_bf16x6_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
+                       const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap tb0,
+                       const __grid_constant__ CUtensorMap tb1, const __grid_constant__ CUtensorMap tb2,
+                       float *__restrict__ C, int M, int N, long long ldc, int num_kb, int tiles_n, int num_tiles,
+                       int *err) {
+  using Cfg = TcCfg<BN, STAGES, ACC_BUFS>;
+  constexpr int kStages = STAGES;
+  constexpr int kStageBytes = Cfg::kStageBytes;
+  constexpr int kBPlaneBytes = Cfg::kBPlaneBytes;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const uint32_t base = smem_u32(smem);
+  const uint32_t bar_full = base + Cfg::kBarOffset;            // + 8*s
+  const uint32_t bar_empty = bar_full + 8 * kStages;           // + 8*s
+  const uint32_t bar_accfull = bar_empty + 8 * kStages;        // + 8*a
+  const uint32_t bar_accempty = bar_accfull + 8 * ACC_BUFS;    // + 8*a
+  const uint32_t bar_drain = bar_accempty + 8 * ACC_BUFS;
+  volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(smem + Cfg::kTmemSlotOffset);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + Cfg::kAbortOffset);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(bar_full + 8 * s, 1);
+      mbar_init(bar_empty + 8 * s, 1);
+    }
+    for (int a = 0; a < ACC_BUFS; ++a) {
+      mbar_init(bar_accfull + 8 * a, 1);
+      mbar_init(bar_accempty + 8 * a, 128);
+    }
+    mbar_init(bar_drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32((const void *)tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const CUtensorMap *ta[3] = {&ta0, &ta1, &ta2};
+      const CUtensorMap *tb[3] = {&tb0, &tb1, &tb2};
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      uint32_t fill_parity[kStages];
+      bool filled[kStages];
+#pragma unroll
+      for (int s = 0; s < kStages; ++s) filled[s] = false;
+      for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
+        const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+        for (int kb = 0; kb < num_kb; ++kb) {
+          if (!mbar_wait(bar_empty + 8 * stage, phase ^ 1u, abort_flag, err, 1)) {
+            ok = false;
+            break;
+          }
+          const uint32_t sbase = base + stage * kStageBytes;
+          filled[stage] = true;
+          fill_parity[stage] = phase;
+          mbar_arrive_expect_tx(bar_full + 8 * stage, kStageBytes);
+#pragma unroll
+          for (int p = 0; p < 3; ++p) tma_load_2d(sbase + p * kAPlaneBytes, ta[p], kb * BK, m0, bar_full + 8 * stage);
+#pragma unroll
+          for (int p = 0; p < 3; ++p)
+            tma_load_2d(sbase + 3 * kAPlaneBytes + p * kBPlaneBytes, tb[p], kb * BK, n0, bar_full + 8 * stage);
+          if (++stage == kStages) {
+            stage = 0;
+            phase ^= 1u;
+          }
+        }
+      }
+      // Before the CTA may exit, every load this thread issued must have landed
+      // (a normal run's consumer has already waited for all of them; after an
+      // abort they may still be in flight).  The last fill of each stage
+      // completes the phase of its recorded parity; the wait is bounded.
+      if (!ok) {
+        for (int s = 0; s < kStages; ++s) {
+          if (!filled[s]) continue;
+          const unsigned long long t0 = globaltimer();
+          while (!mbar_try_wait(bar_full + 8 * s, fill_parity[s]) && globaltimer() - t0 < kWaitNs) __nanosleep(64);
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int stage = 0, acc = 0;
+      uint32_t phase = 0, acc_phase = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
+        if (!mbar_wait(bar_accempty + 8 * acc, acc_phase ^ 1u, abort_flag, err, 2)) break;
+        tc_fence_after();
+        const uint32_t d_big = tmem_base + (uint32_t)(acc * 2 * BN);  // hi*hi
+        const uint32_t d_small = d_big + BN;                           // the five small products
+        for (int kb = 0; kb < num_kb; ++kb) {
+          if (!mbar_wait(bar_full + 8 * stage, phase, abort_flag, err, 3)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sbase = base + stage * kStageBytes;
+#pragma unroll
+          for (int k16 = 0; k16 < BK / 16; ++k16) {
+#pragma unroll
+            for (int prod = 0; prod < 6; ++prod) {
+              const uint64_t adesc = smem_desc(sbase + kProdA[prod] * kAPlaneBytes + k16 * 32);
+              const uint64_t bdesc = smem_desc(sbase + 3 * kAPlaneBytes + kProdB[prod] * kBPlaneBytes + k16 * 32);
+              const bool first = prod == 0 ? (kb | k16) == 0 : ((kb | k16) == 0 && prod == 1);
+              mma_bf16(prod == 0 ? d_big : d_small, adesc, bdesc, Cfg::kIdesc, first ? 0u : 1u);
+            }
+          }
+          mma_commit(bar_empty + 8 * stage);  // the stage is free once these MMAs have read it
+          if (++stage == kStages) {
+            stage = 0;
+            phase ^= 1u;
+          }
+        }
+        if (!ok) break;
+        mma_commit(bar_accfull + 8 * acc);  // the accumulator pair is complete
+        if (++acc == ACC_BUFS) {
+          acc = 0;
+          acc_phase ^= 1u;
+        }
+      }
+      // Every MMA this thread issued must be complete before TMEM is freed.
+      mma_commit(bar_drain);
+      const unsigned long long t0 = globaltimer();
+      while (!mbar_try_wait(bar_drain, 0) && globaltimer() - t0 < kWaitNs) __nanosleep(64);
+    }
+    __syncwarp();
+  } else {
+    // Epilogue: warp w reads TMEM lanes 32*(w%4) .. 32*(w%4)+31 (one row each).
+    const int quarter = warp & 3;
+    const int row_in_tile = quarter * 32 + lane;
+    int acc = 0;
+    uint32_t acc_phase = 0;
+    for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
+      if (!mbar_wait(bar_accfull + 8 * acc, acc_phase, abort_flag, err, 4)) break;
+      tc_fence_after();
+      const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+      const int row = m0 + row_in_tile;
+      float *crow = C + (long long)row * ldc;
+#pragma unroll 1
+      for (int chunk = 0; chunk < BN / 32; ++chunk) {
+        float v[32], w[32];
+        const uint32_t lane_base = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * 2 * BN + chunk * 32);
+        tmem_ld32(lane_base, v);
+        tmem_ld32(lane_base + BN, w);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = __fadd_rn(v[j], w[j]);
+        const int col0 = n0 + chunk * 32;
+        if (row < M) {
+          if (col0 + 32 <= N && (ldc & 3) == 0 && ((reinterpret_cast<uintptr_t>(crow) & 15) == 0)) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4)
+              *reinterpret_cast<float4 *>(crow + col0 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (col0 + j < N) crow[col0 + j] = v[j];
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(bar_accempty + 8 * acc);
+      if (++acc == ACC_BUFS) {
+        acc = 0;
+        acc_phase ^= 1u;
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols) : "memory");
+  }
+}
+
+template <int BN, int STAGES, int ACC_BUFS>
+cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc, int sm_count,
+                           int *err, cudaStream_t stream) {
+  using Cfg = TcCfg<BN, STAGES, ACC_BUFS>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+  const int num_tiles = tiles_m * tiles_n;
+  const int num_kb = K_padded / BK;
+  const int grid = num_tiles < sm_count ? num_tiles : sm_count;
+  gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS><<<grid, kThreads, Cfg::kSmemBytes, stream>>>(
+      maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], C, M, N, ldc, num_kb, tiles_n, num_tiles, err);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int gemm_tc_box_n(int variant) { return variant == 1 ? 256 : 128; }
+
+cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
+                               int sm_count, int *err, int variant, cudaStream_t stream) {
+  if (variant == 1) return launch_variant<256, 3, 1>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
+  return launch_variant<128, 4, 2>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
+}
+
+}  // namespace cc

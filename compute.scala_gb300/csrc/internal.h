@@ -38,6 +38,7 @@ struct Driver {
   decltype(&::cuCtxSetCurrent) CtxSetCurrent = nullptr;
   decltype(&::cuFuncSetAttribute) FuncSetAttribute = nullptr;
   decltype(&::cuTensorMapEncodeTiled) TensorMapEncodeTiled = nullptr;
+  decltype(&::cuOccupancyMaxActiveBlocksPerMultiprocessor) OccupancyMaxActiveBlocks = nullptr;
 };
 extern Driver g_drv;
 
@@ -73,7 +74,19 @@ Ir parse_ir(const char *text, size_t len);
 
 struct CodegenOptions {
   int block = 256;
+  int load_lookahead = 8;   // loads kept in flight ahead of the arithmetic (generic kernels)
+  bool asm_loads = true;    // emit those loads as volatile inline PTX so their order holds
+  int min_blocks = 0;       // __launch_bounds__ minimum blocks per SM of the generic kernels (0: none)
+  int vec_unroll = 4;       // float4 positions per thread per batch in the contiguous kernels
+  int64_t prefetch_min_bytes = -1;  // L2-prefetch loads from inputs at least this large (-1: never)
 };
+
+// Minimum resident blocks per SM to request for a generic kernel over `domain`
+// points (one per thread, `block` threads per block) on `sm_count` SMs: the
+// blocks one wave needs when the whole grid fits in one wave, else 4 (the
+// kernel then loops over the domain with a resident grid).  More registers per
+// thread let the compiler keep more loads in flight.
+int choose_min_blocks(int64_t domain, int block, int sm_count, int override_blocks);
 
 struct Generated {
   std::string source;
@@ -83,6 +96,7 @@ struct Generated {
   int64_t out_elems = 0;   // floats written (1 for a sum)
   int64_t domain = 0;      // points evaluated
   bool uses_fp64_index = false;
+  int vec_unroll = 1;      // positions per thread per batch of the float4 variant
 };
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);

@@ -43,7 +43,11 @@ __global__ void __launch_bounds__(256) random_uniform_kernel(float *__restrict__
   }
 }
 
-// Tensors.scala:397-429: one Box-Muller pair per work item.
+// Tensors.scala:397-429: one Box-Muller pair per work item.  Every float step
+// rounds once, as the reference's statements are written; log, cos and sin are
+// taken in double precision and rounded to float once, which gives the
+// correctly rounded float in all but vanishingly rare cases, so the output
+// matches the reference's golden values bit for bit.
 __global__ void __launch_bounds__(256) random_normal_kernel(float2 *__restrict__ out, long long pairs,
                                                             unsigned int seed) {
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -53,9 +57,12 @@ __global__ void __launch_bounds__(256) random_normal_kernel(float2 *__restrict__
     const unsigned int r2 = xorshift(r1);
     const float u1 = unit_float(r1);
     const float u2 = unit_float(r2);
-    const float r = sqrtf(__fmul_rn(-2.0f, logf(u1)));
+    const float lg = (float)log((double)u1);
+    const float r = __fsqrt_rn(__fmul_rn(-2.0f, lg));
     const float theta = __fmul_rn(two_pi, u2);
-    out[i] = make_float2(__fmul_rn(r, cosf(theta)), __fmul_rn(r, sinf(theta)));
+    double sn, cs;
+    sincos((double)theta, &sn, &cs);
+    out[i] = make_float2(__fmul_rn(r, (float)cs), __fmul_rn(r, (float)sn));
   }
 }
 
@@ -107,6 +114,14 @@ int sum_grid(long long work, int sm_count) {
   long long grid = (work + 255) / 256;
   long long cap = (long long)sm_count * 8;
   if (cap > kMaxSumBlocks) cap = kMaxSumBlocks;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  return (int)grid;
+}
+
+int sum_grid_for(long long work, int block, int max_blocks) {
+  long long grid = (work + block - 1) / block;
+  long long cap = max_blocks < kMaxSumBlocks ? max_blocks : kMaxSumBlocks;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
   return (int)grid;

@@ -12,6 +12,8 @@ constexpr int kMaxSumBlocks = 4096;
 cudaError_t launch_random(float *out, long long n, unsigned int seed, int normal, int sm_count,
                           cudaStream_t stream);
 int sum_grid(long long work, int sm_count);
+// Blocks of a grid sum: one element (or float4) per thread, capped at max_blocks.
+int sum_grid_for(long long work, int block, int max_blocks);
 cudaError_t launch_sum(const float *in, long long n, float2 *partials, unsigned int *counter, float *out,
                        int sm_count, cudaStream_t stream);
 

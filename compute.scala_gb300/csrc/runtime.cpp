@@ -22,6 +22,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "gemm.h"
 #include "internal.h"
 #include "kernels.h"
 
@@ -72,6 +73,7 @@ void load_driver() {
   resolve(g_drv.CtxSetCurrent, "cuCtxSetCurrent");
   resolve(g_drv.FuncSetAttribute, "cuFuncSetAttribute");
   resolve(g_drv.TensorMapEncodeTiled, "cuTensorMapEncodeTiled");
+  resolve(g_drv.OccupancyMaxActiveBlocks, "cuOccupancyMaxActiveBlocksPerMultiprocessor");
   g_drv.loaded = true;
 }
 
@@ -172,6 +174,9 @@ struct Program {
   CUmodule module = nullptr;
   CUfunction scalar = nullptr;  // cc_ew / cc_sum
   CUfunction vec4 = nullptr;    // cc_ew_v4 / cc_sum_v4 (contiguous inputs)
+  int block = 256;              // threads per block the kernels were generated for
+  int resident_scalar = 0;      // blocks one SM holds at once, per variant
+  int resident_vec4 = 0;
   ProgramKind kind = ProgramKind::Elementwise;
   Generated gen;
 };
@@ -202,6 +207,20 @@ struct Context {
   uint64_t cache_hits = 0, cache_misses = 0;
   std::mutex compile_mu;
 
+  // Tuning knobs (cc_config_set).
+  int block = 128;
+  int ew_blocks_per_sm = 0;
+  int sum_blocks_per_sm = 4;
+  int upload_streams = 4;
+  int ew_lookahead = 8;
+  int ew_asm_loads = 1;
+  int vec_unroll = 4;
+  int64_t prefetch_min_bytes = -1;
+  int sum_block = 256;
+  int tc_variant = 1;
+  cudaStream_t copy_streams[8] = {};
+  cudaEvent_t copy_events[9] = {};
+
   // Scratch of the grid sums: kMaxSumBlocks float2 partials, then the counter.
   void *sum_scratch = nullptr;
   size_t sum_scratch_cls = 0;
@@ -210,6 +229,10 @@ struct Context {
   float2 *partials() { return reinterpret_cast<float2 *>(sum_scratch); }
   unsigned int *counter() {
     return reinterpret_cast<unsigned int *>(static_cast<char *>(sum_scratch) + sizeof(float2) * kMaxSumBlocks);
+  }
+  // Device error flag of the kernels with bounded waits (in the same scratch block).
+  int *error_flag() {
+    return reinterpret_cast<int *>(static_cast<char *>(sum_scratch) + sizeof(float2) * kMaxSumBlocks + 128);
   }
 };
 
@@ -279,22 +302,26 @@ std::vector<char> compile_cubin(const std::string &source, int cc_major, int cc_
 
 // ---------------------------------------------------------------- launches
 
-int64_t ew_grid(int64_t work, int block, int sm_count) {
+// Enough blocks for one element per thread, capped at what the GPU holds at
+// once (the kernel then loops), so every SM gets the same share of threads.
+int64_t ew_grid(int64_t work, int block, int sm_count, int resident) {
   int64_t grid = (work + block - 1) / block;
-  int64_t cap = (int64_t)sm_count * 16;
+  int64_t cap = (int64_t)sm_count * (resident > 0 ? resident : 8);
+  if (cap < 1) cap = 1;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
   return grid;
 }
 
 void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
-  const int block = 256;
+  const int block = p.block;
   const int64_t n = p.gen.domain;
   bool aligned = (out & 15u) == 0;
   for (uint64_t a : in) aligned = aligned && (a & 15u) == 0;
   const bool vec = p.vec4 && aligned;
   CUfunction f = vec ? p.vec4 : p.scalar;
-  const int64_t work = vec ? (n >> 2) : n;
+  // float4 kernels: each thread takes vec_unroll positions per batch
+  const int64_t work = vec ? ((n >> 2) + p.gen.vec_unroll - 1) / p.gen.vec_unroll : n;
   std::vector<void *> args;
   std::vector<uint64_t> ptrs(in);
   for (auto &v : ptrs) args.push_back(&v);
@@ -307,15 +334,39 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
     counter = reinterpret_cast<uint64_t>(c.counter());
     args.push_back(&partials);
     args.push_back(&counter);
-    grid = (unsigned)sum_grid(work, c.sm_count);
+    grid = (unsigned)sum_grid_for(work, block, c.sm_count * c.sum_blocks_per_sm);
   } else {
     if (n == 0) return;
-    grid = (unsigned)ew_grid(work, block, c.sm_count);
+    int resident = vec ? p.resident_vec4 : p.resident_scalar;
+    if (c.ew_blocks_per_sm > 0 && (resident <= 0 || c.ew_blocks_per_sm < resident)) resident = c.ew_blocks_per_sm;
+    grid = (unsigned)ew_grid(work, block, c.sm_count, resident);
   }
   args.push_back(&out_ptr);
   args.push_back(&nn);
   check_cu(g_drv.LaunchKernel(f, grid, 1, 1, block, 1, 1, 0, (CUstream)stream, args.data(), nullptr),
            "cuLaunchKernel");
+}
+
+// Upload striped over the context's copy streams, ordered after the work
+// queued on the main stream and joined back into it.
+void striped_upload(Context &c, char *dst, const char *src, size_t bytes) {
+  const int k = c.upload_streams;
+  if (k <= 1 || bytes < (size_t(8) << 20)) {
+    check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c.stream), "cudaMemcpyAsync H2D");
+    return;
+  }
+  check_cuda(cudaEventRecord(c.copy_events[8], c.stream), "cudaEventRecord");
+  size_t chunk = ((bytes + k - 1) / k + 4095) & ~size_t(4095);
+  for (int i = 0; i < k; ++i) {
+    size_t off = chunk * i;
+    if (off >= bytes) break;
+    size_t len = bytes - off < chunk ? bytes - off : chunk;
+    check_cuda(cudaStreamWaitEvent(c.copy_streams[i], c.copy_events[8], 0), "cudaStreamWaitEvent");
+    check_cuda(cudaMemcpyAsync(dst + off, src + off, len, cudaMemcpyHostToDevice, c.copy_streams[i]),
+               "cudaMemcpyAsync H2D");
+    check_cuda(cudaEventRecord(c.copy_events[i], c.copy_streams[i]), "cudaEventRecord");
+    check_cuda(cudaStreamWaitEvent(c.stream, c.copy_events[i], 0), "cudaStreamWaitEvent");
+  }
 }
 
 }  // namespace
@@ -380,6 +431,10 @@ int cc_init(int device_ordinal, uint32_t flags) {
     check_cuda(cudaMemGetInfo(&free_b, &c->total_mem), "cudaMemGetInfo");
   }
   check_cuda(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  for (int i = 0; i < 8; ++i)
+    check_cuda(cudaStreamCreateWithFlags(&c->copy_streams[i], cudaStreamNonBlocking), "cudaStreamCreate");
+  for (int i = 0; i < 9; ++i)
+    check_cuda(cudaEventCreateWithFlags(&c->copy_events[i], cudaEventDisableTiming), "cudaEventCreate");
   c->stream = c->own_stream;
   c->sum_scratch = c->pool.alloc(sizeof(float2) * kMaxSumBlocks + 256, &c->sum_scratch_cls);
   check_cuda(cudaMemsetAsync(c->sum_scratch, 0, sizeof(float2) * kMaxSumBlocks + 256, c->stream), "cudaMemsetAsync");
@@ -410,6 +465,8 @@ int cc_shutdown(void) {
   }
   c->pool.release(c->sum_scratch, c->sum_scratch_cls);
   c->pool.trim();
+  for (int i = 0; i < 8; ++i) cudaStreamDestroy(c->copy_streams[i]);
+  for (int i = 0; i < 9; ++i) cudaEventDestroy(c->copy_events[i]);
   cudaStreamDestroy(c->own_stream);
   g_ctx = nullptr;
   delete c;
@@ -440,6 +497,69 @@ int cc_set_stream(uint64_t stream) {
   // Blocks freed so far may still be read by work on the old stream.
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
   c.stream = stream ? reinterpret_cast<cudaStream_t>(stream) : c.own_stream;
+  CC_API_END
+}
+
+int cc_config_set(const char *key, int64_t value) {
+  CC_API_BEGIN
+  if (!key) fail(CC_ERR_INVALID_VALUE, "null key");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  std::string k(key);
+  if (k == "block") {
+    if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "block must be 64, 128 or 256");
+    c.block = (int)value;
+  } else if (k == "ew_blocks_per_sm") {
+    if (value < 0 || value > 32) fail(CC_ERR_INVALID_VALUE, "ew_blocks_per_sm must be in [0, 32]");
+    c.ew_blocks_per_sm = (int)value;
+  } else if (k == "sum_blocks_per_sm") {
+    if (value < 1 || (int64_t)c.sm_count * value > kMaxSumBlocks)
+      fail(CC_ERR_INVALID_VALUE, "sum_blocks_per_sm out of range for the sum scratch");
+    c.sum_blocks_per_sm = (int)value;
+  } else if (k == "upload_streams") {
+    if (value < 1 || value > 8) fail(CC_ERR_INVALID_VALUE, "upload_streams must be in [1, 8]");
+    c.upload_streams = (int)value;
+  } else if (k == "ew_lookahead") {
+    if (value < 0 || value > 256) fail(CC_ERR_INVALID_VALUE, "ew_lookahead must be in [0, 256]");
+    c.ew_lookahead = (int)value;
+  } else if (k == "prefetch_min_bytes") {
+    if (value < -1) fail(CC_ERR_INVALID_VALUE, "prefetch_min_bytes must be >= -1");
+    c.prefetch_min_bytes = value;
+  } else if (k == "sum_block") {
+    if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
+    c.sum_block = (int)value;
+  } else if (k == "tc_variant") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "tc_variant must be 0 or 1");
+    c.tc_variant = (int)value;
+  } else if (k == "vec_unroll") {
+    if (value < 1 || value > 8) fail(CC_ERR_INVALID_VALUE, "vec_unroll must be in [1, 8]");
+    c.vec_unroll = (int)value;
+  } else if (k == "ew_asm_loads") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "ew_asm_loads must be 0 or 1");
+    c.ew_asm_loads = (int)value;
+  } else {
+    fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
+  }
+  CC_API_END
+}
+
+int cc_config_get(const char *key, int64_t *value) {
+  CC_API_BEGIN
+  if (!key || !value) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  std::string k(key);
+  if (k == "block") *value = c.block;
+  else if (k == "ew_blocks_per_sm") *value = c.ew_blocks_per_sm;
+  else if (k == "sum_blocks_per_sm") *value = c.sum_blocks_per_sm;
+  else if (k == "upload_streams") *value = c.upload_streams;
+  else if (k == "ew_lookahead") *value = c.ew_lookahead;
+  else if (k == "ew_asm_loads") *value = c.ew_asm_loads;
+  else if (k == "vec_unroll") *value = c.vec_unroll;
+  else if (k == "prefetch_min_bytes") *value = c.prefetch_min_bytes;
+  else if (k == "sum_block") *value = c.sum_block;
+  else if (k == "tc_variant") *value = c.tc_variant;
+  else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END
 }
 
@@ -516,7 +636,7 @@ int cc_buf_upload(cc_handle h, size_t offset, const void *host, size_t bytes) {
   }
   if (bytes == 0) return CC_OK;
   if (!host) fail(CC_ERR_INVALID_VALUE, "null host pointer");
-  check_cuda(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, c.stream), "cudaMemcpyAsync H2D");
+  striped_upload(c, static_cast<char *>(dst), static_cast<const char *>(host), bytes);
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
   CC_API_END
 }
@@ -588,6 +708,19 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   if (!ir_text || !out) fail(CC_ERR_INVALID_VALUE, "null pointer");
   Context &c = ctx();
   std::string key(ir_text, ir_len);
+  CodegenOptions opt;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    opt.load_lookahead = c.ew_lookahead;
+    opt.asm_loads = c.ew_asm_loads != 0;
+    opt.min_blocks = -c.ew_blocks_per_sm;  // resolved below, once the domain is known
+    opt.block = c.block;
+    opt.vec_unroll = c.vec_unroll;
+    opt.prefetch_min_bytes = c.prefetch_min_bytes;
+  }
+  key += "#lookahead " + std::to_string(opt.load_lookahead) + " asm " + std::to_string((int)opt.asm_loads) +
+         " blocks " + std::to_string(-opt.min_blocks) + " block " + std::to_string(opt.block) + " unroll " + std::to_string(opt.vec_unroll) +
+         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " sumblock " + std::to_string(c.sum_block) + "\n";
   {
     std::lock_guard<std::recursive_mutex> g(c.mu);
     auto it = c.cache.find(key);
@@ -608,7 +741,12 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     }
   }
   Ir ir = parse_ir(ir_text, ir_len);
-  CodegenOptions opt;
+  if (ir.kind == ProgramKind::Sum) opt.block = c.sum_block;
+  {
+    int64_t domain = 1;
+    for (int64_t d : ir.out_shape) domain *= d;
+    opt.min_blocks = choose_min_blocks(domain, opt.block, c.sm_count, -opt.min_blocks);
+  }
   auto p = std::make_unique<Program>();
   p->gen = generate_cuda(ir, opt);
   p->kind = ir.kind;
@@ -618,6 +756,10 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   const char *vname = ir.kind == ProgramKind::Sum ? "cc_sum_v4" : "cc_ew_v4";
   check_cu(g_drv.ModuleGetFunction(&p->scalar, p->module, sname), "cuModuleGetFunction");
   if (p->gen.has_vec4) check_cu(g_drv.ModuleGetFunction(&p->vec4, p->module, vname), "cuModuleGetFunction");
+  p->block = opt.block;
+  check_cu(g_drv.OccupancyMaxActiveBlocks(&p->resident_scalar, p->scalar, p->block, 0), "cuOccupancyMaxActiveBlocks");
+  if (p->vec4)
+    check_cu(g_drv.OccupancyMaxActiveBlocks(&p->resident_vec4, p->vec4, p->block, 0), "cuOccupancyMaxActiveBlocks");
   std::lock_guard<std::recursive_mutex> g(c.mu);
   uint64_t h = c.make_handle(kTagProgram);
   c.programs[h] = p.release();
@@ -743,6 +885,91 @@ int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stre
   if (s != c.stream && e == cudaSuccess) e = cudaStreamSynchronize(s);  // the pool is ordered on the context stream
   c.pool.release(scratch, cls);
   check_cuda(e, "sum launch");
+  CC_API_END
+}
+
+namespace cc {
+namespace {
+
+void encode_plane_map(CUtensorMap *map, void *base, int rows, int kcols, int box_rows) {
+  const cuuint64_t dims[2] = {(cuuint64_t)kcols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kcols * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  check_cu(g_drv.TensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE),
+           "cuTensorMapEncodeTiled");
+}
+
+}  // namespace
+}  // namespace cc
+
+int cc_gemm_f32(uint64_t a_ptr, uint64_t b_ptr, uint64_t c_ptr, int m, int n, int k, int64_t lda, int64_t ldb,
+                int64_t ldc, int mode, uint64_t stream) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  if (!a_ptr || !b_ptr || !c_ptr) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  if (m < 0 || n < 0 || k <= 0 || lda < k || ldb < n || ldc < n) fail(CC_ERR_INVALID_VALUE, "bad matrix shape");
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  const float *A = reinterpret_cast<const float *>(a_ptr);
+  const float *B = reinterpret_cast<const float *>(b_ptr);
+  float *C = reinterpret_cast<float *>(c_ptr);
+  if (m == 0 || n == 0) return CC_OK;
+  if (mode == CC_GEMM_EXACT || mode == CC_GEMM_FP32) {
+    check_cuda(launch_sgemm(A, B, C, m, n, k, lda, ldb, ldc, mode == CC_GEMM_EXACT, s), "sgemm launch");
+    return CC_OK;
+  }
+  if (mode != CC_GEMM_BF16X6) fail(CC_ERR_INVALID_VALUE, "unknown contraction mode");
+  if (c.cc_major != 10) fail(CC_ERR_INVALID_OPERATION, "the tensor-core contraction needs an sm_10x GPU");
+  const int Mp = (m + kTcBM - 1) / kTcBM * kTcBM;
+  const int Np = (n + kTcBN - 1) / kTcBN * kTcBN;
+  const int Kp = (k + kTcBK - 1) / kTcBK * kTcBK;
+  size_t cls_a = 0, cls_b = 0;
+  const size_t bytes_a = (size_t)3 * Mp * Kp * 2, bytes_b = (size_t)3 * Np * Kp * 2;
+  void *pa = c.pool.alloc(bytes_a, &cls_a);
+  void *pb = nullptr;
+  try {
+    pb = c.pool.alloc(bytes_b, &cls_b);
+  } catch (...) {
+    c.pool.release(pa, cls_a);
+    throw;
+  }
+  cudaError_t e = launch_split_a(A, lda, m, k, static_cast<__nv_bfloat16 *>(pa), Mp, Kp, c.sm_count, s);
+  if (e == cudaSuccess) e = launch_split_bt(B, ldb, k, n, static_cast<__nv_bfloat16 *>(pb), Np, Kp, s);
+  if (e == cudaSuccess) {
+    CUtensorMap maps[6];
+    const size_t plane_a = (size_t)Mp * Kp * 2, plane_b = (size_t)Np * Kp * 2;
+    try {
+      for (int p = 0; p < 3; ++p) {
+        encode_plane_map(&maps[p], static_cast<char *>(pa) + p * plane_a, Mp, Kp, kTcBM);
+        encode_plane_map(&maps[3 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp, gemm_tc_box_n(c.tc_variant));
+      }
+    } catch (...) {
+      c.pool.release(pa, cls_a);
+      c.pool.release(pb, cls_b);
+      throw;
+    }
+    e = launch_gemm_bf16x6(maps, C, m, n, Kp, ldc, c.sm_count, c.error_flag(), c.tc_variant, s);
+  }
+  if (s != c.stream && e == cudaSuccess) e = cudaStreamSynchronize(s);  // the pool is ordered on the context stream
+  c.pool.release(pa, cls_a);
+  c.pool.release(pb, cls_b);
+  check_cuda(e, "bf16x6 contraction launch");
+  CC_API_END
+}
+
+int cc_device_errors(int *code) {
+  CC_API_BEGIN
+  if (!code) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  int v = 0;
+  check_cuda(cudaMemcpyAsync(&v, c.error_flag(), sizeof(int), cudaMemcpyDeviceToHost, c.stream), "read error flag");
+  check_cuda(cudaMemsetAsync(c.error_flag(), 0, sizeof(int), c.stream), "clear error flag");
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  *code = v;
   CC_API_END
 }
 

@@ -68,6 +68,23 @@ int cc_device_info(int *sm_count, int *cc_major, int *cc_minor, size_t *total_me
 int cc_get_stream(uint64_t *stream);            /* the context's cudaStream_t */
 int cc_set_stream(uint64_t stream);             /* order later work on a caller-owned stream */
 int cc_synchronize(void);
+/* Runtime tuning knobs (no reference counterpart: the reference leaves launch
+ * geometry to the OpenCL runtime, Tensors.scala:1360-1375, :697-753).  Keys:
+ *   "block"             threads per block of generated kernels (64, 128 or 256; default 128)
+ *   "ew_blocks_per_sm"  cap on resident blocks per SM for elementwise grids (0 = occupancy; default 0)
+ *   "sum_blocks_per_sm" blocks per SM of the grid sums (default 4)
+ *   "sum_block"         threads per block of the generated sums (64, 128 or 256; default 256)
+ *   "prefetch_min_bytes" generated kernels L2-prefetch every load from an input at least this large
+ *                       before loading (-1: never; default -1)
+ *   "upload_streams"    copy streams a large cc_buf_upload is striped over (1..8; default 4)
+ *   "ew_lookahead"      loads a generated kernel keeps in flight ahead of its arithmetic (0..256; default 8)
+ *   "ew_asm_loads"      1: those loads are volatile inline PTX so the compiler keeps their order (default 1)
+ *   "tc_variant"        tensor-core contraction tiles: 0 = 128x128 with a double-buffered accumulator,
+ *                       1 = 128x256 with a single one (default)
+ *   "vec_unroll"        float4 positions a thread of a contiguous kernel loads before computing (1..8; default 4)
+ * Unknown keys or values out of range return CC_ERR_INVALID_VALUE. */
+int cc_config_set(const char *key, int64_t value);
+int cc_config_get(const char *key, int64_t *value);
 
 /* ---- device buffers: replace allocateBuffer / allocateBufferFrom
  *      (OpenCL.scala:1397-1431) and DeviceBuffer.retain/release/numberOfBytes/
@@ -146,6 +163,24 @@ int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stre
  *     stream are safe, but calls that can overlap on the GPU (on different
  *     streams of one device) race and give wrong sums. */
 int cc_reduce_sum_f32_noalloc(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stream);
+
+/* ---- contraction: the library's matmul, `A.broadcast([i,j,k]) * B.reshape([1,j,k]).broadcast(...)`
+ *      followed by `split(1).reduce(_ + _)` (TensorsSpec.scala:468-485, README.md:311-343), as one
+ *      kernel.  C[M,N] = A[M,K] * B[K,N], float, row-major, leading dimensions in elements.
+ *      mode CC_GEMM_EXACT: FP32 on the CUDA cores, every output the sequential left fold over k of
+ *        separately rounded products: bit-identical to the reference's result;
+ *      mode CC_GEMM_FP32: FP32 on the CUDA cores with fused multiply-adds;
+ *      mode CC_GEMM_BF16X6: each operand split into three bfloat16 planes, the six leading
+ *        products accumulated in FP32 by the tcgen05 tensor cores (FP32-level error).
+ *      The bfloat16 planes (6*(M*K + K*N) bytes, padded) come from the buffer pool. ---------- */
+#define CC_GEMM_EXACT 0
+#define CC_GEMM_FP32 1
+#define CC_GEMM_BF16X6 2
+int cc_gemm_f32(uint64_t a_ptr, uint64_t b_ptr, uint64_t c_ptr, int m, int n, int k, int64_t lda, int64_t ldb,
+                int64_t ldc, int mode, uint64_t stream);
+/* Reads and clears the device error flag that kernels with bounded waits set
+ * when a wait expires (0 = none); blocking. */
+int cc_device_errors(int *code);
 
 /* ---- random numbers: Tensor.random / Tensor.randomNormal with the Wang hash
  *      (Tensors.scala:106-117, :397-524).  normal=0: uniform [0,1]; normal=1:

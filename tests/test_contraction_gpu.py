@@ -1,0 +1,85 @@
+"""The contraction kernels (cc_gemm_f32) against the reference's fold and FP64.
+
+* CC_GEMM_EXACT must equal, bit for bit, the reference's matmul: the left fold
+  over k of float products (TensorsSpec.scala:468-485), computed here in numpy
+  float32 one k at a time.
+* CC_GEMM_FP32 (fused multiply-adds) and CC_GEMM_BF16X6 (three bfloat16 planes,
+  six products, FP32 accumulation on the tensor cores) are measured by their
+  relative Frobenius error against float64: at most 1e-6 for the split-BF16
+  path (BASELINE: <= 1e-6 relative error).
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def reference_fold(a, b):
+    """C[i][j] = ((a[i,0]*b[0,j] + a[i,1]*b[1,j]) + ...) in float32, the reference's order."""
+    acc = (a[:, 0:1] * b[0:1, :]).astype(np.float32)
+    for k in range(1, a.shape[1]):
+        acc = (acc + (a[:, k:k + 1] * b[k:k + 1, :])).astype(np.float32)
+    return acc
+
+
+def rel_fro(c, ref):
+    return float(np.linalg.norm(c.astype(np.float64) - ref) / np.linalg.norm(ref))
+
+
+# Exactly one index per seed makes the Wang hash 0 and log(0) = -inf, so a
+# normal tensor of that seed holds an infinity there (also in the reference).
+# Seeds with bit 30 set move that index past 2^30, beyond these tensors.
+SEED = 0x40000000
+
+
+def _operands(device, m, k, n, seed=SEED):
+    T = device.Tensor
+    a = T.randomNormal([m, k], seed=seed).doCache()
+    b = T.randomNormal([k, n], seed=seed + 1).doCache()
+    return a, b
+
+
+def _run(device, a, b, m, k, n, mode):
+    rt = device.runtime
+    out = rt.alloc(m * n * 4)
+    rt.gemm_ptr(a._cached.device_ptr(), b._cached.device_ptr(), out.device_ptr(), m, n, k, mode)
+    c = rt.download(out, m * n).reshape(m, n)
+    out.release()
+    assert rt.device_errors() == 0
+    return c
+
+
+@pytest.mark.parametrize("shape", [(19, 23, 17), (128, 32, 256), (200, 50, 300), (256, 129, 512)])
+def test_exact_mode_is_the_reference_fold(cuda_device, shape):
+    m, k, n = shape
+    a, b = _operands(cuda_device, m, k, n)
+    c = _run(cuda_device, a, b, m, k, n, 0)
+    want = reference_fold(a.flatArray().reshape(m, k), b.flatArray().reshape(k, n))
+    assert np.array_equal(c.view(np.int32), want.view(np.int32))
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("shape", [(128, 32, 256), (300, 100, 700), (1024, 1024, 1024)])
+def test_fp32_mode(cuda_device, shape):
+    m, k, n = shape
+    a, b = _operands(cuda_device, m, k, n)
+    c = _run(cuda_device, a, b, m, k, n, 1)
+    ref = a.flatArray().reshape(m, k).astype(np.float64) @ b.flatArray().reshape(k, n).astype(np.float64)
+    assert rel_fro(c, ref) <= 1e-6
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("shape", [(128, 32, 256), (256, 64, 512), (300, 100, 700), (1024, 1024, 1024),
+                                   (2048, 256, 2048)])
+def test_split_bf16_tensor_core_mode(cuda_device, shape):
+    m, k, n = shape
+    a, b = _operands(cuda_device, m, k, n)
+    c = _run(cuda_device, a, b, m, k, n, 2)
+    ref = a.flatArray().reshape(m, k).astype(np.float64) @ b.flatArray().reshape(k, n).astype(np.float64)
+    err = rel_fro(c, ref)
+    assert err <= 1e-6, err
+    a.close()
+    b.close()

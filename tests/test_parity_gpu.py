@@ -50,14 +50,16 @@ def test_random_normal_infinities_follow_the_reference():
 
 
 @pytest.mark.parametrize("n", [1, 2, 27, 1001, 1 << 20, 3 << 20])
-def test_random_normal_within_2ulp(cuda_device, n):
+def test_random_normal_matches_the_oracle(cuda_device, n):
     seed = 54321 if n < (3 << 20) else 9
     got = cuda_device.Tensor.randomNormal([n], seed=seed).flatArray()
     want = rng.random_normal(n, seed)
     fin = np.isfinite(want)
     assert np.array_equal(np.isinf(got), np.isinf(want))
-    # log, then sqrt, then cos/sin: the device functions are <= 2 ulp each; allow their composition
-    assert ulp_diff(got[fin], want[fin]).max() <= 4
+    # log/sin/cos are taken in double and rounded once on both sides: bit-exact except, in
+    # vanishingly rare cases, a double-rounding difference of one ulp
+    d = ulp_diff(got[fin], want[fin])
+    assert d.max() <= 1 and (d > 0).sum() <= max(1, n // 10 ** 6)
 
 
 def _c2(T, n, c, h, w):
