@@ -23,8 +23,10 @@ cudaError_t launch_split_bt(const float *B, long long ldb, int K, int N, __nv_bf
 // Tile sizes of the tensor-core kernel: planes are padded to these multiples
 // (kTcBN covers both tile widths).
 constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 32;
-// Tile width (B^T box rows) of a kernel variant: 0 = 128 columns with two
-// accumulator pairs (the epilogue overlaps the next tile), 1 = 256 columns with one.
+// Kernel variants: 0 = 128-column tiles, accumulators restarted every 4
+// k-blocks and summed in registers (FP32-level error at any K); 1 = 256-column
+// tiles, one accumulator pair per tile (fastest; error grows with K);
+// 2 = 128-column tiles, one pair per tile.  gemm_tc_box_n: the tile width.
 int gemm_tc_box_n(int variant);
 // maps: A planes 0..2 (box 32 x 128), B^T planes 0..2 (box 32 x gemm_tc_box_n), 64-byte swizzle.
 cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,

@@ -162,11 +162,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Stores 32 consecutive values of one output row (columns col0..col0+31, masked to N).
+__device__ __forceinline__ void store_row_chunk(float *crow, int row, int M, int N, long long ldc, int col0,
+                                                const float *v) {
+  if (row >= M) return;
+  if (col0 + 32 <= N && (ldc & 3) == 0 && ((reinterpret_cast<uintptr_t>(crow) & 15) == 0)) {
+#pragma unroll
+    for (int j = 0; j < 32; j += 4)
+      *reinterpret_cast<float4 *>(crow + col0 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+      if (col0 + j < N) crow[col0 + j] = v[j];
+  }
+}
+
 // The six (A plane, B plane) products, largest first.
 __device__ __constant__ int kProdA[6] = {0, 0, 1, 1, 0, 2};
 __device__ __constant__ int kProdB[6] = {0, 1, 0, 1, 2, 0};
 
-template <int BN, int STAGES, int ACC_BUFS>
+template <int BN, int STAGES, int ACC_BUFS, int KC>
 __global__ void __launch_bounds__(kThreads, 1)
     gemm_bf16x6_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
                        const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap tb0,
@@ -266,39 +281,50 @@ __global__ void __launch_bounds__(kThreads, 1)
       int stage = 0, acc = 0;
       uint32_t phase = 0, acc_phase = 0;
       bool ok = true;
+      // K is processed in chunks of KC k-blocks (the whole K when KC == 0); each
+      // chunk accumulates into a fresh accumulator pair.
+      const int kc = KC > 0 ? KC : num_kb;
       for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
-        if (!mbar_wait(bar_accempty + 8 * acc, acc_phase ^ 1u, abort_flag, err, 2)) break;
-        tc_fence_after();
-        const uint32_t d_big = tmem_base + (uint32_t)(acc * 2 * BN);  // hi*hi
-        const uint32_t d_small = d_big + BN;                           // the five small products
-        for (int kb = 0; kb < num_kb; ++kb) {
-          if (!mbar_wait(bar_full + 8 * stage, phase, abort_flag, err, 3)) {
+        for (int kb0 = 0; kb0 < num_kb && ok; kb0 += kc) {
+          if (!mbar_wait(bar_accempty + 8 * acc, acc_phase ^ 1u, abort_flag, err, 2)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t sbase = base + stage * kStageBytes;
+          const uint32_t d_big = tmem_base + (uint32_t)(acc * 2 * BN);  // hi*hi
+          const uint32_t d_small = d_big + BN;                           // the five small products
+          const int kend = kb0 + kc < num_kb ? kb0 + kc : num_kb;
+          for (int kb = kb0; kb < kend; ++kb) {
+            if (!mbar_wait(bar_full + 8 * stage, phase, abort_flag, err, 3)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sbase = base + stage * kStageBytes;
 #pragma unroll
-          for (int k16 = 0; k16 < BK / 16; ++k16) {
+            for (int k16 = 0; k16 < BK / 16; ++k16) {
 #pragma unroll
-            for (int prod = 0; prod < 6; ++prod) {
-              const uint64_t adesc = smem_desc(sbase + kProdA[prod] * kAPlaneBytes + k16 * 32);
-              const uint64_t bdesc = smem_desc(sbase + 3 * kAPlaneBytes + kProdB[prod] * kBPlaneBytes + k16 * 32);
-              const bool first = prod == 0 ? (kb | k16) == 0 : ((kb | k16) == 0 && prod == 1);
-              mma_bf16(prod == 0 ? d_big : d_small, adesc, bdesc, Cfg::kIdesc, first ? 0u : 1u);
+              for (int prod = 0; prod < 6; ++prod) {
+                const uint64_t adesc = smem_desc(sbase + kProdA[prod] * kAPlaneBytes + k16 * 32);
+                const uint64_t bdesc =
+                    smem_desc(sbase + 3 * kAPlaneBytes + kProdB[prod] * kBPlaneBytes + k16 * 32);
+                const bool fresh = kb == kb0 && k16 == 0;
+                const bool first = prod == 0 ? fresh : (fresh && prod == 1);
+                mma_bf16(prod == 0 ? d_big : d_small, adesc, bdesc, Cfg::kIdesc, first ? 0u : 1u);
+              }
+            }
+            mma_commit(bar_empty + 8 * stage);  // the stage is free once these MMAs have read it
+            if (++stage == kStages) {
+              stage = 0;
+              phase ^= 1u;
             }
           }
-          mma_commit(bar_empty + 8 * stage);  // the stage is free once these MMAs have read it
-          if (++stage == kStages) {
-            stage = 0;
-            phase ^= 1u;
+          if (!ok) break;
+          mma_commit(bar_accfull + 8 * acc);  // the accumulator pair is complete
+          if (++acc == ACC_BUFS) {
+            acc = 0;
+            acc_phase ^= 1u;
           }
-        }
-        if (!ok) break;
-        mma_commit(bar_accfull + 8 * acc);  // the accumulator pair is complete
-        if (++acc == ACC_BUFS) {
-          acc = 0;
-          acc_phase ^= 1u;
         }
       }
       // Every MMA this thread issued must be complete before TMEM is freed.
@@ -313,38 +339,70 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int row_in_tile = quarter * 32 + lane;
     int acc = 0;
     uint32_t acc_phase = 0;
-    for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
-      if (!mbar_wait(bar_accfull + 8 * acc, acc_phase, abort_flag, err, 4)) break;
-      tc_fence_after();
-      const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
-      const int row = m0 + row_in_tile;
-      float *crow = C + (long long)row * ldc;
+    const uint32_t lane_tmem = tmem_base + ((uint32_t)(quarter * 32) << 16);
+    if constexpr (KC == 0) {
+      // One accumulator pair per tile: add the pair and store, 32 columns at a time.
+      for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
+        if (!mbar_wait(bar_accfull + 8 * acc, acc_phase, abort_flag, err, 4)) break;
+        tc_fence_after();
+        const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+        const int row = m0 + row_in_tile;
+        float *crow = C + (long long)row * ldc;
 #pragma unroll 1
-      for (int chunk = 0; chunk < BN / 32; ++chunk) {
-        float v[32], w[32];
-        const uint32_t lane_base = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * 2 * BN + chunk * 32);
-        tmem_ld32(lane_base, v);
-        tmem_ld32(lane_base + BN, w);
+        for (int chunk = 0; chunk < BN / 32; ++chunk) {
+          float v[32], w[32];
+          const uint32_t t = lane_tmem + (uint32_t)(acc * 2 * BN + chunk * 32);
+          tmem_ld32(t, v);
+          tmem_ld32(t + BN, w);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = __fadd_rn(v[j], w[j]);
-        const int col0 = n0 + chunk * 32;
-        if (row < M) {
-          if (col0 + 32 <= N && (ldc & 3) == 0 && ((reinterpret_cast<uintptr_t>(crow) & 15) == 0)) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 4)
-              *reinterpret_cast<float4 *>(crow + col0 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-          } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if (col0 + j < N) crow[col0 + j] = v[j];
-          }
+          for (int j = 0; j < 32; ++j) v[j] = __fadd_rn(v[j], w[j]);
+          store_row_chunk(crow, row, M, N, ldc, n0 + chunk * 32, v);
+        }
+        tc_fence_before();
+        mbar_arrive(bar_accempty + 8 * acc);
+        if (++acc == ACC_BUFS) {
+          acc = 0;
+          acc_phase ^= 1u;
         }
       }
-      tc_fence_before();
-      mbar_arrive(bar_accempty + 8 * acc);
-      if (++acc == ACC_BUFS) {
-        acc = 0;
-        acc_phase ^= 1u;
+    } else {
+      // A pair per K chunk: fold each into a running sum of the row (in
+      // registers, round-to-nearest), so no FP32 accumulator inside the tensor
+      // core takes more than KC k-blocks of additions.
+      const int nchunks = (num_kb + KC - 1) / KC;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
+        float sum[BN];
+#pragma unroll
+        for (int j = 0; j < BN; ++j) sum[j] = 0.0f;
+        for (int ch = 0; ch < nchunks; ++ch) {
+          if (!mbar_wait(bar_accfull + 8 * acc, acc_phase, abort_flag, err, 4)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+#pragma unroll
+          for (int c32 = 0; c32 < BN / 32; ++c32) {
+            float v[32], w[32];
+            const uint32_t t = lane_tmem + (uint32_t)(acc * 2 * BN + c32 * 32);
+            tmem_ld32(t, v);
+            tmem_ld32(t + BN, w);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) sum[c32 * 32 + j] = __fadd_rn(sum[c32 * 32 + j], __fadd_rn(v[j], w[j]));
+          }
+          tc_fence_before();
+          mbar_arrive(bar_accempty + 8 * acc);
+          if (++acc == ACC_BUFS) {
+            acc = 0;
+            acc_phase ^= 1u;
+          }
+        }
+        if (!ok) break;
+        const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+        const int row = m0 + row_in_tile;
+        float *crow = C + (long long)row * ldc;
+#pragma unroll
+        for (int c32 = 0; c32 < BN / 32; ++c32) store_row_chunk(crow, row, M, N, ldc, n0 + c32 * 32, sum + c32 * 32);
       }
     }
   }
@@ -357,13 +415,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-template <int BN, int STAGES, int ACC_BUFS>
+template <int BN, int STAGES, int ACC_BUFS, int KC>
 cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc, int sm_count,
                            int *err, cudaStream_t stream) {
   using Cfg = TcCfg<BN, STAGES, ACC_BUFS>;
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS>,
+    cudaError_t e = cudaFuncSetAttribute(gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS, KC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmemBytes);
     if (e != cudaSuccess) return e;
     attr_set = true;
@@ -372,7 +430,7 @@ cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int 
   const int num_tiles = tiles_m * tiles_n;
   const int num_kb = K_padded / BK;
   const int grid = num_tiles < sm_count ? num_tiles : sm_count;
-  gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS><<<grid, kThreads, Cfg::kSmemBytes, stream>>>(
+  gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS, KC><<<grid, kThreads, Cfg::kSmemBytes, stream>>>(
       maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], C, M, N, ldc, num_kb, tiles_n, num_tiles, err);
   return cudaGetLastError();
 }
@@ -383,8 +441,9 @@ int gemm_tc_box_n(int variant) { return variant == 1 ? 256 : 128; }
 
 cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
                                int sm_count, int *err, int variant, cudaStream_t stream) {
-  if (variant == 1) return launch_variant<256, 3, 1>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
-  return launch_variant<128, 4, 2>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
+  if (variant == 1) return launch_variant<256, 3, 1, 0>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
+  if (variant == 2) return launch_variant<128, 4, 2, 0>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
+  return launch_variant<128, 4, 2, 4>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
 }
 
 }  // namespace cc

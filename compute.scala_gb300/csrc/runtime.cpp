@@ -217,7 +217,7 @@ struct Context {
   int vec_unroll = 4;
   int64_t prefetch_min_bytes = -1;
   int sum_block = 256;
-  int tc_variant = 1;
+  int tc_variant = 0;
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
 
@@ -529,7 +529,7 @@ int cc_config_set(const char *key, int64_t value) {
     if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
     c.sum_block = (int)value;
   } else if (k == "tc_variant") {
-    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "tc_variant must be 0 or 1");
+    if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "tc_variant must be 0, 1 or 2");
     c.tc_variant = (int)value;
   } else if (k == "vec_unroll") {
     if (value < 1 || value > 8) fail(CC_ERR_INVALID_VALUE, "vec_unroll must be in [1, 8]");

@@ -79,8 +79,9 @@ int cc_synchronize(void);
  *   "upload_streams"    copy streams a large cc_buf_upload is striped over (1..8; default 4)
  *   "ew_lookahead"      loads a generated kernel keeps in flight ahead of its arithmetic (0..256; default 8)
  *   "ew_asm_loads"      1: those loads are volatile inline PTX so the compiler keeps their order (default 1)
- *   "tc_variant"        tensor-core contraction tiles: 0 = 128x128 with a double-buffered accumulator,
- *                       1 = 128x256 with a single one (default)
+ *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
+ *                       registers (FP32-level error at any K; default), 1 = 128x256 tiles, one
+ *                       accumulator per tile (fastest, error grows with K), 2 = 128x128, one per tile
  *   "vec_unroll"        float4 positions a thread of a contiguous kernel loads before computing (1..8; default 4)
  * Unknown keys or values out of range return CC_ERR_INVALID_VALUE. */
 int cc_config_set(const char *key, int64_t value);
