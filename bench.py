@@ -123,6 +123,20 @@ def build_c2(T, x, bias, n, c, h, w):
     return y.translate([0, 0, 1, 0]).split(3).reduce(lambda a, b: a + b)
 
 
+C3 = {"c3": (4096, 4096, 4096), "c3s": (16384, 256, 16384)}
+# Exactly one index per seed makes the Wang hash 0 (log(0) = -inf in Box-Muller);
+# seeds with bit 30 set move it past 2^30, beyond these matrices.
+C3_SEED = 0x40000000
+
+
+def matmul_expr(T, a, b):
+    """The library's matmul (TensorsSpec.scala:472-478): broadcast product, then a left fold of split(1)."""
+    i, j = a.shape
+    _, k = b.shape
+    prod = a.broadcast([i, j, k]) * b.reshape([1, j, k]).broadcast([i, j, k])
+    return prod.split(1).reduce(lambda x, y: x + y)
+
+
 def setup(workload, d):
     """Returns (program, list of input-buffer lists to rotate over, output buffer, bytes, description)."""
     T = d.Tensor
@@ -171,7 +185,54 @@ def setup(workload, d):
                     config={"workload": "fused elementwise+sum: ((a*b+c).tanh).sum, a,b,c [1024,1024] U[-1,1]",
                             "l2": "inputs rotate over %d copies of (a,b,c) (%.0f MB > 4x L2)"
                                   % (copies, copies * 3 * n * m * 4 / 1e6)})
+    if workload in C3:
+        m, k, n = C3[workload]
+        rt.config_set("contraction", 3)  # split-BF16 on the tensor cores
+        a = T.randomNormal([m, k], seed=C3_SEED).doCache()
+        b = T.randomNormal([k, n], seed=C3_SEED + 1).doCache()
+        c = matmul_expr(T, a, b)
+        ser = d.serialize(c.closure, c.shape)
+        # inputs: A, and B's [1,J,K] reshape (which shares B's buffer)
+        assert len(ser.params) == 2 and ser.params[0] is a
+        prog = rt.program(ser.text)
+        out = rt.alloc(m * n * 4)
+        return dict(prog=prog, sets=[[a._cached, b._cached]], out=out, flops=2.0 * m * n * k, bytes=4 * (m * k + k * n + m * n),
+                    keep=[a, b], ser=ser, shape=(m, k, n), copies=1,
+                    config={"workload": "contraction via broadcast+split(1).reduce: A[%d,%d] x B[%d,%d] ~ N(0,1), "
+                                        "split-BF16 (3 planes, 6 products) on tcgen05 tensor cores, FP32 accumulate"
+                                        % (m, k, k, n),
+                            "seeds": [C3_SEED, C3_SEED + 1],
+                            "l2": "operands %.0f MB; no rotation (compute-bound)" % (4 * (m * k + k * n) / 1e6)})
     raise SystemExit("unknown workload " + workload)
+
+
+def contraction_extras(d, st):
+    """Error of the split-BF16 result against float64, and the FP32 CUDA-core GEMM's speed and error."""
+    import numpy as np
+    rt = d.runtime
+    m, k, n = st["shape"]
+    a, b = st["keep"]
+    rt.launch(st["prog"], st["sets"][0], st["out"])
+    c = rt.download(st["out"], m * n).reshape(m, n).astype(np.float64)
+    rows = np.random.RandomState(0).choice(m, size=min(m, 512), replace=False)
+    A = a.flatArray().reshape(m, k)[rows].astype(np.float64)
+    B = b.flatArray().reshape(k, n).astype(np.float64)
+    ref = A @ B
+    err = float(np.linalg.norm(c[rows] - ref) / np.linalg.norm(ref))
+    out = rt.alloc(m * n * 4)
+    args = (a._cached.device_ptr(), b._cached.device_ptr(), out.device_ptr(), m, n, k, rt.GEMM_FP32)
+    rt.gemm_ptr(*args)
+    e0 = rt.event()
+    for _ in range(3):
+        rt.gemm_ptr(*args)
+    e1 = rt.event()
+    rt.event_wait(e1)
+    ms = rt.event_elapsed_ms(e0, e1) / 3
+    c32 = rt.download(out, m * n).reshape(m, n).astype(np.float64)
+    err32 = float(np.linalg.norm(c32[rows] - ref) / np.linalg.norm(ref))
+    out.release()
+    return {"rel_fro_err_vs_fp64": err, "rows_checked": int(len(rows)),
+            "fp32_cuda_core_tflops": 2.0 * m * n * k / (ms * 1e-3) / 1e12, "fp32_cuda_core_rel_fro_err": err32}
 
 
 def time_device(rt, st, steps, warmup):
@@ -259,7 +320,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true", help="skip the clock sampling (and its untimed busy loop)")
@@ -270,6 +331,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     metric = "fused-op GB/s"
+    if args.workload in C3:
+        return main_contraction(args, warmup, rank, world, local_rank)
 
     if args.impl == "reference":
         if rank != 0:
@@ -342,6 +405,70 @@ def main():
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def main_contraction(args, warmup, rank, world, local_rank):
+    """The contraction workloads: TFLOP/s (2*M*N*K per step, counted once) of the
+    split-BF16 tensor-core path, reached through the Tensor API's matmul idiom."""
+    metric = "matmul TFLOP/s"
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import cref
+        r = cref.time_contraction(C3[args.workload])
+        line = {"impl": "reference", "metric": metric, "value": r["tflops"], "unit": "TFLOP/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
+                "config": r["config"],
+                "cpu_baseline": {"value": r["tflops"], "unit": "TFLOP/s", "cores": r["threads"], "kind": "port",
+                                 "sample": r["sample"]},
+                "e2e": {"value": r["tflops"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    from compute import Tensors
+    d = Tensors(device=local_rank)
+    rt = d.runtime
+    st = setup(args.workload, d)
+    sampler = ClockSampler(local_rank)
+    rt.synchronize()
+    if not args.no_clocks:
+        sampler.start()
+    ms_total = time_device(rt, st, args.steps, warmup)
+    clocks = None
+    if not args.no_clocks:
+        keep_busy(rt, st, 1.5)
+        clocks = sampler.stop()
+    ms_step = ms_total / args.steps
+    tflops = st["flops"] / (ms_step * 1e-3) / 1e12
+    extras = contraction_extras(d, st)
+    e2e = None
+    if not args.no_e2e:
+        dt, h2d, d2h = time_e2e(d, st, steps=3)
+        e2e = {"value": st["flops"] / dt / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, peak_kind = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        peak, peak_kind = 1900.0, "fallback"
+    roofline = {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                "traffic": _traffic(args.workload), "peak_source": peak_kind,
+                "tensor_work_frac": 6 * tflops / peak,
+                "note": "achieved counts 2*M*N*K once; the tensor cores execute 6 bf16 products per output term"}
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            from oracle import cref
+            r = cref.time_contraction(C3[args.workload], budget_s=10.0)
+            cpu = {"value": r["tflops"], "unit": "TFLOP/s", "cores": r["threads"], "kind": "port", "sample": r["sample"]}
+        except Exception as e:
+            cpu = {"value": None, "unit": "TFLOP/s", "cores": None, "kind": "port", "sample": "failed: %s" % e}
+    line = {"metric": metric, "value": tflops, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3 split of f32 (fp32 accumulate)", "data": "synthetic (seeded reference RNG)",
+            "config": dict(st["config"], parallelism="single GPU"), "roofline": roofline, "accuracy": extras,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * 3, "clocks": clocks}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -206,13 +206,18 @@ def serialize(root: Node, out_shape: Sequence[int], kind: str = "ew",
     ND-range for a structurally equal closure of another shape; keying on the
     shape too avoids that.
     """
+    import sys
+    if sys.getrecursionlimit() < 200000:
+        sys.setrecursionlimit(200000)  # a J-term fold (split(d).reduce) nests J deep
     out_shape = tuple(int(s) for s in out_shape)
     lines: List[str] = ["ccir 1 %s" % kind, "o %d%s" % (len(out_shape), "".join(" %d" % d for d in out_shape))]
     params: List = []
-    node_ids: Dict[Tuple[int, int], int] = {}  # (id(node), frame) -> node number
+    # id(node) -> node number.  A node's line does not depend on the frame it is
+    # evaluated in (its matrices are sized by its own tensor's shape), so a
+    # subtree reached through several views is written once and shared.
+    node_ids: Dict[int, int] = {}
     param_ids: Dict[int, int] = {}  # id(ArrayParameter) -> node number
     inline_memo: Dict[int, bool] = {}
-    frames: Dict[Tuple[int, int], int] = {}  # (id(view site), parent frame) -> frame number
     counts_memo: Dict[int, Dict[int, int]] = {}
 
     def emit(line: str) -> int:
@@ -229,20 +234,20 @@ def serialize(root: Node, out_shape: Sequence[int], kind: str = "ew",
             counts_memo[id(tree)] = c
         return c
 
-    def gen(node: Node, frame_shape: Tuple[int, ...], frame: int, evals: float, counts: Dict[int, int]) -> int:
+    def gen(node: Node, frame_shape: Tuple[int, ...], evals: float, counts: Dict[int, int]) -> int:
         # ``evals``: how many times each element of this frame is evaluated per output element
-        key = (id(node), frame)
+        key = id(node)
         got = node_ids.get(key)
         if got is not None:
             return got
         if isinstance(node, Literal):
             nid = emit("l " + f32_bits(node.value))
         elif isinstance(node, Unary):
-            a = gen(node.a, frame_shape, frame, evals, counts)
+            a = gen(node.a, frame_shape, evals, counts)
             nid = emit("u %s %d" % (node.op, a))
         elif isinstance(node, Binary):
-            a = gen(node.a, frame_shape, frame, evals, counts)
-            b = gen(node.b, frame_shape, frame, evals, counts)
+            a = gen(node.a, frame_shape, evals, counts)
+            b = gen(node.b, frame_shape, evals, counts)
             nid = emit("b %s %d %d" % (node.op, a, b))
         elif isinstance(node, Extract):
             arr = node.array
@@ -271,13 +276,8 @@ def serialize(root: Node, out_shape: Sequence[int], kind: str = "ew",
             mtext = " ".join(_double_text(m) for m in matrix)
             if fuse:
                 inner_shape = tuple(param.shape)
-                fkey = (id(node), frame)
-                inner = frames.get(fkey)
-                if inner is None:
-                    inner = len(frames) + 1
-                    frames[fkey] = inner
                 closure = tensor.closure
-                sub = gen(closure, inner_shape, inner,
+                sub = gen(closure, inner_shape,
                           evals * elements(frame_shape) / max(1, elements(inner_shape)), counts_of(closure))
                 nid = emit("v %d %d%s %s %d%s" % (sub, rank, "".join(" %d" % d for d in inner_shape),
                                                   f32_bits(param.padding), cols, (" " + mtext) if mtext else ""))
@@ -297,11 +297,11 @@ def serialize(root: Node, out_shape: Sequence[int], kind: str = "ew",
 
     counts = counts_of(root)
     if isinstance(root, Concatenate):
-        ids = [gen(e, out_shape, 0, 1.0, counts) for e in root.elements]
+        ids = [gen(e, out_shape, 1.0, counts) for e in root.elements]
         t = emit("t %d%s" % (len(ids), "".join(" %d" % i for i in ids)))
         lines.append("r %d" % t)
     else:
-        r = gen(root, out_shape, 0, 1.0, counts)
+        r = gen(root, out_shape, 1.0, counts)
         lines.append("r %d" % r)
     n_nodes = len(lines) - 3
     return Serialized("\n".join(lines) + "\n", params, n_nodes)

@@ -10,6 +10,8 @@
 // that statement list sit the sm_103a skeletons: a grid-stride elementwise
 // loop (with a float4 variant when every input is read contiguously) and a
 // compensated full sum with a single-pass grid reduction.
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -17,6 +19,7 @@
 #include <functional>
 #include <map>
 #include <sstream>
+#include <initializer_list>
 #include <utility>
 
 #include "internal.h"
@@ -477,6 +480,68 @@ bool is_contiguous_identity(const IrNode &x, const IrNode &p, const std::vector<
 }
 
 }  // namespace
+
+namespace {
+
+bool matrix_is(const IrNode &n, std::initializer_list<double> want) {
+  if (n.m.size() != want.size()) return false;
+  size_t i = 0;
+  for (double w : want)
+    if (n.m[i++] != w) return false;
+  return true;
+}
+
+}  // namespace
+
+bool match_contraction(const Ir &ir, Contraction *out) {
+  if (ir.kind != ProgramKind::Elementwise || ir.out_shape.size() != 2) return false;
+  // the left spine of additions: ((t0 + t1) + t2) + ...
+  std::vector<int> terms;
+  int node = ir.root;
+  while (ir.nodes[node].kind == NodeKind::Binary && ir.nodes[node].op == (uint8_t)BinOp::Add) {
+    terms.push_back(ir.nodes[node].b);
+    node = ir.nodes[node].a;
+  }
+  terms.push_back(node);
+  if (terms.size() < 2) return false;
+  std::reverse(terms.begin(), terms.end());
+  const int64_t I = ir.out_shape[0], K = ir.out_shape[1], J = (int64_t)terms.size();
+  int sub = -1;
+  for (int64_t j = 0; j < J; ++j) {
+    const IrNode &v = ir.nodes[terms[j]];
+    if (v.kind != NodeKind::View || v.cols != 3) return false;
+    if (v.dims != std::vector<int64_t>{I, J, K}) return false;
+    if (!matrix_is(v, {1, 0, 0, 0, 0, (double)j, 0, 1, 0})) return false;
+    if (sub < 0) sub = v.a;
+    if (v.a != sub) return false;
+  }
+  const IrNode &mul = ir.nodes[sub];
+  if (mul.kind != NodeKind::Binary || mul.op != (uint8_t)BinOp::Mul) return false;
+  int a_in = -1, b_in = -1;
+  for (int operand : {mul.a, mul.b}) {
+    const IrNode &x = ir.nodes[operand];
+    if (x.kind != NodeKind::Extract || x.cols != 4) return false;
+    const IrNode &p = ir.nodes[x.a];
+    if (p.dims == std::vector<int64_t>{I, J} && matrix_is(x, {1, 0, 0, 0, 0, 1, 0, 0})) {
+      a_in = p.param_index;
+    } else if (p.dims == std::vector<int64_t>{1, J, K} &&
+               matrix_is(x, {0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0})) {
+      b_in = p.param_index;
+    } else if (p.dims == std::vector<int64_t>{J, K} && matrix_is(x, {0, 1, 0, 0, 0, 0, 1, 0})) {
+      b_in = p.param_index;
+    } else {
+      return false;
+    }
+  }
+  if (a_in < 0 || b_in < 0) return false;
+  if (I > INT32_MAX || J > INT32_MAX || K > INT32_MAX) return false;
+  out->a_input = a_in;
+  out->b_input = b_in;
+  out->m = I;
+  out->k = J;
+  out->n = K;
+  return true;
+}
 
 int choose_min_blocks(int64_t domain, int block, int sm_count, int override_blocks) {
   if (override_blocks > 0) return override_blocks;

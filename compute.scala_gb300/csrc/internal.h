@@ -101,6 +101,18 @@ struct Generated {
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);
 
+// The library's matmul idiom (TensorsSpec.scala:468-485, README.md:336-343):
+//   A.broadcast([I,J,K]) * B.reshape([1,J,K]).broadcast([I,J,K]), then
+//   split(1).reduce(_ + _)
+// which, with the product fused, arrives as a left fold over j of views that
+// select j from one product node A[i][j] * B[j][k].  On a match, C[I,K] =
+// A[I,J] * B[J,K] with A and B the given kernel inputs (row-major, dense).
+struct Contraction {
+  int a_input = -1, b_input = -1;
+  int64_t m = 0, k = 0, n = 0;  // C is m x n, the folded dimension has k terms
+};
+bool match_contraction(const Ir &ir, Contraction *out);
+
 // The literal text DecimalFormat gives a view coefficient (at most three
 // fraction digits, HALF_EVEN, no grouping), as OpenCLKernelBuilder.toLiteral.
 std::string decimal_format3(double v);

@@ -179,6 +179,9 @@ struct Program {
   int resident_vec4 = 0;
   ProgramKind kind = ProgramKind::Elementwise;
   Generated gen;
+  bool is_contraction = false;  // run as a GEMM (cc_gemm_f32 mode contraction_mode)
+  int contraction_mode = 0;
+  Contraction con;
 };
 
 struct Event {
@@ -218,6 +221,7 @@ struct Context {
   int64_t prefetch_min_bytes = -1;
   int sum_block = 256;
   int tc_variant = 0;
+  int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
 
@@ -313,7 +317,70 @@ int64_t ew_grid(int64_t work, int block, int sm_count, int resident) {
   return grid;
 }
 
+void encode_plane_map(CUtensorMap *map, void *base, int rows, int kcols, int box_rows) {
+  const cuuint64_t dims[2] = {(cuuint64_t)kcols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kcols * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  check_cu(g_drv.TensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE),
+           "cuTensorMapEncodeTiled");
+}
+
+// C[m,n] = A[m,k] * B[k,n] with the kernels of the given CC_GEMM_* mode.
+void run_gemm(Context &c, const float *A, const float *B, float *C, int m, int n, int k, int64_t lda, int64_t ldb,
+              int64_t ldc, int mode, cudaStream_t s) {
+  if (m == 0 || n == 0) return;
+  if (mode == CC_GEMM_EXACT || mode == CC_GEMM_FP32) {
+    check_cuda(launch_sgemm(A, B, C, m, n, k, lda, ldb, ldc, mode == CC_GEMM_EXACT, s), "sgemm launch");
+    return;
+  }
+  if (mode != CC_GEMM_BF16X6) fail(CC_ERR_INVALID_VALUE, "unknown contraction mode");
+  if (c.cc_major != 10) fail(CC_ERR_INVALID_OPERATION, "the tensor-core contraction needs an sm_10x GPU");
+  const int Mp = (m + kTcBM - 1) / kTcBM * kTcBM;
+  const int Np = (n + kTcBN - 1) / kTcBN * kTcBN;
+  const int Kp = (k + kTcBK - 1) / kTcBK * kTcBK;
+  size_t cls_a = 0, cls_b = 0;
+  const size_t bytes_a = (size_t)3 * Mp * Kp * 2, bytes_b = (size_t)3 * Np * Kp * 2;
+  void *pa = c.pool.alloc(bytes_a, &cls_a);
+  void *pb = nullptr;
+  try {
+    pb = c.pool.alloc(bytes_b, &cls_b);
+  } catch (...) {
+    c.pool.release(pa, cls_a);
+    throw;
+  }
+  cudaError_t e = launch_split_a(A, lda, m, k, static_cast<__nv_bfloat16 *>(pa), Mp, Kp, c.sm_count, s);
+  if (e == cudaSuccess) e = launch_split_bt(B, ldb, k, n, static_cast<__nv_bfloat16 *>(pb), Np, Kp, s);
+  if (e == cudaSuccess) {
+    CUtensorMap maps[6];
+    const size_t plane_a = (size_t)Mp * Kp * 2, plane_b = (size_t)Np * Kp * 2;
+    try {
+      for (int p = 0; p < 3; ++p) {
+        encode_plane_map(&maps[p], static_cast<char *>(pa) + p * plane_a, Mp, Kp, kTcBM);
+        encode_plane_map(&maps[3 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp, gemm_tc_box_n(c.tc_variant));
+      }
+    } catch (...) {
+      c.pool.release(pa, cls_a);
+      c.pool.release(pb, cls_b);
+      throw;
+    }
+    e = launch_gemm_bf16x6(maps, C, m, n, Kp, ldc, c.sm_count, c.error_flag(), c.tc_variant, s);
+  }
+  if (s != c.stream && e == cudaSuccess) e = cudaStreamSynchronize(s);  // the pool is ordered on the context stream
+  c.pool.release(pa, cls_a);
+  c.pool.release(pb, cls_b);
+  check_cuda(e, "bf16x6 contraction launch");
+}
+
 void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
+  if (p.is_contraction) {
+    const Contraction &q = p.con;
+    run_gemm(c, reinterpret_cast<const float *>(in[q.a_input]), reinterpret_cast<const float *>(in[q.b_input]),
+             reinterpret_cast<float *>(out), (int)q.m, (int)q.n, (int)q.k, q.k, q.n, q.n, p.contraction_mode, stream);
+    return;
+  }
   const int block = p.block;
   const int64_t n = p.gen.domain;
   bool aligned = (out & 15u) == 0;
@@ -528,6 +595,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "sum_block") {
     if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
     c.sum_block = (int)value;
+  } else if (k == "contraction") {
+    if (value < 0 || value > 3) fail(CC_ERR_INVALID_VALUE, "contraction must be in [0, 3]");
+    c.contraction = (int)value;
   } else if (k == "tc_variant") {
     if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "tc_variant must be 0, 1 or 2");
     c.tc_variant = (int)value;
@@ -559,6 +629,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "prefetch_min_bytes") *value = c.prefetch_min_bytes;
   else if (k == "sum_block") *value = c.sum_block;
   else if (k == "tc_variant") *value = c.tc_variant;
+  else if (k == "contraction") *value = c.contraction;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END
 }
@@ -720,7 +791,8 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   }
   key += "#lookahead " + std::to_string(opt.load_lookahead) + " asm " + std::to_string((int)opt.asm_loads) +
          " blocks " + std::to_string(-opt.min_blocks) + " block " + std::to_string(opt.block) + " unroll " + std::to_string(opt.vec_unroll) +
-         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " sumblock " + std::to_string(c.sum_block) + "\n";
+         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " sumblock " + std::to_string(c.sum_block) +
+         " contraction " + std::to_string(c.contraction) + " tc " + std::to_string(c.tc_variant) + "\n";
   {
     std::lock_guard<std::recursive_mutex> g(c.mu);
     auto it = c.cache.find(key);
@@ -742,6 +814,31 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   }
   Ir ir = parse_ir(ir_text, ir_len);
   if (ir.kind == ProgramKind::Sum) opt.block = c.sum_block;
+  Contraction con;
+  int contraction_knob;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    contraction_knob = c.contraction;
+  }
+  if (contraction_knob > 0 && match_contraction(ir, &con)) {
+    auto p = std::make_unique<Program>();
+    p->kind = ProgramKind::Elementwise;
+    p->is_contraction = true;
+    p->contraction_mode = contraction_knob - 1;
+    p->con = con;
+    p->gen.n_inputs = ir.n_params;
+    p->gen.out_elems = con.m * con.n;
+    p->gen.domain = con.m * con.n;
+    p->gen.source = "// contraction: C[" + std::to_string(con.m) + "," + std::to_string(con.n) + "] = A * B over " +
+                    std::to_string(con.k) + " terms, cc_gemm_f32 mode " + std::to_string(p->contraction_mode) + "\n";
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    uint64_t h = c.make_handle(kTagProgram);
+    c.programs[h] = p.release();
+    c.cache[key] = h;
+    ++c.cache_misses;
+    *out = h;
+    return CC_OK;
+  }
   {
     int64_t domain = 1;
     for (int64_t d : ir.out_shape) domain *= d;
@@ -774,6 +871,11 @@ int cc_codegen(const char *ir_text, size_t ir_len, char *buf, size_t len, size_t
   if (!ir_text) fail(CC_ERR_INVALID_VALUE, "null pointer");
   Ir ir = parse_ir(ir_text, ir_len);
   Generated gen = generate_cuda(ir, CodegenOptions{});
+  Contraction con;
+  if (match_contraction(ir, &con))
+    gen.source = "// contraction m=" + std::to_string(con.m) + " n=" + std::to_string(con.n) + " k=" +
+                 std::to_string(con.k) + " a=" + std::to_string(con.a_input) + " b=" + std::to_string(con.b_input) +
+                 "\n" + gen.source;
   if (needed) *needed = gen.source.size() + 1;
   if (buf && len) {
     size_t n = gen.source.size() < len - 1 ? gen.source.size() : len - 1;
@@ -888,23 +990,6 @@ int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stre
   CC_API_END
 }
 
-namespace cc {
-namespace {
-
-void encode_plane_map(CUtensorMap *map, void *base, int rows, int kcols, int box_rows) {
-  const cuuint64_t dims[2] = {(cuuint64_t)kcols, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)kcols * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
-  const cuuint32_t estr[2] = {1, 1};
-  check_cu(g_drv.TensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
-                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE),
-           "cuTensorMapEncodeTiled");
-}
-
-}  // namespace
-}  // namespace cc
-
 int cc_gemm_f32(uint64_t a_ptr, uint64_t b_ptr, uint64_t c_ptr, int m, int n, int k, int64_t lda, int64_t ldb,
                 int64_t ldc, int mode, uint64_t stream) {
   CC_API_BEGIN
@@ -913,50 +998,8 @@ int cc_gemm_f32(uint64_t a_ptr, uint64_t b_ptr, uint64_t c_ptr, int m, int n, in
   if (m < 0 || n < 0 || k <= 0 || lda < k || ldb < n || ldc < n) fail(CC_ERR_INVALID_VALUE, "bad matrix shape");
   std::lock_guard<std::recursive_mutex> g(c.mu);
   cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
-  const float *A = reinterpret_cast<const float *>(a_ptr);
-  const float *B = reinterpret_cast<const float *>(b_ptr);
-  float *C = reinterpret_cast<float *>(c_ptr);
-  if (m == 0 || n == 0) return CC_OK;
-  if (mode == CC_GEMM_EXACT || mode == CC_GEMM_FP32) {
-    check_cuda(launch_sgemm(A, B, C, m, n, k, lda, ldb, ldc, mode == CC_GEMM_EXACT, s), "sgemm launch");
-    return CC_OK;
-  }
-  if (mode != CC_GEMM_BF16X6) fail(CC_ERR_INVALID_VALUE, "unknown contraction mode");
-  if (c.cc_major != 10) fail(CC_ERR_INVALID_OPERATION, "the tensor-core contraction needs an sm_10x GPU");
-  const int Mp = (m + kTcBM - 1) / kTcBM * kTcBM;
-  const int Np = (n + kTcBN - 1) / kTcBN * kTcBN;
-  const int Kp = (k + kTcBK - 1) / kTcBK * kTcBK;
-  size_t cls_a = 0, cls_b = 0;
-  const size_t bytes_a = (size_t)3 * Mp * Kp * 2, bytes_b = (size_t)3 * Np * Kp * 2;
-  void *pa = c.pool.alloc(bytes_a, &cls_a);
-  void *pb = nullptr;
-  try {
-    pb = c.pool.alloc(bytes_b, &cls_b);
-  } catch (...) {
-    c.pool.release(pa, cls_a);
-    throw;
-  }
-  cudaError_t e = launch_split_a(A, lda, m, k, static_cast<__nv_bfloat16 *>(pa), Mp, Kp, c.sm_count, s);
-  if (e == cudaSuccess) e = launch_split_bt(B, ldb, k, n, static_cast<__nv_bfloat16 *>(pb), Np, Kp, s);
-  if (e == cudaSuccess) {
-    CUtensorMap maps[6];
-    const size_t plane_a = (size_t)Mp * Kp * 2, plane_b = (size_t)Np * Kp * 2;
-    try {
-      for (int p = 0; p < 3; ++p) {
-        encode_plane_map(&maps[p], static_cast<char *>(pa) + p * plane_a, Mp, Kp, kTcBM);
-        encode_plane_map(&maps[3 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp, gemm_tc_box_n(c.tc_variant));
-      }
-    } catch (...) {
-      c.pool.release(pa, cls_a);
-      c.pool.release(pb, cls_b);
-      throw;
-    }
-    e = launch_gemm_bf16x6(maps, C, m, n, Kp, ldc, c.sm_count, c.error_flag(), c.tc_variant, s);
-  }
-  if (s != c.stream && e == cudaSuccess) e = cudaStreamSynchronize(s);  // the pool is ordered on the context stream
-  c.pool.release(pa, cls_a);
-  c.pool.release(pb, cls_b);
-  check_cuda(e, "bf16x6 contraction launch");
+  run_gemm(c, reinterpret_cast<const float *>(a_ptr), reinterpret_cast<const float *>(b_ptr),
+           reinterpret_cast<float *>(c_ptr), m, n, k, lda, ldb, ldc, mode, s);
   CC_API_END
 }
 

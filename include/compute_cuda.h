@@ -79,6 +79,10 @@ int cc_synchronize(void);
  *   "upload_streams"    copy streams a large cc_buf_upload is striped over (1..8; default 4)
  *   "ew_lookahead"      loads a generated kernel keeps in flight ahead of its arithmetic (0..256; default 8)
  *   "ew_asm_loads"      1: those loads are volatile inline PTX so the compiler keeps their order (default 1)
+ *   "contraction"       how a program that is the library's matmul idiom runs (a left fold over j
+ *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
+ *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
+ *                       3 = CC_GEMM_BF16X6
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
  *                       registers (FP32-level error at any K; default), 1 = 128x256 tiles, one
  *                       accumulator per tile (fastest, error grows with K), 2 = 128x128, one per tile

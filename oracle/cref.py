@@ -255,3 +255,53 @@ def time_workload(workload: str, budget_s: float = 15.0, threads=None):
                           "16-lane sequential sum" % reps,
                 "config": {"workload": "fused elementwise+sum (reference CPU path, OpenCL C on host cores)"}}
     raise ValueError(workload)
+
+
+FOLD_GEMM_C = r"""
+/* The reference's matmul semantics (TensorsSpec.scala:468-485): each output is
+ * the left fold over k of separately rounded float products, in k order.
+ * Rows are spread over OpenMP threads; the j loop vectorises. */
+void cc_fold_gemm(const float *restrict A, const float *restrict B, float *restrict C, int m, int n, int k) {
+  #pragma omp parallel for schedule(static)
+  for (int i = 0; i < m; ++i) {
+    float *restrict c = C + (long)i * n;
+    const float *restrict a = A + (long)i * k;
+    for (int j = 0; j < n; ++j) c[j] = a[0] * B[j];
+    for (int kk = 1; kk < k; ++kk) {
+      const float av = a[kk];
+      const float *restrict b = B + (long)kk * n;
+      for (int j = 0; j < n; ++j) c[j] = c[j] + av * b[j];
+    }
+  }
+}
+"""
+
+
+def time_contraction(shape, budget_s: float = 15.0, threads=None):
+    """TFLOP/s of the reference's contraction semantics on the host cores, on a row sample.
+
+    The reference itself would materialise the I*J*K product (256 GiB at these
+    shapes); this times the same arithmetic without that, so it is an upper
+    bound for the reference's CPU path.
+    """
+    m, k, n = shape
+    threads = threads or _threads()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    lib = _compile(FOLD_GEMM_C, "foldgemm")
+    lib.cc_fold_gemm.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 3
+    lib.cc_fold_gemm.restype = None
+    b = rng.random_normal(k * n, 0x40000001).reshape(k, n)
+    rows = max(threads, 1)
+    while True:
+        a = rng.random_normal(rows * k, 0x40000000).reshape(rows, k)
+        c = np.empty((rows, n), dtype=np.float32)
+        t0 = time.perf_counter()
+        lib.cc_fold_gemm(a.ctypes.data, b.ctypes.data, c.ctypes.data, rows, n, k)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or rows >= m:
+            break
+        rows = min(m, rows * 4)
+    tflops = 2.0 * rows * n * k / dt / 1e12
+    return {"tflops": tflops, "ms_per_step": dt * 1e3 * m / rows, "threads": threads,
+            "sample": "%d of %d rows of A[%d,%d] x B[%d,%d]; sequential-k FP32 fold, OpenMP over rows" % (rows, m, m, k, k, n),
+            "config": {"workload": "contraction (reference fold semantics on host cores)", "shape": [m, k, n]}}

@@ -83,3 +83,37 @@ def test_split_bf16_tensor_core_mode(cuda_device, shape):
     assert err <= 1e-6, err
     a.close()
     b.close()
+
+
+def _api_matmul(device, m1, m2):
+    """TensorsSpec.scala:472-478, through the Tensor API."""
+    i, j = m1.shape
+    _, k = m2.shape
+    prod = m1.broadcast([i, j, k]) * m2.reshape([1, j, k]).broadcast([i, j, k])
+    return prod.split(1).reduce(lambda x, y: x + y)
+
+
+def test_matmul_idiom_through_the_api_in_every_contraction_mode(cuda_device):
+    rt = cuda_device.runtime
+    T = cuda_device.Tensor
+    m, k, n = 64, 300, 96
+    a = T.randomNormal([m, k], seed=SEED).doCache()
+    b = T.randomNormal([k, n], seed=SEED + 1).doCache()
+    want = reference_fold(a.flatArray().reshape(m, k), b.flatArray().reshape(k, n))
+    ref64 = a.flatArray().reshape(m, k).astype(np.float64) @ b.flatArray().reshape(k, n).astype(np.float64)
+    saved = rt.config_get("contraction")
+    got = {}
+    try:
+        for mode in (0, 1, 2, 3):
+            rt.config_set("contraction", mode)
+            c = _api_matmul(cuda_device, a, b)
+            got[mode] = c.flatArray().reshape(m, n)
+            assert rt.device_errors() == 0
+    finally:
+        rt.config_set("contraction", saved)
+    assert np.array_equal(got[0].view(np.int32), want.view(np.int32))  # the generated fold
+    assert np.array_equal(got[1].view(np.int32), want.view(np.int32))  # the exact GEMM
+    assert rel_fro(got[2], ref64) <= 1e-6
+    assert rel_fro(got[3], ref64) <= 1e-6
+    a.close()
+    b.close()

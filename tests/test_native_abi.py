@@ -87,3 +87,36 @@ def test_compile_failure_carries_the_nvrtc_log():
     with pytest.raises(_native.BuildProgramFailure) as e:
         compile_check(ir, (1, 0))
     assert "NVRTC" in str(e.value)
+
+
+def _matmul_ir(i, j, k, swap=False):
+    from compute import Tensors
+    d = Tensors(runtime=object())
+    T = d.Tensor
+    m1 = T.randomNormal([i, j], seed=1)
+    m2 = T.randomNormal([j, k], seed=2)
+    a = m1.broadcast([i, j, k])
+    b = m2.reshape([1, j, k]).broadcast([i, j, k])
+    prod = b * a if swap else a * b
+    c = prod.split(1).reduce(lambda x, y: x + y)
+    return d.serialize(c.closure, c.shape).text
+
+
+def test_the_matmul_idiom_is_recognised_as_a_contraction():
+    """TensorsSpec.scala:472-478's matmul reaches the runtime as one fused fold, recognised as C = A * B."""
+    src = codegen(_matmul_ir(5, 7, 3))
+    assert src.startswith("// contraction m=5 n=3 k=7 a=0 b=1")
+    src = codegen(_matmul_ir(5, 7, 3, swap=True))
+    assert src.startswith("// contraction m=5 n=3 k=7 a=1 b=0")
+    # a fold whose terms are not the split views of one product is not a contraction
+    from compute import Tensors
+    d = Tensors(runtime=object())
+    T = d.Tensor
+    t = T.randomNormal([4, 6, 3], seed=1)
+    s = t.split(1).reduce(lambda x, y: x + y)
+    assert not codegen(d.serialize(s.closure, s.shape).text).startswith("// contraction")
+
+
+def test_a_long_fold_serialises():
+    text = _matmul_ir(8, 2048, 8)
+    assert text.count("\nv ") == 2048
