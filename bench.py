@@ -137,6 +137,46 @@ def matmul_expr(T, a, b):
     return prod.split(1).reduce(lambda x, y: x + y)
 
 
+def c4_programs(T, seed=0, count=2048, lo=1024, hi=4194304, shapes_only=False):
+    """The batched-programs workload: `count` independent fused programs, lengths
+    log-uniform on [lo, hi], each a random expression tree of 3-12 operator
+    nodes over {+,-,*,/,exp,log,tanh,max} on 1-4 inputs uniform in [0.1, 2]."""
+    import numpy as np
+    r = np.random.RandomState(seed)
+    progs = []
+    for p in range(count):
+        n = int(round(float(np.exp(r.uniform(np.log(lo), np.log(hi))))))
+        n_in = int(r.randint(1, 5))
+        n_nodes = int(r.randint(3, 13))
+        ops = [r.choice(["+", "-", "*", "/", "exp", "log", "tanh", "max"]) for _ in range(n_nodes)]
+        picks = [(int(r.randint(0, 1 << 30)), int(r.randint(0, 1 << 30))) for _ in range(n_nodes)]
+        progs.append((n, n_in, ops, picks, int(r.randint(0, 1 << 30))))
+    if shapes_only:
+        return progs
+    out = []
+    for n, n_in, ops, picks, in_seed in progs:
+        inputs = [(T.random([n], seed=in_seed + i) * T.fill(1.9, [n]) + T.fill(0.1, [n])).doCache() for i in range(n_in)]
+        pool = list(inputs)
+        for op, (pa, pb) in zip(ops, picks):
+            a = pool[-1]  # keep the tree connected: every node uses the previous one
+            b = pool[pb % len(pool)]
+            if op == "+":
+                t = a + b
+            elif op == "-":
+                t = a - b
+            elif op == "*":
+                t = a * b
+            elif op == "/":
+                t = a / b
+            elif op == "max":
+                t = T.max(a, b)
+            else:
+                t = getattr(T, op)(a)
+            pool.append(t)
+        out.append((pool[-1], inputs))
+    return out
+
+
 def setup(workload, d):
     """Returns (program, list of input-buffer lists to rotate over, output buffer, bytes, description)."""
     T = d.Tensor
@@ -320,7 +360,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s", "c4"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true", help="skip the clock sampling (and its untimed busy loop)")
@@ -333,6 +373,8 @@ def main():
     metric = "fused-op GB/s"
     if args.workload in C3:
         return main_contraction(args, warmup, rank, world, local_rank)
+    if args.workload == "c4":
+        return main_batch(args, warmup, rank, world, local_rank)
 
     if args.impl == "reference":
         if rank != 0:
@@ -405,6 +447,76 @@ def main():
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def main_batch(args, warmup, rank, world, local_rank):
+    """The batched-programs workload: 2048 independent fused programs evaluated by
+    one persistent launch; the same programs launched one by one, and replayed
+    from a CUDA graph, are the comparison."""
+    from compute import Tensors
+    from compute.batch import Batch
+    d = Tensors(device=local_rank)
+    rt = d.runtime
+    T = d.Tensor
+    t0 = time.time()
+    progs = c4_programs(T, seed=0)
+    tensors = [t for t, _ in progs]
+    b = Batch(d, tensors).bind()
+    setup_s = time.time() - t0
+    nbytes = 0
+    for t, ser in zip(tensors, b.serialized):
+        n = 1
+        for s_ in t.shape:
+            n *= s_
+        nbytes += 4 * n * (len(ser.params) + 1)
+    n_progs, n_structs, regs, resident = rt.batch_info(b.handle)
+
+    def timed(mode, steps):
+        for _ in range(max(3, warmup)):
+            b.run(mode)
+        rt.synchronize()
+        e0 = rt.event()
+        for _ in range(steps):
+            b.run(mode)
+        e1 = rt.event()
+        rt.event_wait(e1, 600 * 10 ** 9)
+        ms = rt.event_elapsed_ms(e0, e1) / steps
+        rt.event_release(e0)
+        rt.event_release(e1)
+        return ms
+
+    sampler = ClockSampler(local_rank)
+    if not args.no_clocks:
+        sampler.start()
+    ms_persistent = timed(Batch.PERSISTENT, args.steps)
+    clocks = None
+    if not args.no_clocks:
+        t_end = time.time() + 1.5
+        while time.time() < t_end:
+            b.run(Batch.PERSISTENT)
+            rt.synchronize()
+        clocks = sampler.stop()
+    k2 = max(3, min(args.steps, 20))
+    ms_each = timed(Batch.PER_PROGRAM, k2)
+    ms_graph = timed(Batch.GRAPH, k2)
+    gbs = nbytes / (ms_persistent * 1e-3) / 1e9
+    peak, peak_kind = _peaks()
+    line = {"metric": "fused-op GB/s", "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": warmup, "ms_per_step": ms_persistent, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
+            "config": {"workload": "batched uneven programs: 2048 random fused programs (3-12 nodes over "
+                                   "+,-,*,/,exp,log,tanh,max; 1-4 inputs U[0.1,2]), lengths log-uniform [1K,4M]",
+                       "programs": n_progs, "distinct_structures": n_structs, "bytes_per_step": nbytes,
+                       "persistent_registers": regs, "persistent_blocks_per_sm": resident,
+                       "l2": "inputs %.1f GB > L2" % (nbytes / 1e9), "setup_s": round(setup_s, 1),
+                       "parallelism": "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "traffic": _traffic("c4"), "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes},
+            "batch": {"persistent_ms": ms_persistent, "per_program_ms": ms_each, "graph_ms": ms_graph,
+                      "speedup_vs_per_program": ms_each / ms_persistent, "speedup_vs_graph": ms_graph / ms_persistent},
+            "cpu_baseline": None, "e2e": None, "gpu_launches": args.steps, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    b.close()
 
 
 def main_contraction(args, warmup, rank, world, local_rank):

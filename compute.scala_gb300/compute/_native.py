@@ -145,6 +145,14 @@ _SIGNATURES = {
     "cc_gemm_f32": [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                     ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64],
     "cc_device_errors": [ctypes.POINTER(ctypes.c_int)],
+    "cc_batch_create": [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(c_size), ctypes.c_int, ctypes.POINTER(c_handle)],
+    "cc_batch_info": [c_handle, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                      ctypes.POINTER(ctypes.c_int)],
+    "cc_batch_bind": [c_handle, ctypes.POINTER(ctypes.c_uint64), c_size],
+    "cc_batch_run": [c_handle, ctypes.c_int, ctypes.c_uint64],
+    "cc_batch_release": [c_handle],
+    "cc_batch_compile_check": [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(c_size), ctypes.c_int, ctypes.c_int,
+                               ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
     "cc_event_record": [ctypes.POINTER(c_handle)],
     "cc_event_query": [c_handle, ctypes.POINTER(ctypes.c_int)],
     "cc_event_wait": [c_handle, ctypes.c_uint64],

@@ -166,6 +166,33 @@ class NativeRuntime:
         call("cc_device_errors", ctypes.byref(v))
         return v.value
 
+    # -- batches (many independent contiguous elementwise programs)
+    BATCH_PERSISTENT, BATCH_PER_PROGRAM, BATCH_GRAPH = 0, 1, 2
+
+    def batch_create(self, texts: Sequence[str]) -> int:
+        raws = [t.encode() for t in texts]
+        arr = (ctypes.c_char_p * len(raws))(*raws)
+        lens = (ctypes.c_size_t * len(raws))(*[len(r) for r in raws])
+        h = c_handle()
+        call("cc_batch_create", arr, lens, len(raws), ctypes.byref(h))
+        return h.value
+
+    def batch_info(self, batch: int):
+        """(programs, distinct structures, registers per thread, resident blocks per SM) of a batch."""
+        n, k, r, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        call("cc_batch_info", c_handle(batch), ctypes.byref(n), ctypes.byref(k), ctypes.byref(r), ctypes.byref(b))
+        return n.value, k.value, r.value, b.value
+
+    def batch_bind(self, batch: int, ptrs: Sequence[int]):
+        arr = (ctypes.c_uint64 * len(ptrs))(*ptrs)
+        call("cc_batch_bind", c_handle(batch), arr, ctypes.c_size_t(len(ptrs)))
+
+    def batch_run(self, batch: int, mode: int = 0, stream: int = 0):
+        call("cc_batch_run", c_handle(batch), int(mode), ctypes.c_uint64(stream))
+
+    def batch_release(self, batch: int):
+        call("cc_batch_release", c_handle(batch))
+
     # -- events
     def event(self) -> int:
         h = c_handle()
@@ -192,6 +219,16 @@ def codegen(ir_text: str) -> str:
     buf = ctypes.create_string_buffer(need.value)
     call("cc_codegen", raw, ctypes.c_size_t(len(raw)), buf, need.value, ctypes.byref(need))
     return buf.value.decode()
+
+
+def batch_compile_check(texts, cc=(10, 3)):
+    """NVRTC-compiles the batch module of these programs (no GPU needed); returns (structures, seconds)."""
+    raws = [t.encode() for t in texts]
+    arr = (ctypes.c_char_p * len(raws))(*raws)
+    lens = (ctypes.c_size_t * len(raws))(*[len(r) for r in raws])
+    k, secs = ctypes.c_int(), ctypes.c_double()
+    call("cc_batch_compile_check", arr, lens, len(raws), int(cc[0]), int(cc[1]), ctypes.byref(k), ctypes.byref(secs))
+    return k.value, secs.value
 
 
 def compile_check(ir_text: str, cc=(10, 3), flags: int = 0) -> None:

@@ -234,10 +234,13 @@ std::string decimal_format3(double v) {
 
 namespace {
 
+}  // namespace
 // device_common.cuh, embedded at build time as a string literal.
+extern const char *kPrelude;
 const char *kPrelude =
 #include "device_common.inc"
     ;
+namespace {
 
 std::string lit_code(uint32_t bits) {
   char b[48];
@@ -261,8 +264,10 @@ struct Stmt {
 
 class Generator {
  public:
-  Generator(const Ir &ir, bool contiguous_mode, bool asm_loads = false, int64_t prefetch_min_bytes = -1)
-      : ir_(ir), contig_(contiguous_mode), asm_loads_(asm_loads), prefetch_min_bytes_(prefetch_min_bytes) {}
+  Generator(const Ir &ir, bool contiguous_mode, bool asm_loads = false, int64_t prefetch_min_bytes = -1,
+            bool shared_transcendentals = false)
+      : ir_(ir), contig_(contiguous_mode), asm_loads_(asm_loads), prefetch_min_bytes_(prefetch_min_bytes),
+        shared_transcendentals_(shared_transcendentals) {}
 
   // Returns the name of the variable holding node `n` evaluated in frame `f`;
   // the statements computing it are appended to the statement list.
@@ -281,10 +286,12 @@ class Generator {
         std::string a = gen(node.a, f);
         v = fresh();
         static const char *fn[] = {"-", "expf", "logf", "tanhf", "fabsf", "sqrtf"};
+        static const char *shared_fn[] = {"-", "cc_expf", "cc_logf", "cc_tanhf", "fabsf", "sqrtf"};
         if (node.op == (uint8_t)UnOp::Neg)
           add(Cat::Compute, "const float " + v + " = -" + a + ";");
         else
-          add(Cat::Compute, "const float " + v + " = " + fn[node.op] + "(" + a + ");");
+          add(Cat::Compute, "const float " + v + " = " + (shared_transcendentals_ ? shared_fn : fn)[node.op] + "(" +
+                                a + ");");
         break;
       }
       case NodeKind::Binary: {
@@ -461,6 +468,7 @@ class Generator {
   bool contig_;
   bool asm_loads_;
   int64_t prefetch_min_bytes_;
+  bool shared_transcendentals_;
   bool fp64_ = false;
   int next_var_ = 0;
   int next_frame_ = 1;
@@ -543,6 +551,35 @@ bool match_contraction(const Ir &ir, Contraction *out) {
   return true;
 }
 
+bool is_batchable(const Ir &ir, std::string *why) {
+  auto no = [&](const char *m) {
+    if (why) *why = m;
+    return false;
+  };
+  if (ir.kind != ProgramKind::Elementwise) return no("only elementwise programs are batched");
+  if (ir.nodes[ir.root].kind == NodeKind::Tuple) return no("tuple-valued programs are not batched");
+  if (ir.n_params > kBatchMaxInputs) return no("a batched program has at most 4 inputs");
+  for (const IrNode &n : ir.nodes) {
+    if (n.kind == NodeKind::View) return no("a batched program reads its inputs without views");
+    if (n.kind == NodeKind::Extract && !is_contiguous_identity(n, ir.nodes[n.a], ir.out_shape))
+      return no("a batched program reads its inputs without views");
+  }
+  return true;
+}
+
+std::string point_function(const Ir &ir, const std::string &name, bool inline_it, bool shared_transcendentals) {
+  Generator gen(ir, true, false, -1, shared_transcendentals);
+  std::ostringstream body;
+  Frame f0{0, {}, ir.out_shape};
+  std::string r = gen.gen(ir.root, f0);
+  gen.emit(body, 2, 0);
+  std::ostringstream o;
+  o << "__device__ " << (inline_it ? "__forceinline__" : "__noinline__") << " float " << name << "(";
+  for (int i = 0; i < kBatchMaxInputs; ++i) o << (i ? ", " : "") << "float a" << i;
+  o << ") {\n" << body.str() << "  return " << r << ";\n}\n";
+  return o.str();
+}
+
 int choose_min_blocks(int64_t domain, int block, int sm_count, int override_blocks) {
   if (override_blocks > 0) return override_blocks;
   if (sm_count <= 0) return 0;
@@ -552,6 +589,61 @@ int choose_min_blocks(int64_t domain, int block, int sm_count, int override_bloc
   if (max_per_sm > 32) max_per_sm = 32;  // resident blocks per SM
   if (per_sm <= max_per_sm) return (int)(per_sm < 1 ? 1 : per_sm);
   return 4;
+}
+
+namespace {
+
+bool program_is_contiguous(const Ir &ir) {
+  const IrNode &root = ir.nodes[ir.root];
+  if (root.kind == NodeKind::Tuple) return false;
+  int64_t domain = 1;
+  for (int64_t d : ir.out_shape) domain *= d;
+  if (domain <= 0) return false;
+  for (const IrNode &n : ir.nodes) {
+    if (n.kind == NodeKind::View) return false;
+    if (n.kind == NodeKind::Extract && !is_contiguous_identity(n, ir.nodes[n.a], ir.out_shape)) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+std::string contiguous_structure_key(const Ir &ir) {
+  if (!program_is_contiguous(ir)) return std::string();
+  std::ostringstream o;
+  o << "contiguous " << (ir.kind == ProgramKind::Sum ? "sum" : "ew") << "\n";
+  char b[16];
+  for (const IrNode &n : ir.nodes) {
+    switch (n.kind) {
+      case NodeKind::Param:
+        snprintf(b, sizeof b, "%08x", n.bits);
+        o << "p " << b << "\n";
+        break;
+      case NodeKind::Literal:
+        snprintf(b, sizeof b, "%08x", n.bits);
+        o << "l " << b << "\n";
+        break;
+      case NodeKind::Extract: o << "x " << n.a << "\n"; break;
+      case NodeKind::Unary: o << "u " << kUnNames[n.op] << " " << n.a << "\n"; break;
+      case NodeKind::Binary: o << "b " << kBinNames[n.op] << " " << n.a << " " << n.b << "\n"; break;
+      default: return std::string();
+    }
+  }
+  o << "r " << ir.root << "\n";
+  return o.str();
+}
+
+Generated describe_program(const Ir &ir) {
+  Generated g;
+  g.n_inputs = ir.n_params;
+  const IrNode &root = ir.nodes[ir.root];
+  g.tuple_len = root.kind == NodeKind::Tuple ? (int)root.elems.size() : 1;
+  int64_t domain = 1;
+  for (int64_t d : ir.out_shape) domain *= d;
+  g.domain = domain;
+  g.out_elems = ir.kind == ProgramKind::Sum ? 1 : domain * g.tuple_len;
+  g.has_vec4 = program_is_contiguous(ir);
+  return g;
 }
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
@@ -683,7 +775,35 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     return o.str();
   };
 
-  if (ir.kind == ProgramKind::Elementwise) {
+  // Scalar loads of the contiguous form: the kernel needs no shape, only n.
+  std::string contig_scalar;
+  if (contiguous) {
+    for (int i = 0; i < ir.n_params; ++i)
+      contig_scalar += "    const float v" + std::to_string(i) + " = __ldg(in" + std::to_string(i) + " + lin);\n";
+  }
+  if (ir.kind == ProgramKind::Elementwise && contiguous) {
+    src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_ew(" << params
+        << "float *__restrict__ out, cc_i64 n) {\n"
+        << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+        << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
+        << contig_scalar << "    out[lin] = " << contig_call("") << ";\n  }\n}\n\n"
+        << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_ew_v4(" << params
+        << "float *__restrict__ out, cc_i64 n) {\n"
+        << vec4_loop(ir.n_params, U, true, contig_call) << "}\n\n";
+  } else if (ir.kind == ProgramKind::Sum && contiguous) {
+    src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum(" << params
+        << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
+        << "  float s_ = 0.0f, c_ = 0.0f;\n"
+        << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+        << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
+        << contig_scalar << "    cc_acc(s_, c_, " << contig_call("") << ");\n  }\n"
+        << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n"
+        << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum_v4(" << params
+        << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
+        << "  float s_ = 0.0f, c_ = 0.0f;\n"
+        << vec4_loop(ir.n_params, U, false, contig_call)
+        << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+  } else if (ir.kind == ProgramKind::Elementwise) {
     src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_ew(" << params
         << "float *__restrict__ out, cc_i64 n) {\n"
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"

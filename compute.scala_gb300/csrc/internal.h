@@ -37,8 +37,13 @@ struct Driver {
   decltype(&::cuCtxGetCurrent) CtxGetCurrent = nullptr;
   decltype(&::cuCtxSetCurrent) CtxSetCurrent = nullptr;
   decltype(&::cuFuncSetAttribute) FuncSetAttribute = nullptr;
+  decltype(&::cuFuncGetAttribute) FuncGetAttribute = nullptr;
   decltype(&::cuTensorMapEncodeTiled) TensorMapEncodeTiled = nullptr;
   decltype(&::cuOccupancyMaxActiveBlocksPerMultiprocessor) OccupancyMaxActiveBlocks = nullptr;
+  decltype(&::cuLinkCreate) LinkCreate = nullptr;
+  decltype(&::cuLinkAddData) LinkAddData = nullptr;
+  decltype(&::cuLinkComplete) LinkComplete = nullptr;
+  decltype(&::cuLinkDestroy) LinkDestroy = nullptr;
 };
 extern Driver g_drv;
 
@@ -100,6 +105,11 @@ struct Generated {
 };
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);
+// The shape information of generate_cuda without generating code.
+Generated describe_program(const Ir &ir);
+// For a program that reads every input contiguously with the output's shape
+// (no views): a key that identifies its code whatever the shape.  Empty otherwise.
+std::string contiguous_structure_key(const Ir &ir);
 
 // The library's matmul idiom (TensorsSpec.scala:468-485, README.md:336-343):
 //   A.broadcast([I,J,K]) * B.reshape([1,J,K]).broadcast([I,J,K]), then
@@ -112,6 +122,19 @@ struct Contraction {
   int64_t m = 0, k = 0, n = 0;  // C is m x n, the folded dimension has k terms
 };
 bool match_contraction(const Ir &ir, Contraction *out);
+
+// Batching: a program is batchable when it is an elementwise program whose
+// inputs are all read contiguously with the output's shape (the float4 form)
+// and it has at most kBatchMaxInputs inputs.
+constexpr int kBatchMaxInputs = 4;
+bool is_batchable(const Ir &ir, std::string *why);
+// `__device__ float <name>(float a0, ..., float a<kBatchMaxInputs-1>)`: the
+// program's value at one point from its inputs' values there (unused
+// arguments are ignored).  With shared_transcendentals, exp/log/tanh go through
+// the module's cc_expf/cc_logf/cc_tanhf (the same functions, called, which keeps
+// the code of thousands of structures small).
+std::string point_function(const Ir &ir, const std::string &name, bool inline_it = true,
+                           bool shared_transcendentals = false);
 
 // The literal text DecimalFormat gives a view coefficient (at most three
 // fraction digits, HALF_EVEN, no grouping), as OpenCLKernelBuilder.toLiteral.

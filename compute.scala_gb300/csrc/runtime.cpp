@@ -11,12 +11,14 @@
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <mutex>
+#include <sstream>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -72,8 +74,13 @@ void load_driver() {
   resolve(g_drv.CtxGetCurrent, "cuCtxGetCurrent");
   resolve(g_drv.CtxSetCurrent, "cuCtxSetCurrent");
   resolve(g_drv.FuncSetAttribute, "cuFuncSetAttribute");
+  resolve(g_drv.FuncGetAttribute, "cuFuncGetAttribute");
   resolve(g_drv.TensorMapEncodeTiled, "cuTensorMapEncodeTiled");
   resolve(g_drv.OccupancyMaxActiveBlocks, "cuOccupancyMaxActiveBlocksPerMultiprocessor");
+  resolve(g_drv.LinkCreate, "cuLinkCreate");
+  resolve(g_drv.LinkAddData, "cuLinkAddData");
+  resolve(g_drv.LinkComplete, "cuLinkComplete");
+  resolve(g_drv.LinkDestroy, "cuLinkDestroy");
   g_drv.loaded = true;
 }
 
@@ -170,15 +177,27 @@ struct Buffer {
   int refs = 1;
 };
 
-struct Program {
+// A compiled module.  Programs whose inputs are all read contiguously share one
+// module per structure whatever their shape (the length is a launch argument);
+// other programs have their own.
+struct Module {
   CUmodule module = nullptr;
   CUfunction scalar = nullptr;  // cc_ew / cc_sum
   CUfunction vec4 = nullptr;    // cc_ew_v4 / cc_sum_v4 (contiguous inputs)
   int block = 256;              // threads per block the kernels were generated for
   int resident_scalar = 0;      // blocks one SM holds at once, per variant
   int resident_vec4 = 0;
+  int vec_unroll = 1;
+  std::string source;
+  ~Module() {
+    if (module && g_drv.ModuleUnload) g_drv.ModuleUnload(module);
+  }
+};
+
+struct Program {
+  std::shared_ptr<Module> mod;
   ProgramKind kind = ProgramKind::Elementwise;
-  Generated gen;
+  Generated gen;                // shape information (its source lives in the module)
   bool is_contraction = false;  // run as a GEMM (cc_gemm_f32 mode contraction_mode)
   int contraction_mode = 0;
   Contraction con;
@@ -188,7 +207,26 @@ struct Event {
   cudaEvent_t ev = nullptr;
 };
 
-enum : uint64_t { kTagBuffer = 1, kTagProgram = 2, kTagEvent = 3 };
+// Many independent programs evaluated together (cc_batch_*).
+struct Batch {
+  CUmodule module = nullptr;
+  CUfunction persistent = nullptr;
+  std::vector<CUfunction> per_structure;  // one float4 kernel per distinct program
+  std::vector<int> sid;                   // structure of each program
+  std::vector<int> n_inputs;              // inputs of each program
+  std::vector<int64_t> length;            // points of each program
+  int resident = 0;                       // persistent blocks one SM holds
+  // bound buffers
+  bool bound = false;
+  std::vector<std::vector<uint64_t>> ptrs;  // per program: inputs..., output
+  void *table = nullptr;
+  size_t table_cls = 0;
+  int64_t total_tiles = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+};
+
+enum : uint64_t { kTagBuffer = 1, kTagProgram = 2, kTagEvent = 3, kTagBatch = 4 };
 
 struct Context {
   int device = 0;
@@ -206,7 +244,9 @@ struct Context {
   std::unordered_map<uint64_t, Buffer *> buffers;
   std::unordered_map<uint64_t, Program *> programs;   // by handle
   std::unordered_map<std::string, uint64_t> cache;    // IR text -> program handle
+  std::unordered_map<std::string, std::shared_ptr<Module>> modules;  // structure key -> module
   std::unordered_map<uint64_t, Event *> events;
+  std::unordered_map<uint64_t, Batch *> batches;
   uint64_t cache_hits = 0, cache_misses = 0;
   std::mutex compile_mu;
 
@@ -222,6 +262,8 @@ struct Context {
   int sum_block = 256;
   int tc_variant = 0;
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
+  int batch_inline = 0;
+  int batch_max_registers = 0;
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
 
@@ -278,13 +320,16 @@ Event &event_of(Context &c, cc_handle h) {
 
 // ---------------------------------------------------------------- NVRTC
 
-std::vector<char> compile_cubin(const std::string &source, int cc_major, int cc_minor, uint32_t flags) {
+std::vector<char> compile_cubin(const std::string &source, int cc_major, int cc_minor, uint32_t flags,
+                                bool relocatable = false, int max_registers = 0) {
   nvrtcProgram prog;
   nvrtcResult r = nvrtcCreateProgram(&prog, source.c_str(), "cc_program.cu", 0, nullptr, nullptr);
   if (r != NVRTC_SUCCESS) fail(CC_ERR_BUILD_PROGRAM_FAILURE, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
   std::string arch = "-arch=sm_" + std::to_string(cc_major) + std::to_string(cc_minor) + "a";
   std::vector<std::string> opts = {arch, "--std=c++17", "-default-device",
                                    (flags & CC_FLAG_FMA_CONTRACT) ? "--fmad=true" : "--fmad=false"};
+  if (relocatable) opts.push_back("-rdc=true");
+  if (max_registers > 0) opts.push_back("--maxrregcount=" + std::to_string(max_registers));
   std::vector<const char *> optp;
   for (auto &o : opts) optp.push_back(o.c_str());
   r = nvrtcCompileProgram(prog, (int)optp.size(), optp.data());
@@ -381,14 +426,15 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
              reinterpret_cast<float *>(out), (int)q.m, (int)q.n, (int)q.k, q.k, q.n, q.n, p.contraction_mode, stream);
     return;
   }
-  const int block = p.block;
+  const Module &m = *p.mod;
+  const int block = m.block;
   const int64_t n = p.gen.domain;
   bool aligned = (out & 15u) == 0;
   for (uint64_t a : in) aligned = aligned && (a & 15u) == 0;
-  const bool vec = p.vec4 && aligned;
-  CUfunction f = vec ? p.vec4 : p.scalar;
+  const bool vec = m.vec4 && aligned;
+  CUfunction f = vec ? m.vec4 : m.scalar;
   // float4 kernels: each thread takes vec_unroll positions per batch
-  const int64_t work = vec ? ((n >> 2) + p.gen.vec_unroll - 1) / p.gen.vec_unroll : n;
+  const int64_t work = vec ? ((n >> 2) + m.vec_unroll - 1) / m.vec_unroll : n;
   std::vector<void *> args;
   std::vector<uint64_t> ptrs(in);
   for (auto &v : ptrs) args.push_back(&v);
@@ -404,7 +450,7 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
     grid = (unsigned)sum_grid_for(work, block, c.sm_count * c.sum_blocks_per_sm);
   } else {
     if (n == 0) return;
-    int resident = vec ? p.resident_vec4 : p.resident_scalar;
+    int resident = vec ? m.resident_vec4 : m.resident_scalar;
     if (c.ew_blocks_per_sm > 0 && (resident <= 0 || c.ew_blocks_per_sm < resident)) resident = c.ew_blocks_per_sm;
     grid = (unsigned)ew_grid(work, block, c.sm_count, resident);
   }
@@ -518,10 +564,8 @@ int cc_shutdown(void) {
   cudaSetDevice(c->device);
   g_drv.CtxSetCurrent(c->cuctx);
   cudaStreamSynchronize(c->stream);
-  for (auto &kv : c->programs) {
-    g_drv.ModuleUnload(kv.second->module);
-    delete kv.second;
-  }
+  for (auto &kv : c->programs) delete kv.second;
+  c->modules.clear();
   for (auto &kv : c->buffers) {
     cudaFree(kv.second->ptr);
     delete kv.second;
@@ -595,6 +639,12 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "sum_block") {
     if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
     c.sum_block = (int)value;
+  } else if (k == "batch_max_registers") {
+    if (value < 0 || value > 255) fail(CC_ERR_INVALID_VALUE, "batch_max_registers must be in [0, 255]");
+    c.batch_max_registers = (int)value;
+  } else if (k == "batch_inline") {
+    if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "batch_inline must be 0, 1 or 2");
+    c.batch_inline = (int)value;
   } else if (k == "contraction") {
     if (value < 0 || value > 3) fail(CC_ERR_INVALID_VALUE, "contraction must be in [0, 3]");
     c.contraction = (int)value;
@@ -630,6 +680,8 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "sum_block") *value = c.sum_block;
   else if (k == "tc_variant") *value = c.tc_variant;
   else if (k == "contraction") *value = c.contraction;
+  else if (k == "batch_inline") *value = c.batch_inline;
+  else if (k == "batch_max_registers") *value = c.batch_max_registers;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END
 }
@@ -839,24 +891,49 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     *out = h;
     return CC_OK;
   }
-  {
-    int64_t domain = 1;
-    for (int64_t d : ir.out_shape) domain *= d;
+  int64_t domain = 1;
+  for (int64_t d : ir.out_shape) domain *= d;
+  // Contiguous programs compile once per structure; the shape only sizes the launch.
+  std::string skey = contiguous_structure_key(ir);
+  if (!skey.empty()) {
+    skey += key.substr(key.rfind('#'));
+    opt.min_blocks = 0;
+  } else {
     opt.min_blocks = choose_min_blocks(domain, opt.block, c.sm_count, -opt.min_blocks);
   }
   auto p = std::make_unique<Program>();
-  p->gen = generate_cuda(ir, opt);
   p->kind = ir.kind;
-  std::vector<char> cubin = compile_cubin(p->gen.source, c.cc_major, c.cc_minor, c.flags);
-  check_cu(g_drv.ModuleLoadData(&p->module, cubin.data()), "cuModuleLoadData");
-  const char *sname = ir.kind == ProgramKind::Sum ? "cc_sum" : "cc_ew";
-  const char *vname = ir.kind == ProgramKind::Sum ? "cc_sum_v4" : "cc_ew_v4";
-  check_cu(g_drv.ModuleGetFunction(&p->scalar, p->module, sname), "cuModuleGetFunction");
-  if (p->gen.has_vec4) check_cu(g_drv.ModuleGetFunction(&p->vec4, p->module, vname), "cuModuleGetFunction");
-  p->block = opt.block;
-  check_cu(g_drv.OccupancyMaxActiveBlocks(&p->resident_scalar, p->scalar, p->block, 0), "cuOccupancyMaxActiveBlocks");
-  if (p->vec4)
-    check_cu(g_drv.OccupancyMaxActiveBlocks(&p->resident_vec4, p->vec4, p->block, 0), "cuOccupancyMaxActiveBlocks");
+  std::shared_ptr<Module> mod;
+  if (!skey.empty()) {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    auto it = c.modules.find(skey);
+    if (it != c.modules.end()) mod = it->second;
+  }
+  if (mod) {
+    p->gen = describe_program(ir);
+  } else {
+    p->gen = generate_cuda(ir, opt);
+    mod = std::make_shared<Module>();
+    mod->source = p->gen.source;
+    std::vector<char> cubin = compile_cubin(mod->source, c.cc_major, c.cc_minor, c.flags);
+    check_cu(g_drv.ModuleLoadData(&mod->module, cubin.data()), "cuModuleLoadData");
+    const char *sname = ir.kind == ProgramKind::Sum ? "cc_sum" : "cc_ew";
+    const char *vname = ir.kind == ProgramKind::Sum ? "cc_sum_v4" : "cc_ew_v4";
+    check_cu(g_drv.ModuleGetFunction(&mod->scalar, mod->module, sname), "cuModuleGetFunction");
+    if (p->gen.has_vec4) check_cu(g_drv.ModuleGetFunction(&mod->vec4, mod->module, vname), "cuModuleGetFunction");
+    mod->block = opt.block;
+    mod->vec_unroll = p->gen.vec_unroll;
+    check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_scalar, mod->scalar, mod->block, 0),
+             "cuOccupancyMaxActiveBlocks");
+    if (mod->vec4)
+      check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_vec4, mod->vec4, mod->block, 0),
+               "cuOccupancyMaxActiveBlocks");
+    if (!skey.empty()) {
+      std::lock_guard<std::recursive_mutex> g(c.mu);
+      c.modules[skey] = mod;
+    }
+  }
+  p->mod = mod;
   std::lock_guard<std::recursive_mutex> g(c.mu);
   uint64_t h = c.make_handle(kTagProgram);
   c.programs[h] = p.release();
@@ -911,7 +988,7 @@ int cc_program_source(cc_handle h, char *buf, size_t len, size_t *needed) {
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
   Program &p = program_of(c, h);
-  const std::string &s = p.gen.source;
+  const std::string &s = p.mod ? p.mod->source : p.gen.source;
   if (needed) *needed = s.size() + 1;
   if (buf && len) {
     size_t n = s.size() < len - 1 ? s.size() : len - 1;
@@ -1104,6 +1181,418 @@ int cc_event_release(cc_handle h) {
   cudaEventDestroy(e.ev);
   delete &e;
   c.events.erase(h);
+  CC_API_END
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- batches
+//
+// A batch evaluates many independent elementwise programs of uneven lengths.
+// The reference launches one kernel per tensor (Tensors.scala:1331-1381) and
+// leans on five queues per device for concurrency; here one persistent kernel
+// walks all programs' tiles, with the per-program launches (and a CUDA graph
+// of them) kept as the comparison and for callers that want them.
+
+namespace cc {
+extern const char *kPrelude;
+namespace {
+
+constexpr int kBatchBlock = 256;
+constexpr int kBatchUnroll = 4;
+constexpr int64_t kBatchTile = (int64_t)kBatchBlock * 4 * kBatchUnroll;  // floats per tile (4096)
+
+// The device table entry; must match the struct in the generated module.
+struct BatchEntry {
+  uint64_t in[kBatchMaxInputs];
+  uint64_t out;
+  int64_t n;
+  int64_t tile_begin;
+  int32_t sid;
+  int32_t pad;
+};
+static_assert(sizeof(BatchEntry) == 64, "batch entry layout");
+
+// A batch module is linked from separately compiled parts, because compile
+// time grows faster than linearly with the size of one NVRTC program:
+//   - chunk units: for kBatchChunk structures each, the structure's expression
+//     (a real function), a tile function walking one tile of that structure
+//     one float4 per thread at a time, and the structure's own kernel;
+//   - the main unit: a device table of the tile functions and the persistent
+//     kernel, which finds a tile's program by binary search and calls its tile
+//     function through the table.
+// The parts compile in parallel (relocatable code) and the driver links them.
+constexpr int kBatchChunk = 32;
+
+const char *kTileParams =
+    "(const float *__restrict__ in0, const float *__restrict__ in1, const float *__restrict__ in2, "
+    "const float *__restrict__ in3, float *__restrict__ out, long long n, long long base)";
+
+// inline_level: 0 = the expression is a called function and so are exp/log/tanh;
+// 1 = the expression is inlined into its tile function, exp/log/tanh called;
+// 2 = everything inlined.  Higher levels run faster and compile slower.
+std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs, size_t first,
+                               size_t last, int inline_level) {
+  std::ostringstream o;
+  o << "// generated batch part for sm_103a\n"
+    << "static __device__ __noinline__ float cc_expf(float x) { return expf(x); }\n"
+       "static __device__ __noinline__ float cc_logf(float x) { return logf(x); }\n"
+       "static __device__ __noinline__ float cc_tanhf(float x) { return tanhf(x); }\n";
+  const std::string B = std::to_string(kBatchBlock);
+  for (size_t s = first; s < last; ++s) {
+    const int nin = struct_inputs[s];
+    const std::string S = std::to_string(s);
+    std::string pf = point_function(structs[s], "cc_point_" + S, inline_level >= 1, inline_level <= 1);
+    o << "static " << pf;
+    auto call = [&](const std::string &suffix) {
+      std::string c = "cc_point_" + S + "(";
+      for (int i = 0; i < kBatchMaxInputs; ++i)
+        c += (i ? ", " : "") + (i < nin ? "v" + std::to_string(i) + suffix : std::string("0.0f"));
+      return c + ")";
+    };
+    // A full tile loads all its float4s before computing any, so every thread
+    // has kBatchUnroll loads per input in flight; the ragged last tile of a
+    // program takes the plain loops.
+    o << "extern \"C\" __device__ __noinline__ void cc_tile_" << S << kTileParams << " {\n"
+      << "  if (base + " << kBatchTile << "LL <= n) {\n"
+      << "    const long long q0 = (base >> 2) + threadIdx.x;\n";
+    for (int i = 0; i < nin; ++i)
+      for (int u = 0; u < kBatchUnroll; ++u)
+        o << "    const float4 v" << i << "_" << u << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q0 + "
+          << u * kBatchBlock << ");\n";
+    for (int u = 0; u < kBatchUnroll; ++u) {
+      const std::string U = "_" + std::to_string(u);
+      o << "    float4 r" << U << ";\n";
+      for (const char *lane : {".x", ".y", ".z", ".w"})
+        o << "    r" << U << lane << " = " << call(U + lane) << ";\n";
+    }
+    for (int u = 0; u < kBatchUnroll; ++u)
+      o << "    reinterpret_cast<float4 *>(out)[q0 + " << u * kBatchBlock << "] = r_" << u << ";\n";
+    o << "    return;\n  }\n"
+      << "  const long long end = base + " << kBatchTile << "LL < n ? base + " << kBatchTile << "LL : n;\n"
+      << "  const long long end4 = end & ~3LL;\n"
+      << "  for (long long q = (base >> 2) + threadIdx.x; (q << 2) < end4; q += " << B << ") {\n";
+    for (int i = 0; i < nin; ++i)
+      o << "    const float4 v" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
+    o << "    float4 r;\n";
+    for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    r" << lane << " = " << call(lane) << ";\n";
+    o << "    reinterpret_cast<float4 *>(out)[q] = r;\n  }\n"
+      << "  for (long long i = end4 + threadIdx.x; i < end; i += " << B << ") {\n";
+    for (int i = 0; i < nin; ++i) o << "    const float v" << i << " = __ldg(in" << i << " + i);\n";
+    o << "    out[i] = " << call("") << ";\n  }\n}\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(" << B << ") cc_prog_" << S
+      << "(const float *__restrict__ in0, const float *__restrict__ in1, const float *__restrict__ in2, "
+         "const float *__restrict__ in3, float *__restrict__ out, long long n) {\n"
+      << "  const long long tiles = (n + " << kBatchTile - 1 << "LL) / " << kBatchTile << "LL;\n"
+      << "  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) cc_tile_" << S
+      << "(in0, in1, in2, in3, out, n, t * " << kBatchTile << "LL);\n}\n";
+  }
+  return o.str();
+}
+
+std::string batch_main_source(size_t n_structs) {
+  std::ostringstream o;
+  o << "// generated batch main part for sm_103a\n"
+    << "struct cc_entry { const float *in[4]; float *out; long long n; long long tile_begin; int sid; int pad; };\n"
+    << "typedef void (*cc_tile_fn)" << kTileParams << ";\n";
+  for (size_t s = 0; s < n_structs; ++s) o << "extern \"C\" __device__ void cc_tile_" << s << kTileParams << ";\n";
+  o << "__device__ cc_tile_fn const cc_tiles[" << n_structs << "] = {\n";
+  for (size_t s = 0; s < n_structs; ++s) o << "  cc_tile_" << s << ",\n";
+  o << "};\n"
+    << "extern \"C\" __global__ void __launch_bounds__(" << kBatchBlock
+    << ") cc_batch(const cc_entry *__restrict__ table, int nprog, long long total_tiles) {\n"
+    << "  extern __shared__ long long s_begin[];\n"
+    << "  for (int i = threadIdx.x; i < nprog; i += blockDim.x) s_begin[i] = table[i].tile_begin;\n"
+    << "  __syncthreads();\n"
+    << "  for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {\n"
+    << "    int lo = 0, hi = nprog - 1;\n"
+    << "    while (lo < hi) {\n      const int mid = (lo + hi + 1) >> 1;\n"
+    << "      if (s_begin[mid] <= t) lo = mid; else hi = mid - 1;\n    }\n"
+    << "    const cc_entry e = table[lo];\n"
+    << "    const long long base = (t - e.tile_begin) * " << kBatchTile << "LL;\n"
+    << "    if (e.sid >= 0 && e.sid < " << n_structs << ") cc_tiles[e.sid](e.in[0], e.in[1], e.in[2], e.in[3], e.out, e.n, base);\n"
+    << "  }\n}\n";
+  return o.str();
+}
+
+// Compiles the parts in parallel and links them into one loadable image.
+std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs,
+                                    int cc_major, int cc_minor, uint32_t flags, bool link, int inline_level,
+                                    int max_registers) {
+  std::vector<std::string> sources;
+  for (size_t first = 0; first < structs.size(); first += kBatchChunk)
+    sources.push_back(batch_chunk_source(structs, struct_inputs, first,
+                                         std::min(structs.size(), first + (size_t)kBatchChunk), inline_level));
+  sources.push_back(batch_main_source(structs.size()));
+  std::vector<std::vector<char>> parts(sources.size());
+  std::vector<std::string> errors(sources.size());
+  std::atomic<size_t> next{0};
+  unsigned nthreads = std::thread::hardware_concurrency();
+  if (nthreads == 0) nthreads = 4;
+  if (nthreads > sources.size()) nthreads = (unsigned)sources.size();
+  std::vector<std::thread> pool;
+  for (unsigned t = 0; t < nthreads; ++t) {
+    pool.emplace_back([&]() {
+      for (size_t i; (i = next.fetch_add(1)) < sources.size();) {
+        try {
+          parts[i] = compile_cubin(sources[i], cc_major, cc_minor, flags, true, max_registers);
+        } catch (const Error &e) {
+          errors[i] = e.message;
+        }
+      }
+    });
+  }
+  for (auto &th : pool) th.join();
+  for (auto &e : errors)
+    if (!e.empty()) fail(CC_ERR_BUILD_PROGRAM_FAILURE, e);
+  if (!link) return {};
+  CUlinkState state;
+  check_cu(g_drv.LinkCreate(0, nullptr, nullptr, &state), "cuLinkCreate");
+  try {
+    for (size_t i = 0; i < parts.size(); ++i) {
+      std::string name = "batch_part_" + std::to_string(i);
+      check_cu(g_drv.LinkAddData(state, CU_JIT_INPUT_CUBIN, parts[i].data(), parts[i].size(), name.c_str(), 0,
+                                 nullptr, nullptr),
+               "cuLinkAddData");
+    }
+    void *image = nullptr;
+    size_t size = 0;
+    check_cu(g_drv.LinkComplete(state, &image, &size), "cuLinkComplete");
+    std::vector<char> out(static_cast<char *>(image), static_cast<char *>(image) + size);
+    g_drv.LinkDestroy(state);
+    return out;
+  } catch (...) {
+    g_drv.LinkDestroy(state);
+    throw;
+  }
+}
+
+Batch &batch_of(Context &c, cc_handle h) {
+  auto it = c.batches.find(h);
+  if (tag_of(h) != kTagBatch || it == c.batches.end()) fail(CC_ERR_INVALID_VALUE, "not a live batch handle");
+  return *it->second;
+}
+
+void batch_drop_graph(Batch &b) {
+  if (b.graph_exec) cudaGraphExecDestroy(b.graph_exec);
+  if (b.graph) cudaGraphDestroy(b.graph);
+  b.graph_exec = nullptr;
+  b.graph = nullptr;
+}
+
+void batch_launch_each(Context &c, Batch &b, cudaStream_t s) {
+  for (size_t p = 0; p < b.sid.size(); ++p) {
+    if (b.length[p] == 0) continue;
+    uint64_t in[kBatchMaxInputs] = {0, 0, 0, 0};
+    for (int i = 0; i < b.n_inputs[p]; ++i) in[i] = b.ptrs[p][i];
+    uint64_t out = b.ptrs[p][b.n_inputs[p]];
+    long long n = b.length[p];
+    void *args[] = {&in[0], &in[1], &in[2], &in[3], &out, &n};
+    int64_t tiles = (n + kBatchTile - 1) / kBatchTile;
+    int64_t cap = (int64_t)c.sm_count * 8;
+    unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
+    check_cu(g_drv.LaunchKernel(b.per_structure[b.sid[p]], grid, 1, 1, kBatchBlock, 1, 1, 0, (CUstream)s, args, nullptr),
+             "cuLaunchKernel");
+  }
+}
+
+}  // namespace
+}  // namespace cc
+
+extern "C" {
+
+int cc_batch_create(const char *const *irs, const size_t *lens, int n_programs, cc_handle *out) {
+  CC_API_BEGIN
+  if (!irs || !lens || !out || n_programs <= 0) fail(CC_ERR_INVALID_VALUE, "empty batch");
+  Context &c = ctx();
+  auto b = std::make_unique<Batch>();
+  std::unordered_map<std::string, int> seen;
+  std::vector<Ir> structs;
+  std::vector<int> struct_inputs;
+  for (int p = 0; p < n_programs; ++p) {
+    if (!irs[p]) fail(CC_ERR_INVALID_VALUE, "null program text");
+    std::string text(irs[p], lens[p]);
+    Ir ir = parse_ir(text.data(), text.size());
+    std::string why;
+    if (!is_batchable(ir, &why)) fail(CC_ERR_INVALID_PROGRAM, "program " + std::to_string(p) + ": " + why);
+    int64_t n = 1;
+    for (int64_t d : ir.out_shape) n *= d;
+    // programs differing only in length share code
+    std::string key = contiguous_structure_key(ir);
+    if (key.empty()) key = text;
+    auto it = seen.find(key);
+    int sid;
+    if (it == seen.end()) {
+      sid = (int)structs.size();
+      seen.emplace(key, sid);
+      struct_inputs.push_back(ir.n_params);
+      structs.push_back(std::move(ir));
+    } else {
+      sid = it->second;
+    }
+    b->sid.push_back(sid);
+    b->n_inputs.push_back(struct_inputs[sid]);
+    b->length.push_back(n);
+  }
+  std::vector<char> cubin;
+  {
+    std::lock_guard<std::mutex> cg(c.compile_mu);
+    cubin = build_batch_image(structs, struct_inputs, c.cc_major, c.cc_minor, c.flags, true, c.batch_inline,
+                              c.batch_max_registers);
+  }
+  check_cu(g_drv.ModuleLoadData(&b->module, cubin.data()), "cuModuleLoadData");
+  check_cu(g_drv.ModuleGetFunction(&b->persistent, b->module, "cc_batch"), "cuModuleGetFunction");
+  for (size_t s = 0; s < structs.size(); ++s) {
+    CUfunction f;
+    check_cu(g_drv.ModuleGetFunction(&f, b->module, ("cc_prog_" + std::to_string(s)).c_str()), "cuModuleGetFunction");
+    b->per_structure.push_back(f);
+  }
+  const size_t smem = sizeof(int64_t) * (size_t)n_programs;
+  if (smem > 48 * 1024)
+    check_cu(g_drv.FuncSetAttribute(b->persistent, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem),
+             "cuFuncSetAttribute");
+  check_cu(g_drv.OccupancyMaxActiveBlocks(&b->resident, b->persistent, kBatchBlock, smem), "occupancy");
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  uint64_t h = c.make_handle(kTagBatch);
+  c.batches[h] = b.release();
+  *out = h;
+  CC_API_END
+}
+
+int cc_batch_compile_check(const char *const *irs, const size_t *lens, int n_programs, int cc_major, int cc_minor,
+                           int *n_structures, double *seconds) {
+  CC_API_BEGIN
+  if (!irs || !lens || n_programs <= 0) fail(CC_ERR_INVALID_VALUE, "empty batch");
+  std::unordered_map<std::string, int> seen;
+  std::vector<Ir> structs;
+  std::vector<int> struct_inputs;
+  for (int p = 0; p < n_programs; ++p) {
+    Ir ir = parse_ir(irs[p], lens[p]);
+    std::string why;
+    if (!is_batchable(ir, &why)) fail(CC_ERR_INVALID_PROGRAM, "program " + std::to_string(p) + ": " + why);
+    std::string key = contiguous_structure_key(ir);
+    if (key.empty()) key = std::string(irs[p], lens[p]);
+    if (seen.emplace(key, (int)structs.size()).second) {
+      struct_inputs.push_back(ir.n_params);
+      structs.push_back(std::move(ir));
+    }
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  build_batch_image(structs, struct_inputs, cc_major, cc_minor, 0, false, 0, 0);  // linking needs a driver
+  if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (n_structures) *n_structures = (int)structs.size();
+  CC_API_END
+}
+
+int cc_batch_info(cc_handle batch, int *n_programs, int *n_structures, int *registers, int *resident_blocks) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Batch &b = batch_of(c, batch);
+  if (n_programs) *n_programs = (int)b.sid.size();
+  if (n_structures) *n_structures = (int)b.per_structure.size();
+  if (registers) check_cu(g_drv.FuncGetAttribute(registers, CU_FUNC_ATTRIBUTE_NUM_REGS, b.persistent), "cuFuncGetAttribute");
+  if (resident_blocks) *resident_blocks = b.resident;
+  CC_API_END
+}
+
+int cc_batch_bind(cc_handle batch, const uint64_t *ptrs, size_t n_ptrs) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Batch &b = batch_of(c, batch);
+  size_t need = 0;
+  for (size_t p = 0; p < b.sid.size(); ++p) need += b.n_inputs[p] + 1;
+  if (!ptrs || n_ptrs != need)
+    fail(CC_ERR_INVALID_KERNEL_ARGS, "the batch needs " + std::to_string(need) + " pointers (inputs, then the output, per program)");
+  std::vector<BatchEntry> table(b.sid.size());
+  std::vector<std::vector<uint64_t>> bound(b.sid.size());
+  size_t k = 0;
+  int64_t tiles = 0;
+  for (size_t p = 0; p < b.sid.size(); ++p) {
+    BatchEntry &e = table[p];
+    memset(&e, 0, sizeof e);
+    for (int i = 0; i <= b.n_inputs[p]; ++i) {
+      uint64_t q = ptrs[k++];
+      if (!q || (q & 15u)) fail(CC_ERR_INVALID_VALUE, "batch buffers must be non-null and 16-byte aligned");
+      bound[p].push_back(q);
+      if (i < b.n_inputs[p]) e.in[i] = q; else e.out = q;
+    }
+    e.n = b.length[p];
+    e.tile_begin = tiles;
+    e.sid = b.sid[p];
+    tiles += (b.length[p] + kBatchTile - 1) / kBatchTile;
+  }
+  if (!b.table) b.table = c.pool.alloc(sizeof(BatchEntry) * table.size(), &b.table_cls);
+  check_cuda(cudaMemcpyAsync(b.table, table.data(), sizeof(BatchEntry) * table.size(), cudaMemcpyHostToDevice, c.stream),
+             "upload batch table");
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  b.ptrs = std::move(bound);
+  b.total_tiles = tiles;
+  b.bound = true;
+  batch_drop_graph(b);
+  CC_API_END
+}
+
+int cc_batch_run(cc_handle batch, int mode, uint64_t stream) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Batch &b = batch_of(c, batch);
+  if (!b.bound) fail(CC_ERR_INVALID_OPERATION, "bind the batch's buffers first");
+  cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  if (mode == CC_BATCH_PERSISTENT) {
+    if (b.total_tiles == 0) return CC_OK;
+    uint64_t table = reinterpret_cast<uint64_t>(b.table);
+    int nprog = (int)b.sid.size();
+    long long total = b.total_tiles;
+    void *args[] = {&table, &nprog, &total};
+    int64_t cap = (int64_t)c.sm_count * (b.resident > 0 ? b.resident : 4);
+    unsigned grid = (unsigned)(b.total_tiles < cap ? b.total_tiles : cap);
+    check_cu(g_drv.LaunchKernel(b.persistent, grid, 1, 1, kBatchBlock, 1, 1, (unsigned)(sizeof(int64_t) * nprog),
+                                (CUstream)s, args, nullptr),
+             "cuLaunchKernel");
+  } else if (mode == CC_BATCH_PER_PROGRAM) {
+    batch_launch_each(c, b, s);
+  } else if (mode == CC_BATCH_GRAPH) {
+    if (!b.graph_exec) {
+      cudaStream_t cap_stream;
+      check_cuda(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      cudaError_t e = cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        try {
+          batch_launch_each(c, b, cap_stream);
+        } catch (...) {
+          cudaGraph_t broken = nullptr;
+          cudaStreamEndCapture(cap_stream, &broken);
+          if (broken) cudaGraphDestroy(broken);
+          cudaStreamDestroy(cap_stream);
+          throw;
+        }
+        e = cudaStreamEndCapture(cap_stream, &b.graph);
+      }
+      cudaStreamDestroy(cap_stream);
+      check_cuda(e, "graph capture");
+      check_cuda(cudaGraphInstantiate(&b.graph_exec, b.graph, 0), "cudaGraphInstantiate");
+    }
+    check_cuda(cudaGraphLaunch(b.graph_exec, s), "cudaGraphLaunch");
+  } else {
+    fail(CC_ERR_INVALID_VALUE, "unknown batch mode");
+  }
+  CC_API_END
+}
+
+int cc_batch_release(cc_handle batch) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Batch &b = batch_of(c, batch);
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  batch_drop_graph(b);
+  if (b.table) c.pool.release(b.table, b.table_cls);
+  g_drv.ModuleUnload(b.module);
+  delete &b;
+  c.batches.erase(batch);
   CC_API_END
 }
 

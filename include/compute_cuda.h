@@ -83,6 +83,9 @@ int cc_synchronize(void);
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
  *                       3 = CC_GEMM_BF16X6
+ *   "batch_max_registers" batch modules: register cap per thread of every compiled part (0 = none)
+ *   "batch_inline"      batch modules: 0 = expressions and exp/log/tanh are called functions
+ *                       (default), 1 = expressions inlined, exp/log/tanh called, 2 = all inlined
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
  *                       registers (FP32-level error at any K; default), 1 = 128x256 tiles, one
  *                       accumulator per tile (fastest, error grows with K), 2 = 128x128, one per tile
@@ -186,6 +189,26 @@ int cc_gemm_f32(uint64_t a_ptr, uint64_t b_ptr, uint64_t c_ptr, int m, int n, in
 /* Reads and clears the device error flag that kernels with bounded waits set
  * when a wait expires (0 = none); blocking. */
 int cc_device_errors(int *code);
+
+/* ---- batches: many independent elementwise programs of uneven lengths evaluated
+ *      together (no reference counterpart: the reference launches one kernel per
+ *      tensor, Tensors.scala:1331-1381).  A batch compiles once; each distinct
+ *      program structure gets a point function shared by all three run modes, so
+ *      every mode gives the same bits.  Programs must be contiguous elementwise
+ *      programs (inputs read without views) with at most 4 inputs. ------------- */
+#define CC_BATCH_PERSISTENT 0   /* one persistent kernel over every program's 4096-float tiles */
+#define CC_BATCH_PER_PROGRAM 1  /* one launch per program, back to back */
+#define CC_BATCH_GRAPH 2        /* the per-program launches, captured once into a CUDA graph and replayed */
+int cc_batch_create(const char *const *irs, const size_t *ir_lens, int n_programs, cc_handle *batch);
+/* registers: per thread of the persistent kernel; resident_blocks: its blocks per SM.  Any pointer may be NULL. */
+int cc_batch_info(cc_handle batch, int *n_programs, int *n_structures, int *registers, int *resident_blocks);
+/* ptrs: for each program, its inputs in parameter order, then its output (16-byte aligned). */
+int cc_batch_bind(cc_handle batch, const uint64_t *ptrs, size_t n_ptrs);
+int cc_batch_run(cc_handle batch, int mode, uint64_t stream);
+int cc_batch_release(cc_handle batch);
+/* GPU-free: generates and NVRTC-compiles a batch module for sm_<cc_major><cc_minor>a. */
+int cc_batch_compile_check(const char *const *irs, const size_t *ir_lens, int n_programs, int cc_major, int cc_minor,
+                           int *n_structures, double *seconds);
 
 /* ---- random numbers: Tensor.random / Tensor.randomNormal with the Wang hash
  *      (Tensors.scala:106-117, :397-524).  normal=0: uniform [0,1]; normal=1:

@@ -120,3 +120,20 @@ def test_the_matmul_idiom_is_recognised_as_a_contraction():
 def test_a_long_fold_serialises():
     text = _matmul_ir(8, 2048, 8)
     assert text.count("\nv ") == 2048
+
+
+def test_batch_module_compiles_for_sm103a():
+    """A batch of contiguous programs of several structures and lengths builds (parts compile; no GPU to link)."""
+    from compute import Tensors
+    from compute.runtime import batch_compile_check
+    from compute.tensors import NonInlineTensor
+    d = Tensors(runtime=object())
+    T = d.Tensor
+    texts = []
+    for k, n in enumerate([5, 4096, 70001, 3, 4096]):
+        a = NonInlineTensor(d, (n,), 0.0, None)
+        b = NonInlineTensor(d, (n,), 0.0, None)
+        e = [T.tanh(a * b + a), T.exp(a) / b, T.max(a, b) - T.log(b), T.tanh(a * b + a), a * b][k]
+        texts.append(d.serialize(e.closure, e.shape).text)
+    structures, seconds = batch_compile_check(texts)
+    assert structures == 4  # programs 0 and 3 share code although their lengths differ
