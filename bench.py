@@ -360,7 +360,10 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s", "c4", "c5"])
+    ap.add_argument("--programs", type=int, default=2048, help="c5: tuning workloads to time (the last 10%% held out)")
+    ap.add_argument("--db", default=None, help="c5: append the timing records (JSON lines) to this file")
+    ap.add_argument("--collect-budget-s", type=float, default=None, help="c5: stop collecting after this long")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true", help="skip the clock sampling (and its untimed busy loop)")
@@ -375,6 +378,8 @@ def main():
         return main_contraction(args, warmup, rank, world, local_rank)
     if args.workload == "c4":
         return main_batch(args, warmup, rank, world, local_rank)
+    if args.workload == "c5":
+        return main_tuner(args, warmup, rank, world, local_rank)
 
     if args.impl == "reference":
         if rank != 0:
@@ -447,6 +452,70 @@ def main():
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def main_tuner(args, warmup, rank, world, local_rank):
+    """C5: the exhaustive tuner times every configuration of seeded tuning
+    workloads; the cost model trains on the first 90% of programs (its own CUDA
+    kernels) and picks configurations for the held-out 10%.  The value is the
+    held-out geometric-mean slowdown of the learned pick against the exhaustive
+    best (0 = always the best); the default configuration's and the best single
+    fixed configuration's figures are reported beside it."""
+    if rank != 0:
+        return
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no tuner (the OpenCL runtime picks "
+                          "its local size)"}), flush=True)
+        return
+    from compute.runtime import NativeRuntime
+    from compute import tuner
+    rt = NativeRuntime(local_rank)
+    sm = rt.device_info()["sm_count"]
+    t0 = time.time()
+    progs = tuner.random_programs(args.programs, seed=0)
+    gen_s = time.time() - t0
+    log = open(args.db, "a") if args.db else None
+    t0 = time.time()
+    try:
+        recs = tuner.collect(rt, progs, reps=3, flush_l2=True, log=log, time_budget_s=args.collect_budget_s)
+    finally:
+        if log:
+            log.close()
+    collect_s = time.time() - t0
+    split = int(len(recs) * 0.9)
+    train, test = recs[:split], recs[split:]
+    x, y = tuner.training_arrays(train, sm)
+    model = tuner.CostModel(rt, seed=0)
+    t0 = time.time()
+    losses = model.fit(x, y, epochs=40, batch=4096, lr=2e-3, lr_final=1e-4)
+    rt.synchronize()
+    train_s = time.time() - t0
+    steps = 40 * max(1, x.shape[0] // 4096)
+    fixed = tuner.best_fixed_config(train)
+    res = tuner.evaluate(model, test, sm, fixed=fixed)
+    xt = tuner.feature_matrix([r["ir"] for r in test], sm)
+    t0 = time.time()
+    model.predict(xt)
+    predict_s = time.time() - t0
+    kinds = {}
+    for r in recs:
+        kinds[r["kind"]] = kinds.get(r["kind"], 0) + 1
+    line = {"metric": "learned-tuner regret (held-out geometric-mean slowdown vs exhaustive best)",
+            "value": res["learned"]["geomean_slowdown"], "unit": "fraction", "n_gpus": 1, "steps": steps,
+            "warmup": 0, "ms_per_step": train_s * 1e3 / steps, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tuning workloads)",
+            "config": {"workload": "tuning workloads: rank 1-4, dims 1-4096, <= 64M points, inputs through "
+                                   "random permute/broadcast/translate views, 3-12-node trees over "
+                                   "+,-,*,/,exp,log,tanh,max, optional full or inner-axis sum; 48 configs each",
+                       "programs_timed": len(recs), "train": len(train), "held_out": len(test), "kinds": kinds,
+                       "timing": "median of 3 launches per config, L2 flushed (256 MiB write) before each",
+                       "model": "MLP 64-256-256-256-1 ReLU, Adam, 40 epochs, batch 4096, own CUDA kernels"},
+            "tuner": res, "train_loss_first_last": [losses[0], losses[-1]],
+            "seconds": {"generate": round(gen_s, 1), "compile_and_time": round(collect_s, 1),
+                        "train": round(train_s, 2), "predict_held_out": round(predict_s, 3)},
+            "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": None}
+    print(json.dumps(line), flush=True)
+    model.close()
 
 
 def main_batch(args, warmup, rank, world, local_rank):

@@ -146,6 +146,32 @@ _SIGNATURES = {
                     ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64],
     "cc_device_errors": [ctypes.POINTER(ctypes.c_int)],
     "cc_batch_create": [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(c_size), ctypes.c_int, ctypes.POINTER(c_handle)],
+    "cc_tune_config": [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                       ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+    "cc_program_features": [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)],
+    "cc_tuner_choice": [c_handle, ctypes.POINTER(ctypes.c_int)],
+    "cc_tuner_set_model": [c_handle, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+    "cc_tune_create": [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_size_t), ctypes.c_int,
+                       ctypes.POINTER(c_handle)],
+    "cc_tune_info": [c_handle, ctypes.POINTER(ctypes.c_int)],
+    "cc_tune_launch": [c_handle, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64), ctypes.c_size_t, ctypes.c_int,
+                       ctypes.c_uint64],
+    "cc_tune_time": [c_handle, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64), ctypes.c_size_t,
+                     ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                     ctypes.POINTER(ctypes.c_float)],
+    "cc_tune_release": [c_handle],
+    "cc_tune_compile_check": [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_size_t), ctypes.c_int,
+                              ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
+    "cc_mlp_create": [ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(c_handle)],
+    "cc_mlp_info": [c_handle, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_int)],
+    "cc_mlp_set_params": [c_handle, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t],
+    "cc_mlp_get_params": [c_handle, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t],
+    "cc_mlp_forward": [c_handle, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64],
+    "cc_mlp_gradients": [c_handle, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                         ctypes.POINTER(ctypes.c_float)],
+    "cc_mlp_train_step": [c_handle, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, ctypes.c_float, ctypes.POINTER(ctypes.c_float)],
+    "cc_mlp_release": [c_handle],
     "cc_batch_info": [c_handle, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                       ctypes.POINTER(ctypes.c_int)],
     "cc_batch_bind": [c_handle, ctypes.POINTER(ctypes.c_uint64), c_size],

@@ -161,6 +161,12 @@ class NativeRuntime:
              int(k), ctypes.c_int64(k if lda is None else lda), ctypes.c_int64(n if ldb is None else ldb),
              ctypes.c_int64(n if ldc is None else ldc), int(mode), ctypes.c_uint64(stream))
 
+    def tuner_choice(self, prog: Program) -> int:
+        """The launch configuration the tuner chose for a program (-1: none yet)."""
+        v = ctypes.c_int()
+        call("cc_tuner_choice", c_handle(prog.handle), ctypes.byref(v))
+        return v.value
+
     def device_errors(self) -> int:
         v = ctypes.c_int()
         call("cc_device_errors", ctypes.byref(v))

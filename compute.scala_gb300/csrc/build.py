@@ -20,8 +20,8 @@ PKG = os.path.normpath(os.path.join(HERE, "..", "compute"))
 BUILD = os.path.normpath(os.path.join(HERE, "..", "_build"))
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-HOST_SOURCES = ["runtime.cpp", "codegen.cpp"]
-DEVICE_SOURCES = ["kernels.cu", "noalloc.cu", "gemm.cu", "gemm_tc.cu"]
+HOST_SOURCES = ["runtime.cpp", "codegen.cpp", "tuning.cpp"]
+DEVICE_SOURCES = ["kernels.cu", "noalloc.cu", "gemm.cu", "gemm_tc.cu", "mlp.cu"]
 LIB_NAME = "libcomputecuda.so"
 
 

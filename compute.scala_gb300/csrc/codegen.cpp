@@ -633,6 +633,31 @@ std::string contiguous_structure_key(const Ir &ir) {
   return o.str();
 }
 
+namespace {
+
+// Output coordinates g0..g<rank-1> of linear index `lin` (row-major).  Below
+// 2^31 points the arithmetic is 32-bit unsigned, whose division by a constant
+// compiles to a multiply and shifts; larger domains divide in 64 bits.
+std::string decode_coordinates(const std::vector<int64_t> &shape, int64_t domain, const std::string &pad) {
+  std::ostringstream os;
+  const int rank = (int)shape.size();
+  const bool narrow = domain < (int64_t(1) << 31);
+  os << pad << (narrow ? "unsigned int rem_ = (unsigned int)lin;\n" : "cc_i64 rem_ = lin;\n");
+  for (int d = rank - 1; d >= 1; --d) {
+    if (narrow) {
+      os << pad << "const int g" << d << " = (int)(rem_ % " << shape[d] << "u);\n";
+      os << pad << "rem_ /= " << shape[d] << "u;\n";
+    } else {
+      os << pad << "const int g" << d << " = (int)(rem_ % " << shape[d] << "LL);\n";
+      os << pad << "rem_ /= " << shape[d] << "LL;\n";
+    }
+  }
+  os << pad << "const int g0 = (int)rem_;\n";
+  return os.str();
+}
+
+}  // namespace
+
 Generated describe_program(const Ir &ir) {
   Generated g;
   g.n_inputs = ir.n_params;
@@ -678,12 +703,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   auto decode = [&](std::ostringstream &os, int ind) {
     std::string pad(ind, ' ');
     if (rank == 0) return;
-    os << pad << "cc_i64 rem_ = lin;\n";
-    for (int d = rank - 1; d >= 1; --d) {
-      os << pad << "const int g" << d << " = (int)(rem_ % " << ir.out_shape[d] << "LL);\n";
-      os << pad << "rem_ /= " << ir.out_shape[d] << "LL;\n";
-    }
-    os << pad << "const int g0 = (int)rem_;\n";
+    os << decode_coordinates(ir.out_shape, domain, pad);
   };
 
   const std::string block = std::to_string(opt.block);
@@ -839,6 +859,178 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   }
   g.source = src.str();
   return g;
+}
+
+}  // namespace cc
+
+// ---------------------------------------------------------------- tunable form
+
+namespace cc {
+
+bool is_tunable(const Ir &ir, std::string *why) {
+  auto no = [&](const char *w) {
+    if (why) *why = w;
+    return false;
+  };
+  if (ir.nodes[ir.root].kind == NodeKind::Tuple) return no("a tuned program has one value per point (no join)");
+  int64_t domain = 1;
+  for (int64_t d : ir.out_shape) domain *= d;
+  if (domain <= 0) return no("a tuned program has at least one point");
+  return true;
+}
+
+std::string tunable_source(const Ir &ir, const std::string &suffix) {
+  const bool contiguous = program_is_contiguous(ir);
+  const bool sum = ir.kind == ProgramKind::Sum;
+  const int nin = ir.n_params;
+  const int rank = (int)ir.out_shape.size();
+  std::ostringstream o;
+  const std::string P = (contiguous ? "cc_pt" : "cc_gp") + suffix;
+  Frame f0{0, {}, ir.out_shape};
+  if (contiguous) {
+    Generator gen(ir, true);
+    std::ostringstream body;
+    std::string r = gen.gen(ir.root, f0);
+    gen.emit(body, 2, 0);
+    o << "static __device__ __forceinline__ float " << P << "(";
+    for (int i = 0; i < nin; ++i) o << (i ? ", " : "") << "float a" << i;
+    if (nin == 0) o << "void";
+    o << ") {\n" << body.str() << "  return " << r << ";\n}\n";
+  } else {
+    // The generic point: output coordinates decoded from `lin`, then the
+    // program's loads and arithmetic.
+    for (int d = 0; d < rank; ++d) f0.gid.push_back("g" + std::to_string(d));
+    Generator gen(ir, false, true, -1);
+    std::ostringstream body;
+    int64_t domain = 1;
+    for (int64_t d : ir.out_shape) domain *= d;
+    if (rank > 0) body << decode_coordinates(ir.out_shape, domain, "  ");
+    std::string r = gen.gen(ir.root, f0);
+    gen.emit(body, 2, 8);
+    o << "static __device__ __forceinline__ float " << P << "(cc_i64 lin";
+    for (int i = 0; i < nin; ++i) o << ", const float *__restrict__ in" << i;
+    o << ") {\n" << body.str() << "  return " << r << ";\n}\n";
+  }
+  std::string params;
+  for (int i = 0; i < nin; ++i) params += "const float *__restrict__ in" + std::to_string(i) + ", ";
+  std::string ins;
+  for (int i = 0; i < nin; ++i) ins += ", in" + std::to_string(i);
+  // value at scalar position `pos` (an expression of type cc_i64)
+  auto scalar_value = [&](const std::string &pos, std::ostringstream &os, const std::string &var,
+                          const std::string &pad) {
+    if (contiguous) {
+      for (int i = 0; i < nin; ++i)
+        os << pad << "const float " << var << "_a" << i << " = __ldg(in" << i << " + " << pos << ");\n";
+      os << pad << "const float " << var << " = " << P << "(";
+      for (int i = 0; i < nin; ++i) os << (i ? ", " : "") << var << "_a" << i;
+      os << ");\n";
+    } else {
+      os << pad << "const float " << var << " = " << P << "(" << pos << ins << ");\n";
+    }
+  };
+  auto consume = [&](const std::string &pos, const std::string &val) {
+    return sum ? "cc_acc(s_, c_, " + val + ");" : "out[" + pos + "] = " + val + ";";
+  };
+  for (int V : {1, 4}) {
+    for (int E : {1, 2, 4}) {
+      o << "extern \"C\" __global__ void __launch_bounds__(512) cc_t" << suffix << "_v" << V << "_e" << E << "("
+        << params
+        << (sum ? "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out"
+                : "float *__restrict__ out")
+        << ", cc_i64 n) {\n";
+      if (sum) o << "  float s_ = 0.0f, c_ = 0.0f;\n";
+      o << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+        << "  const cc_i64 tid = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x;\n";
+      if (V == 1) {
+        o << "  cc_i64 lin = tid;\n  for (; lin + " << (E - 1) << " * stride < n; lin += " << E << " * stride) {\n";
+        if (contiguous) {
+          // every load of the E positions first, then the arithmetic
+          for (int e = 0; e < E; ++e)
+            for (int i = 0; i < nin; ++i)
+              o << "    const float x" << e << "_" << i << " = __ldg(in" << i << " + lin + " << e << " * stride);\n";
+          for (int e = 0; e < E; ++e) {
+            std::string call = P + "(";
+            for (int i = 0; i < nin; ++i) call += (i ? ", " : "") + std::string("x") + std::to_string(e) + "_" + std::to_string(i);
+            call += ")";
+            o << "    " << consume("lin + " + std::to_string(e) + " * stride", call) << "\n";
+          }
+        } else {
+          for (int e = 0; e < E; ++e)
+            o << "    const float r" << e << " = " << P << "(lin + " << e << " * stride" << ins << ");\n";
+          for (int e = 0; e < E; ++e)
+            o << "    " << consume("lin + " + std::to_string(e) + " * stride", "r" + std::to_string(e)) << "\n";
+        }
+        o << "  }\n  for (; lin < n; lin += stride) {\n";
+        scalar_value("lin", o, "r", "    ");
+        o << "    " << consume("lin", "r") << "\n  }\n";
+      } else if (contiguous) {
+        // float4 loads: E float4 positions `stride` apart per thread
+        o << "  const cc_i64 n4 = n >> 2;\n  cc_i64 q = tid;\n"
+          << "  for (; q + " << (E - 1) << " * stride < n4; q += " << E << " * stride) {\n";
+        for (int e = 0; e < E; ++e)
+          for (int i = 0; i < nin; ++i)
+            o << "    const float4 x" << e << "_" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i
+              << ") + q + " << e << " * stride);\n";
+        for (int e = 0; e < E; ++e) {
+          auto lane_call = [&](const char *lane) {
+            std::string c = P + "(";
+            for (int i = 0; i < nin; ++i) c += (i ? ", " : "") + std::string("x") + std::to_string(e) + "_" + std::to_string(i) + lane;
+            return c + ")";
+          };
+          if (sum) {
+            for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    cc_acc(s_, c_, " << lane_call(lane) << ");\n";
+          } else {
+            o << "    {\n      float4 r;\n";
+            for (const char *lane : {".x", ".y", ".z", ".w"}) o << "      r" << lane << " = " << lane_call(lane) << ";\n";
+            o << "      reinterpret_cast<float4 *>(out)[q + " << e << " * stride] = r;\n    }\n";
+          }
+        }
+        o << "  }\n  for (; q < n4; q += stride) {\n";
+        for (int i = 0; i < nin; ++i)
+          o << "    const float4 x_" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
+        auto lane_call = [&](const char *lane) {
+          std::string c = P + "(";
+          for (int i = 0; i < nin; ++i) c += (i ? ", " : "") + std::string("x_") + std::to_string(i) + lane;
+          return c + ")";
+        };
+        if (sum) {
+          for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    cc_acc(s_, c_, " << lane_call(lane) << ");\n";
+        } else {
+          o << "    float4 r;\n";
+          for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    r" << lane << " = " << lane_call(lane) << ";\n";
+          o << "    reinterpret_cast<float4 *>(out)[q] = r;\n";
+        }
+        o << "  }\n  for (cc_i64 lin = (n4 << 2) + tid; lin < n; lin += stride) {\n";
+        scalar_value("lin", o, "r", "    ");
+        o << "    " << consume("lin", "r") << "\n  }\n";
+      } else {
+        // four consecutive points per work item, one float4 store when whole
+        o << "  const cc_i64 nw = (n + 3) >> 2;\n  cc_i64 w = tid;\n"
+          << "  for (; w + " << (E - 1) << " * stride < nw; w += " << E << " * stride) {\n";
+        for (int e = 0; e < E; ++e) {
+          const std::string b = "b" + std::to_string(e);
+          o << "    const cc_i64 " << b << " = (w + " << e << " * stride) << 2;\n"
+            << "    if (" << b << " + 3 < n) {\n";
+          for (int v = 0; v < 4; ++v)
+            o << "      const float r" << v << " = " << P << "(" << b << " + " << v << ins << ");\n";
+          if (sum)
+            o << "      cc_acc(s_, c_, r0);\n      cc_acc(s_, c_, r1);\n      cc_acc(s_, c_, r2);\n      cc_acc(s_, c_, r3);\n";
+          else
+            o << "      reinterpret_cast<float4 *>(out)[" << b << " >> 2] = make_float4(r0, r1, r2, r3);\n";
+          o << "    } else {\n      for (cc_i64 lin = " << b << "; lin < n; ++lin) {\n";
+          scalar_value("lin", o, "r", "        ");
+          o << "        " << consume("lin", "r") << "\n      }\n    }\n";
+        }
+        o << "  }\n  for (; w < nw; w += stride) {\n"
+          << "    for (cc_i64 lin = w << 2; lin < n && lin < (w << 2) + 4; ++lin) {\n";
+        scalar_value("lin", o, "r", "      ");
+        o << "      " << consume("lin", "r") << "\n    }\n  }\n";
+      }
+      if (sum) o << "  cc_grid_finish(s_, c_, partials, counter, out);\n";
+      o << "}\n";
+    }
+  }
+  return o.str();
 }
 
 }  // namespace cc

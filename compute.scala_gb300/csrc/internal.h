@@ -77,6 +77,9 @@ struct Ir {
 
 Ir parse_ir(const char *text, size_t len);
 
+// Device helpers every generated module starts with (device_common.cuh).
+extern const char *kPrelude;
+
 struct CodegenOptions {
   int block = 256;
   int load_lookahead = 8;   // loads kept in flight ahead of the arithmetic (generic kernels)
@@ -135,6 +138,28 @@ bool is_batchable(const Ir &ir, std::string *why);
 // the code of thousands of structures small).
 std::string point_function(const Ir &ir, const std::string &name, bool inline_it = true,
                            bool shared_transcendentals = false);
+
+// ---- tuning
+// A launch configuration of a program's tunable form: threads per block,
+// points per work item (1, or 4 consecutive points with float4 access),
+// work items per thread per loop iteration (their loads issued together), and
+// the grid: split 1 = at most one resident wave (the threads loop), split 2 =
+// one work batch per thread (sums: up to kMaxSumBlocks partials).
+struct TuneConfig {
+  int block = 256, vec = 1, ept = 1, split = 1;
+};
+constexpr int kTuneConfigs = 48;
+constexpr int kTuneKernels = 6;  // (vec, ept) pairs compiled per program
+constexpr int kFeatures = 64;
+TuneConfig tune_config(int index);
+int tune_kernel_index(const TuneConfig &c);
+int64_t tune_grid(int64_t n, const TuneConfig &c, bool sum, int sm_count, int resident);
+bool is_tunable(const Ir &ir, std::string *why);
+// Kernels cc_t<suffix>_v<1|4>_e<1|2|4> (arguments as the program's cc_ew /
+// cc_sum) and their point function; the module needs the prelude first.
+std::string tunable_source(const Ir &ir, const std::string &suffix);
+// The cost model's input for (program, configuration): kFeatures floats.
+void program_features(const Ir &ir, int config, int sm_count, float *out);
 
 // The literal text DecimalFormat gives a view coefficient (at most three
 // fraction digits, HALF_EVEN, no grouping), as OpenCLKernelBuilder.toLiteral.

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -27,6 +28,7 @@
 #include "gemm.h"
 #include "internal.h"
 #include "kernels.h"
+#include "mlp.h"
 
 namespace cc {
 
@@ -194,8 +196,54 @@ struct Module {
   }
 };
 
+// The tunable form of programs (tunable_source); one module may serve several.
+struct TuneModule {
+  CUmodule module = nullptr;
+  ~TuneModule() {
+    if (module && g_drv.ModuleUnload) g_drv.ModuleUnload(module);
+  }
+};
+
+struct TuneEntry {
+  std::shared_ptr<TuneModule> mod;
+  CUfunction fn[kTuneKernels] = {};
+  int resident[kTuneKernels][4] = {};  // blocks per SM by kernel and block size (0: not queried yet)
+  ProgramKind kind = ProgramKind::Elementwise;
+  int n_inputs = 0;
+  int64_t n = 0;
+  bool contiguous = false;
+  Ir ir;
+};
+
+// Programs compiled in their tunable form for timing (cc_tune_*).
+struct TuneSet {
+  std::vector<TuneEntry> entries;
+  void *flush = nullptr;  // written between timed launches to empty L2
+  size_t flush_cls = 0;
+  size_t flush_bytes = 0;
+};
+
+// A multilayer perceptron with its Adam state and batch scratch (cc_mlp_*).
+struct Mlp {
+  std::vector<int> dims;  // widths, input first
+  std::vector<size_t> w_off, b_off;
+  size_t n_params = 0;
+  void *state = nullptr;  // params, grads, Adam m, Adam v
+  size_t state_cls = 0;
+  int steps = 0;
+  int cap = 0;             // batch the scratch holds
+  void *scratch = nullptr;  // activations, deltas, column-sum partials, loss
+  size_t scratch_cls = 0;
+  float *params() { return static_cast<float *>(state); }
+  float *grads() { return params() + n_params; }
+  float *adam_m() { return params() + 2 * n_params; }
+  float *adam_v() { return params() + 3 * n_params; }
+};
+
 struct Program {
   std::shared_ptr<Module> mod;
+  std::unique_ptr<TuneEntry> tune;  // the tunable form (tuner on)
+  int tuned_config = -1;            // the configuration the tuner chose
   ProgramKind kind = ProgramKind::Elementwise;
   Generated gen;                // shape information (its source lives in the module)
   bool is_contraction = false;  // run as a GEMM (cc_gemm_f32 mode contraction_mode)
@@ -226,7 +274,7 @@ struct Batch {
   cudaGraphExec_t graph_exec = nullptr;
 };
 
-enum : uint64_t { kTagBuffer = 1, kTagProgram = 2, kTagEvent = 3, kTagBatch = 4 };
+enum : uint64_t { kTagBuffer = 1, kTagProgram = 2, kTagEvent = 3, kTagBatch = 4, kTagTuneSet = 5, kTagMlp = 6 };
 
 struct Context {
   int device = 0;
@@ -247,6 +295,10 @@ struct Context {
   std::unordered_map<std::string, std::shared_ptr<Module>> modules;  // structure key -> module
   std::unordered_map<uint64_t, Event *> events;
   std::unordered_map<uint64_t, Batch *> batches;
+  std::unordered_map<uint64_t, TuneSet *> tune_sets;
+  std::unordered_map<uint64_t, Mlp *> mlps;
+  uint64_t cost_model = 0;              // Mlp handle the learned tuner consults
+  std::vector<float> cost_mean, cost_inv_std;  // its feature normalisation
   uint64_t cache_hits = 0, cache_misses = 0;
   std::mutex compile_mu;
 
@@ -262,8 +314,9 @@ struct Context {
   int sum_block = 256;
   int tc_variant = 0;
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
-  int batch_inline = 0;
-  int batch_max_registers = 0;
+  int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
+  int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel
+  int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
 
@@ -419,7 +472,16 @@ void run_gemm(Context &c, const float *A, const float *B, float *C, int m, int n
   check_cuda(e, "bf16x6 contraction launch");
 }
 
+// Defined with the tuner, below.
+void launch_tuned_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream);
+std::shared_ptr<TuneModule> load_tune_module(const std::vector<char> &cubin);
+void load_tune_entry(TuneEntry &e, const Ir &ir, std::shared_ptr<TuneModule> mod, const std::string &suffix);
+
 void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
+  if (p.tune) {
+    launch_tuned_program(c, p, in, out, stream);
+    return;
+  }
   if (p.is_contraction) {
     const Contraction &q = p.con;
     run_gemm(c, reinterpret_cast<const float *>(in[q.a_input]), reinterpret_cast<const float *>(in[q.b_input]),
@@ -639,6 +701,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "sum_block") {
     if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
     c.sum_block = (int)value;
+  } else if (k == "tuner") {
+    if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "tuner must be 0 (off), 1 (exhaustive) or 2 (learned)");
+    c.tuner = (int)value;
   } else if (k == "batch_max_registers") {
     if (value < 0 || value > 255) fail(CC_ERR_INVALID_VALUE, "batch_max_registers must be in [0, 255]");
     c.batch_max_registers = (int)value;
@@ -681,6 +746,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "tc_variant") *value = c.tc_variant;
   else if (k == "contraction") *value = c.contraction;
   else if (k == "batch_inline") *value = c.batch_inline;
+  else if (k == "tuner") *value = c.tuner;
   else if (k == "batch_max_registers") *value = c.batch_max_registers;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END
@@ -844,7 +910,8 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   key += "#lookahead " + std::to_string(opt.load_lookahead) + " asm " + std::to_string((int)opt.asm_loads) +
          " blocks " + std::to_string(-opt.min_blocks) + " block " + std::to_string(opt.block) + " unroll " + std::to_string(opt.vec_unroll) +
          " prefetch " + std::to_string(opt.prefetch_min_bytes) + " sumblock " + std::to_string(c.sum_block) +
-         " contraction " + std::to_string(c.contraction) + " tc " + std::to_string(c.tc_variant) + "\n";
+         " contraction " + std::to_string(c.contraction) + " tc " + std::to_string(c.tc_variant) + " tuner " +
+         std::to_string(c.tuner) + "\n";
   {
     std::lock_guard<std::recursive_mutex> g(c.mu);
     auto it = c.cache.find(key);
@@ -883,6 +950,29 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     p->gen.domain = con.m * con.n;
     p->gen.source = "// contraction: C[" + std::to_string(con.m) + "," + std::to_string(con.n) + "] = A * B over " +
                     std::to_string(con.k) + " terms, cc_gemm_f32 mode " + std::to_string(p->contraction_mode) + "\n";
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    uint64_t h = c.make_handle(kTagProgram);
+    c.programs[h] = p.release();
+    c.cache[key] = h;
+    ++c.cache_misses;
+    *out = h;
+    return CC_OK;
+  }
+  int tuner_mode;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    tuner_mode = c.tuner;
+  }
+  if (tuner_mode > 0 && is_tunable(ir, nullptr)) {
+    // The tunable form alone; the tuner picks its configuration at the first launch.
+    auto p = std::make_unique<Program>();
+    p->kind = ir.kind;
+    p->gen = describe_program(ir);
+    p->gen.source = std::string("// generated by compute.scala_gb300 for sm_103a (tunable form)\n") + kPrelude + "\n" +
+                    tunable_source(ir, "");
+    std::vector<char> cubin = compile_cubin(p->gen.source, c.cc_major, c.cc_minor, c.flags);
+    p->tune = std::make_unique<TuneEntry>();
+    load_tune_entry(*p->tune, ir, load_tune_module(cubin), "");
     std::lock_guard<std::recursive_mutex> g(c.mu);
     uint64_t h = c.make_handle(kTagProgram);
     c.programs[h] = p.release();
@@ -1195,7 +1285,6 @@ int cc_event_release(cc_handle h) {
 // of them) kept as the comparison and for callers that want them.
 
 namespace cc {
-extern const char *kPrelude;
 namespace {
 
 constexpr int kBatchBlock = 256;
@@ -1315,15 +1404,9 @@ std::string batch_main_source(size_t n_structs) {
   return o.str();
 }
 
-// Compiles the parts in parallel and links them into one loadable image.
-std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs,
-                                    int cc_major, int cc_minor, uint32_t flags, bool link, int inline_level,
-                                    int max_registers) {
-  std::vector<std::string> sources;
-  for (size_t first = 0; first < structs.size(); first += kBatchChunk)
-    sources.push_back(batch_chunk_source(structs, struct_inputs, first,
-                                         std::min(structs.size(), first + (size_t)kBatchChunk), inline_level));
-  sources.push_back(batch_main_source(structs.size()));
+// NVRTC-compiles the sources on all host threads; the first failure is raised.
+std::vector<std::vector<char>> compile_parallel(const std::vector<std::string> &sources, int cc_major, int cc_minor,
+                                                uint32_t flags, bool relocatable, int max_registers) {
   std::vector<std::vector<char>> parts(sources.size());
   std::vector<std::string> errors(sources.size());
   std::atomic<size_t> next{0};
@@ -1335,7 +1418,7 @@ std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::v
     pool.emplace_back([&]() {
       for (size_t i; (i = next.fetch_add(1)) < sources.size();) {
         try {
-          parts[i] = compile_cubin(sources[i], cc_major, cc_minor, flags, true, max_registers);
+          parts[i] = compile_cubin(sources[i], cc_major, cc_minor, flags, relocatable, max_registers);
         } catch (const Error &e) {
           errors[i] = e.message;
         }
@@ -1345,6 +1428,19 @@ std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::v
   for (auto &th : pool) th.join();
   for (auto &e : errors)
     if (!e.empty()) fail(CC_ERR_BUILD_PROGRAM_FAILURE, e);
+  return parts;
+}
+
+// Compiles the parts in parallel and links them into one loadable image.
+std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs,
+                                    int cc_major, int cc_minor, uint32_t flags, bool link, int inline_level,
+                                    int max_registers) {
+  std::vector<std::string> sources;
+  for (size_t first = 0; first < structs.size(); first += kBatchChunk)
+    sources.push_back(batch_chunk_source(structs, struct_inputs, first,
+                                         std::min(structs.size(), first + (size_t)kBatchChunk), inline_level));
+  sources.push_back(batch_main_source(structs.size()));
+  std::vector<std::vector<char>> parts = compile_parallel(sources, cc_major, cc_minor, flags, true, max_registers);
   if (!link) return {};
   CUlinkState state;
   check_cu(g_drv.LinkCreate(0, nullptr, nullptr, &state), "cuLinkCreate");
@@ -1593,6 +1689,582 @@ int cc_batch_release(cc_handle batch) {
   g_drv.ModuleUnload(b.module);
   delete &b;
   c.batches.erase(batch);
+  CC_API_END
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- tuner
+//
+// A program's tunable form (tunable_source) runs in any of kTuneConfigs launch
+// configurations.  The exhaustive tuner times them all on the program's own
+// buffers at its first launch; the learned tuner asks a cost model (an Mlp
+// trained on such timings) for the configuration with the least predicted
+// log-runtime.  Tuning sets (cc_tune_*) compile many programs' tunable forms
+// at once and time configurations on request: the data the model learns from.
+
+namespace cc {
+namespace {
+
+constexpr int kTuneChunk = 16;                     // programs per NVRTC unit of a tuning set
+constexpr size_t kFlushBytes = size_t(256) << 20;  // written between timed launches: twice L2
+
+void wait_event_bounded(cudaEvent_t ev, uint64_t timeout_ns, const char *what) {
+  auto t0 = std::chrono::steady_clock::now();
+  int spin = 0;
+  for (;;) {
+    cudaError_t r = cudaEventQuery(ev);
+    if (r == cudaSuccess) return;
+    if (r != cudaErrorNotReady) check_cuda(r, what);
+    auto dt = std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
+    if ((uint64_t)dt >= timeout_ns) fail(CC_ERR_TIMEOUT, std::string(what) + ": not complete in time");
+    if (++spin > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+bool tune_config_fits(const TuneEntry &e, int config, const std::vector<uint64_t> &in, uint64_t out) {
+  if (tune_config(config).vec != 4) return true;
+  if (e.kind == ProgramKind::Elementwise && (out & 15u)) return false;
+  if (e.contiguous)
+    for (uint64_t a : in)
+      if (a & 15u) return false;
+  return true;
+}
+
+void launch_tune_entry(Context &c, TuneEntry &e, int config, const std::vector<uint64_t> &in, uint64_t out,
+                       cudaStream_t s) {
+  if (config < 0 || config >= kTuneConfigs) fail(CC_ERR_INVALID_VALUE, "configuration index out of range");
+  if (!tune_config_fits(e, config, in, out))
+    fail(CC_ERR_INVALID_VALUE, "a float4 configuration needs 16-byte aligned buffers");
+  const TuneConfig t = tune_config(config);
+  const int k = tune_kernel_index(t), bi = config % 4;
+  if (e.resident[k][bi] <= 0) {
+    check_cu(g_drv.OccupancyMaxActiveBlocks(&e.resident[k][bi], e.fn[k], t.block, 0), "cuOccupancyMaxActiveBlocks");
+    if (e.resident[k][bi] <= 0) fail(CC_ERR_OUT_OF_RESOURCES, "the configuration's block does not fit on an SM");
+  }
+  const bool sum = e.kind == ProgramKind::Sum;
+  const int64_t grid = tune_grid(e.n, t, sum, c.sm_count, e.resident[k][bi]);
+  std::vector<uint64_t> ptrs(in);
+  std::vector<void *> args;
+  for (auto &v : ptrs) args.push_back(&v);
+  uint64_t partials = reinterpret_cast<uint64_t>(c.partials());
+  uint64_t counter = reinterpret_cast<uint64_t>(c.counter());
+  uint64_t o = out;
+  long long n = e.n;
+  if (sum) {
+    args.push_back(&partials);
+    args.push_back(&counter);
+  }
+  args.push_back(&o);
+  args.push_back(&n);
+  check_cu(g_drv.LaunchKernel(e.fn[k], (unsigned)grid, 1, 1, t.block, 1, 1, 0, (CUstream)s, args.data(), nullptr),
+           "cuLaunchKernel");
+}
+
+// Median device time (ms) over `reps` launches of each configuration, after
+// one untimed launch; with a flush buffer, a write twice the size of L2
+// precedes every timed launch.  Configurations that do not apply to these
+// buffers get -1.
+void time_tune_entry(Context &c, TuneEntry &e, const int *configs, int n_configs, const std::vector<uint64_t> &in,
+                     uint64_t out, int reps, void *flush, size_t flush_bytes, float *ms) {
+  if (reps < 1) reps = 1;
+  cudaStream_t s = c.stream;
+  std::vector<cudaEvent_t> ev(2 * (size_t)reps, nullptr);
+  for (auto &x : ev) check_cuda(cudaEventCreate(&x), "cudaEventCreate");
+  auto destroy = [&]() {
+    for (auto &x : ev)
+      if (x) cudaEventDestroy(x);
+  };
+  try {
+    std::vector<float> t(reps);
+    for (int i = 0; i < n_configs; ++i) {
+      if (configs[i] < 0 || configs[i] >= kTuneConfigs) fail(CC_ERR_INVALID_VALUE, "configuration index out of range");
+      if (!tune_config_fits(e, configs[i], in, out)) {
+        ms[i] = -1.0f;
+        continue;
+      }
+      launch_tune_entry(c, e, configs[i], in, out, s);
+      for (int r = 0; r < reps; ++r) {
+        if (flush) check_cuda(cudaMemsetAsync(flush, r & 0xff, flush_bytes, s), "cudaMemsetAsync");
+        check_cuda(cudaEventRecord(ev[2 * r], s), "cudaEventRecord");
+        launch_tune_entry(c, e, configs[i], in, out, s);
+        check_cuda(cudaEventRecord(ev[2 * r + 1], s), "cudaEventRecord");
+      }
+      wait_event_bounded(ev[2 * reps - 1], 60ull * 1000000000ull, "timing a configuration");
+      for (int r = 0; r < reps; ++r) check_cuda(cudaEventElapsedTime(&t[r], ev[2 * r], ev[2 * r + 1]), "cudaEventElapsedTime");
+      std::sort(t.begin(), t.end());
+      ms[i] = t[reps / 2];
+    }
+  } catch (...) {
+    destroy();
+    throw;
+  }
+  destroy();
+}
+
+Mlp &mlp_of(Context &c, uint64_t h) {
+  auto it = c.mlps.find(h);
+  if (tag_of(h) != kTagMlp || it == c.mlps.end()) fail(CC_ERR_INVALID_VALUE, "not a live network handle");
+  return *it->second;
+}
+
+int mlp_max_width(const Mlp &m) { return *std::max_element(m.dims.begin(), m.dims.end()); }
+
+// Scratch layout for a batch of `cap`: activations h_1..h_L, two deltas, the
+// column-sum partials, the loss.
+void mlp_reserve(Context &c, Mlp &m, int batch) {
+  if (batch <= m.cap) return;
+  size_t acts = 0;
+  for (size_t l = 1; l < m.dims.size(); ++l) acts += (size_t)m.dims[l];
+  const size_t w = (size_t)mlp_max_width(m);
+  const size_t floats = (size_t)batch * acts + 2 * (size_t)batch * w + (size_t)colsum_chunks(batch) * w + 64;
+  if (m.scratch) {
+    check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+    c.pool.release(m.scratch, m.scratch_cls);
+    m.scratch = nullptr;
+    m.cap = 0;
+  }
+  m.scratch = c.pool.alloc(floats * sizeof(float), &m.scratch_cls);
+  m.cap = batch;
+}
+
+float *mlp_act(Mlp &m, size_t l) {  // h_l, l >= 1
+  size_t off = 0;
+  for (size_t j = 1; j < l; ++j) off += (size_t)m.dims[j] * m.cap;
+  return static_cast<float *>(m.scratch) + off;
+}
+float *mlp_delta(Mlp &m, int which) {
+  return mlp_act(m, m.dims.size()) + (size_t)which * m.cap * mlp_max_width(m);
+}
+float *mlp_partial(Mlp &m) { return mlp_delta(m, 2); }
+float *mlp_loss(Mlp &m) { return mlp_partial(m) + (size_t)colsum_chunks(m.cap) * mlp_max_width(m); }
+
+void mlp_forward(Context &c, Mlp &m, const float *x, int batch, float *y, cudaStream_t s) {
+  const size_t L = m.dims.size() - 1;
+  for (size_t l = 1; l <= L; ++l) {
+    const float *in = l == 1 ? x : mlp_act(m, l - 1);
+    float *o = (l == L && y) ? y : mlp_act(m, l);
+    const int k = m.dims[l - 1], n = m.dims[l];
+    check_cuda(launch_mlp_gemm(false, false, in, m.params() + m.w_off[l], o, batch, n, k, k, n, n,
+                               m.params() + m.b_off[l], l < L ? kMlpBiasRelu : kMlpBias, nullptr, s),
+               "network forward");
+  }
+}
+
+// Forward, loss and every parameter's gradient (into m.grads()).
+void mlp_backward(Context &c, Mlp &m, const float *x, const float *t, int batch, cudaStream_t s) {
+  const size_t L = m.dims.size() - 1;
+  mlp_forward(c, m, x, batch, nullptr, s);
+  int cur = 0;
+  check_cuda(launch_mse(mlp_act(m, L), t, batch, mlp_delta(m, cur), mlp_loss(m), s), "loss");
+  for (size_t l = L; l >= 1; --l) {
+    const float *in = l == 1 ? x : mlp_act(m, l - 1);
+    const int k = m.dims[l - 1], n = m.dims[l];
+    float *d = mlp_delta(m, cur);
+    check_cuda(launch_mlp_gemm(true, false, in, d, m.grads() + m.w_off[l], k, n, batch, k, n, n, nullptr, kMlpNone,
+                               nullptr, s),
+               "weight gradient");
+    check_cuda(launch_colsum(d, batch, n, mlp_partial(m), m.grads() + m.b_off[l], s), "bias gradient");
+    if (l > 1) {
+      check_cuda(launch_mlp_gemm(false, true, d, m.params() + m.w_off[l], mlp_delta(m, 1 - cur), batch, k, n, n, n, k,
+                                 nullptr, kMlpReluMask, mlp_act(m, l - 1), s),
+                 "delta");
+      cur = 1 - cur;
+    }
+  }
+}
+
+int choose_exhaustive(Context &c, TuneEntry &e, const std::vector<uint64_t> &in, uint64_t out) {
+  std::vector<int> configs(kTuneConfigs);
+  for (int i = 0; i < kTuneConfigs; ++i) configs[i] = i;
+  std::vector<float> ms(kTuneConfigs);
+  size_t cls = 0;
+  void *flush = c.pool.alloc(kFlushBytes, &cls);
+  try {
+    time_tune_entry(c, e, configs.data(), kTuneConfigs, in, out, 3, flush, kFlushBytes, ms.data());
+  } catch (...) {
+    c.pool.release(flush, cls);
+    throw;
+  }
+  c.pool.release(flush, cls);
+  int best = -1;
+  for (int i = 0; i < kTuneConfigs; ++i)
+    if (ms[i] >= 0.0f && (best < 0 || ms[i] < ms[best])) best = i;
+  if (best < 0) fail(CC_ERR_INVALID_OPERATION, "no configuration applies to these buffers");
+  return best;
+}
+
+int choose_learned(Context &c, TuneEntry &e, const std::vector<uint64_t> &in, uint64_t out) {
+  if (!c.cost_model) fail(CC_ERR_INVALID_OPERATION, "the learned tuner needs a cost model (cc_tuner_set_model)");
+  Mlp &m = mlp_of(c, c.cost_model);
+  std::vector<float> x((size_t)kTuneConfigs * kFeatures);
+  for (int i = 0; i < kTuneConfigs; ++i) {
+    float *f = &x[(size_t)i * kFeatures];
+    program_features(e.ir, i, c.sm_count, f);
+    for (int j = 0; j < kFeatures; ++j) f[j] = (f[j] - c.cost_mean[j]) * c.cost_inv_std[j];
+  }
+  size_t cls = 0;
+  float *dx = static_cast<float *>(c.pool.alloc((x.size() + kTuneConfigs) * sizeof(float), &cls));
+  std::vector<float> y(kTuneConfigs);
+  try {
+    mlp_reserve(c, m, kTuneConfigs);
+    check_cuda(cudaMemcpyAsync(dx, x.data(), x.size() * sizeof(float), cudaMemcpyHostToDevice, c.stream), "upload");
+    mlp_forward(c, m, dx, kTuneConfigs, dx + x.size(), c.stream);
+    check_cuda(cudaMemcpyAsync(y.data(), dx + x.size(), y.size() * sizeof(float), cudaMemcpyDeviceToHost, c.stream),
+               "download");
+    check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  } catch (...) {
+    c.pool.release(dx, cls);
+    throw;
+  }
+  c.pool.release(dx, cls);
+  int best = -1;
+  for (int i = 0; i < kTuneConfigs; ++i)
+    if (tune_config_fits(e, i, in, out) && (best < 0 || y[i] < y[best])) best = i;
+  if (best < 0) fail(CC_ERR_INVALID_OPERATION, "no configuration applies to these buffers");
+  return best;
+}
+
+TuneSet &tune_set_of(Context &c, uint64_t h) {
+  auto it = c.tune_sets.find(h);
+  if (tag_of(h) != kTagTuneSet || it == c.tune_sets.end()) fail(CC_ERR_INVALID_VALUE, "not a live tuning set handle");
+  return *it->second;
+}
+
+std::vector<Ir> parse_tunable(const char *const *irs, const size_t *lens, int n) {
+  if (!irs || !lens || n <= 0) fail(CC_ERR_INVALID_VALUE, "no programs");
+  std::vector<Ir> out;
+  out.reserve(n);
+  for (int p = 0; p < n; ++p) {
+    if (!irs[p]) fail(CC_ERR_INVALID_VALUE, "null program text");
+    out.push_back(parse_ir(irs[p], lens[p]));
+    std::string why;
+    if (!is_tunable(out.back(), &why)) fail(CC_ERR_INVALID_PROGRAM, "program " + std::to_string(p) + ": " + why);
+  }
+  return out;
+}
+
+std::vector<std::string> tune_sources(const std::vector<Ir> &irs) {
+  std::vector<std::string> sources;
+  for (size_t first = 0; first < irs.size(); first += kTuneChunk) {
+    std::ostringstream o;
+    o << "// generated by compute.scala_gb300 for sm_103a (tunable forms)\n" << kPrelude << "\n";
+    for (size_t p = first; p < irs.size() && p < first + kTuneChunk; ++p) o << tunable_source(irs[p], "_" + std::to_string(p));
+    sources.push_back(o.str());
+  }
+  return sources;
+}
+
+std::shared_ptr<TuneModule> load_tune_module(const std::vector<char> &cubin) {
+  auto m = std::make_shared<TuneModule>();
+  check_cu(g_drv.ModuleLoadData(&m->module, cubin.data()), "cuModuleLoadData");
+  return m;
+}
+
+void load_tune_entry(TuneEntry &e, const Ir &ir, std::shared_ptr<TuneModule> mod, const std::string &suffix) {
+  e.mod = std::move(mod);
+  int k = 0;
+  for (int V : {1, 4})
+    for (int E : {1, 2, 4}) {
+      std::string name = "cc_t" + suffix + "_v" + std::to_string(V) + "_e" + std::to_string(E);
+      check_cu(g_drv.ModuleGetFunction(&e.fn[k++], e.mod->module, name.c_str()), "cuModuleGetFunction");
+    }
+  e.kind = ir.kind;
+  e.n_inputs = ir.n_params;
+  e.n = 1;
+  for (int64_t d : ir.out_shape) e.n *= d;
+  e.contiguous = !contiguous_structure_key(ir).empty();
+  e.ir = ir;
+}
+
+void launch_tuned_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
+  TuneEntry &e = *p.tune;
+  if (p.tuned_config < 0 || !tune_config_fits(e, p.tuned_config, in, out)) {
+    if (stream != c.stream) check_cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    p.tuned_config = c.tuner == 2 ? choose_learned(c, e, in, out) : choose_exhaustive(c, e, in, out);
+  }
+  launch_tune_entry(c, e, p.tuned_config, in, out, stream);
+}
+
+}  // namespace
+}  // namespace cc
+
+extern "C" {
+
+int cc_tune_config(int index, int *block, int *vec, int *ept, int *split) {
+  CC_API_BEGIN
+  if (index < 0 || index >= kTuneConfigs) fail(CC_ERR_INVALID_VALUE, "configuration index out of range");
+  TuneConfig t = tune_config(index);
+  if (block) *block = t.block;
+  if (vec) *vec = t.vec;
+  if (ept) *ept = t.ept;
+  if (split) *split = t.split;
+  CC_API_END
+}
+
+int cc_program_features(const char *ir_text, size_t ir_len, int config, int sm_count, float *out) {
+  CC_API_BEGIN
+  if (!ir_text || !out) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  if (config < 0 || config >= kTuneConfigs) fail(CC_ERR_INVALID_VALUE, "configuration index out of range");
+  Ir ir = parse_ir(ir_text, ir_len);
+  std::string why;
+  if (!is_tunable(ir, &why)) fail(CC_ERR_INVALID_PROGRAM, why);
+  program_features(ir, config, sm_count, out);
+  CC_API_END
+}
+
+int cc_tune_compile_check(const char *const *irs, const size_t *lens, int n_programs, int cc_major, int cc_minor,
+                          double *seconds) {
+  CC_API_BEGIN
+  auto t0 = std::chrono::steady_clock::now();
+  std::vector<Ir> parsed = parse_tunable(irs, lens, n_programs);
+  compile_parallel(tune_sources(parsed), cc_major, cc_minor, 0, false, 0);
+  if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  CC_API_END
+}
+
+int cc_tune_create(const char *const *irs, const size_t *lens, int n_programs, cc_handle *set) {
+  CC_API_BEGIN
+  if (!set) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Context &c = ctx();
+  std::vector<Ir> parsed = parse_tunable(irs, lens, n_programs);
+  std::vector<std::vector<char>> cubins;
+  {
+    std::lock_guard<std::mutex> cg(c.compile_mu);
+    cubins = compile_parallel(tune_sources(parsed), c.cc_major, c.cc_minor, c.flags, false, 0);
+  }
+  auto ts = std::make_unique<TuneSet>();
+  ts->entries.resize(parsed.size());
+  for (size_t u = 0; u < cubins.size(); ++u) {
+    auto mod = load_tune_module(cubins[u]);
+    for (size_t p = u * kTuneChunk; p < parsed.size() && p < (u + 1) * kTuneChunk; ++p)
+      load_tune_entry(ts->entries[p], parsed[p], mod, "_" + std::to_string(p));
+  }
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  uint64_t h = c.make_handle(kTagTuneSet);
+  c.tune_sets[h] = ts.release();
+  *set = h;
+  CC_API_END
+}
+
+namespace {
+std::vector<uint64_t> tune_ptrs(const TuneEntry &e, const uint64_t *ptrs, size_t n_ptrs) {
+  if (!ptrs || n_ptrs != (size_t)e.n_inputs + 1)
+    fail(CC_ERR_INVALID_KERNEL_ARGS, "the program needs " + std::to_string(e.n_inputs + 1) + " pointers (inputs, then the output)");
+  for (size_t i = 0; i < n_ptrs; ++i)
+    if (!ptrs[i]) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  return std::vector<uint64_t>(ptrs, ptrs + e.n_inputs);
+}
+}  // namespace
+
+int cc_tune_info(cc_handle set, int *n_programs) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  TuneSet &ts = tune_set_of(c, set);
+  if (n_programs) *n_programs = (int)ts.entries.size();
+  CC_API_END
+}
+
+int cc_tune_launch(cc_handle set, int program, const uint64_t *ptrs, size_t n_ptrs, int config, uint64_t stream) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  TuneSet &ts = tune_set_of(c, set);
+  if (program < 0 || program >= (int)ts.entries.size()) fail(CC_ERR_INVALID_VALUE, "program index out of range");
+  TuneEntry &e = ts.entries[program];
+  std::vector<uint64_t> in = tune_ptrs(e, ptrs, n_ptrs);
+  launch_tune_entry(c, e, config, in, ptrs[e.n_inputs], stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream);
+  CC_API_END
+}
+
+int cc_tune_time(cc_handle set, int program, const uint64_t *ptrs, size_t n_ptrs, const int *configs, int n_configs,
+                 int reps, int flush_l2, float *ms) {
+  CC_API_BEGIN
+  if (!configs || !ms || n_configs <= 0) fail(CC_ERR_INVALID_VALUE, "no configurations");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  TuneSet &ts = tune_set_of(c, set);
+  if (program < 0 || program >= (int)ts.entries.size()) fail(CC_ERR_INVALID_VALUE, "program index out of range");
+  TuneEntry &e = ts.entries[program];
+  std::vector<uint64_t> in = tune_ptrs(e, ptrs, n_ptrs);
+  if (flush_l2 && !ts.flush) {
+    ts.flush = c.pool.alloc(kFlushBytes, &ts.flush_cls);
+    ts.flush_bytes = kFlushBytes;
+  }
+  time_tune_entry(c, e, configs, n_configs, in, ptrs[e.n_inputs], reps, flush_l2 ? ts.flush : nullptr, ts.flush_bytes,
+                  ms);
+  CC_API_END
+}
+
+int cc_tune_release(cc_handle set) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  TuneSet &ts = tune_set_of(c, set);
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  if (ts.flush) c.pool.release(ts.flush, ts.flush_cls);
+  delete &ts;
+  c.tune_sets.erase(set);
+  CC_API_END
+}
+
+int cc_tuner_choice(cc_handle prog, int *config) {
+  CC_API_BEGIN
+  if (!config) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Program &p = program_of(c, prog);
+  *config = p.tune ? p.tuned_config : -1;
+  CC_API_END
+}
+
+// ---- the cost model's network
+
+int cc_mlp_create(const int *dims, int n_dims, cc_handle *mlp) {
+  CC_API_BEGIN
+  if (!dims || !mlp || n_dims < 2 || n_dims > 16) fail(CC_ERR_INVALID_VALUE, "a network has 2 to 16 widths");
+  Context &c = ctx();
+  auto m = std::make_unique<Mlp>();
+  m->dims.assign(dims, dims + n_dims);
+  m->w_off.assign(n_dims, 0);
+  m->b_off.assign(n_dims, 0);
+  size_t off = 0;
+  for (int l = 1; l < n_dims; ++l) {
+    if (dims[l - 1] <= 0 || dims[l] <= 0 || dims[l] > 65536) fail(CC_ERR_INVALID_VALUE, "widths must be in [1, 65536]");
+    m->w_off[l] = off;
+    off += (size_t)dims[l - 1] * dims[l];
+    m->b_off[l] = off;
+    off += (size_t)dims[l];
+  }
+  m->n_params = off;
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  m->state = c.pool.alloc(4 * off * sizeof(float), &m->state_cls);
+  check_cuda(cudaMemsetAsync(m->state, 0, 4 * off * sizeof(float), c.stream), "cudaMemsetAsync");
+  uint64_t h = c.make_handle(kTagMlp);
+  c.mlps[h] = m.release();
+  *mlp = h;
+  CC_API_END
+}
+
+int cc_mlp_info(cc_handle mlp, size_t *n_params, int *steps) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Mlp &m = mlp_of(c, mlp);
+  if (n_params) *n_params = m.n_params;
+  if (steps) *steps = m.steps;
+  CC_API_END
+}
+
+int cc_mlp_set_params(cc_handle mlp, const float *host, size_t n) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Mlp &m = mlp_of(c, mlp);
+  if (!host || n != m.n_params) fail(CC_ERR_INVALID_VALUE, "expected " + std::to_string(m.n_params) + " parameters");
+  check_cuda(cudaMemcpyAsync(m.params(), host, n * sizeof(float), cudaMemcpyHostToDevice, c.stream), "upload");
+  check_cuda(cudaMemsetAsync(m.adam_m(), 0, 2 * n * sizeof(float), c.stream), "cudaMemsetAsync");
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  m.steps = 0;
+  CC_API_END
+}
+
+int cc_mlp_get_params(cc_handle mlp, float *host, size_t n) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Mlp &m = mlp_of(c, mlp);
+  if (!host || n != m.n_params) fail(CC_ERR_INVALID_VALUE, "expected " + std::to_string(m.n_params) + " parameters");
+  check_cuda(cudaMemcpyAsync(host, m.params(), n * sizeof(float), cudaMemcpyDeviceToHost, c.stream), "download");
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  CC_API_END
+}
+
+int cc_mlp_forward(cc_handle mlp, uint64_t x, int batch, uint64_t y, uint64_t stream) {
+  CC_API_BEGIN
+  if (!x || !y || batch <= 0) fail(CC_ERR_INVALID_VALUE, "null pointer or empty batch");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Mlp &m = mlp_of(c, mlp);
+  cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
+  if (s != c.stream) check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  mlp_reserve(c, m, batch);
+  mlp_forward(c, m, reinterpret_cast<const float *>(x), batch, reinterpret_cast<float *>(y), s);
+  if (s != c.stream) check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");  // the scratch is the context's
+  CC_API_END
+}
+
+int cc_mlp_gradients(cc_handle mlp, uint64_t x, uint64_t t, int batch, float *loss, float *grads) {
+  CC_API_BEGIN
+  if (!x || !t || batch <= 0) fail(CC_ERR_INVALID_VALUE, "null pointer or empty batch");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Mlp &m = mlp_of(c, mlp);
+  mlp_reserve(c, m, batch);
+  mlp_backward(c, m, reinterpret_cast<const float *>(x), reinterpret_cast<const float *>(t), batch, c.stream);
+  if (loss)
+    check_cuda(cudaMemcpyAsync(loss, mlp_loss(m), sizeof(float), cudaMemcpyDeviceToHost, c.stream), "download");
+  if (grads)
+    check_cuda(cudaMemcpyAsync(grads, m.grads(), m.n_params * sizeof(float), cudaMemcpyDeviceToHost, c.stream),
+               "download");
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  CC_API_END
+}
+
+int cc_mlp_train_step(cc_handle mlp, uint64_t x, uint64_t t, int batch, float lr, float beta1, float beta2, float eps,
+                      float *loss) {
+  CC_API_BEGIN
+  if (!x || !t || batch <= 0) fail(CC_ERR_INVALID_VALUE, "null pointer or empty batch");
+  if (!(lr > 0.0f) || !(beta1 >= 0.0f && beta1 < 1.0f) || !(beta2 >= 0.0f && beta2 < 1.0f) || !(eps > 0.0f))
+    fail(CC_ERR_INVALID_VALUE, "Adam needs lr > 0, betas in [0, 1) and eps > 0");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Mlp &m = mlp_of(c, mlp);
+  mlp_reserve(c, m, batch);
+  mlp_backward(c, m, reinterpret_cast<const float *>(x), reinterpret_cast<const float *>(t), batch, c.stream);
+  ++m.steps;
+  const float c1 = (float)(1.0 - std::pow((double)beta1, (double)m.steps));
+  const float c2 = (float)(1.0 - std::pow((double)beta2, (double)m.steps));
+  check_cuda(launch_adam(m.params(), m.grads(), m.adam_m(), m.adam_v(), (long long)m.n_params, lr, beta1, beta2, eps,
+                         c1, c2, c.sm_count, c.stream),
+             "adam");
+  if (loss) {
+    check_cuda(cudaMemcpyAsync(loss, mlp_loss(m), sizeof(float), cudaMemcpyDeviceToHost, c.stream), "download");
+    check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  }
+  CC_API_END
+}
+
+int cc_mlp_release(cc_handle mlp) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Mlp &m = mlp_of(c, mlp);
+  check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
+  if (m.scratch) c.pool.release(m.scratch, m.scratch_cls);
+  c.pool.release(m.state, m.state_cls);
+  if (c.cost_model == mlp) c.cost_model = 0;
+  delete &m;
+  c.mlps.erase(mlp);
+  CC_API_END
+}
+
+int cc_tuner_set_model(cc_handle mlp, const float *mean, const float *inv_std) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  if (!mlp) {
+    c.cost_model = 0;
+    return CC_OK;
+  }
+  Mlp &m = mlp_of(c, mlp);
+  if (m.dims.front() != kFeatures || m.dims.back() != 1)
+    fail(CC_ERR_INVALID_VALUE, "a cost model maps " + std::to_string(kFeatures) + " features to one value");
+  if (!mean || !inv_std) fail(CC_ERR_INVALID_VALUE, "null pointer");
+  c.cost_mean.assign(mean, mean + kFeatures);
+  c.cost_inv_std.assign(inv_std, inv_std + kFeatures);
+  c.cost_model = mlp;
   CC_API_END
 }
 

@@ -83,9 +83,13 @@ int cc_synchronize(void);
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
  *                       3 = CC_GEMM_BF16X6
- *   "batch_max_registers" batch modules: register cap per thread of every compiled part (0 = none)
- *   "batch_inline"      batch modules: 0 = expressions and exp/log/tanh are called functions
- *                       (default), 1 = expressions inlined, exp/log/tanh called, 2 = all inlined
+ *   "tuner"             0 = generated kernels with the fixed launch shape (default), 1 = exhaustive
+ *                       tuner, 2 = learned tuner (see the tuner section)
+ *   "batch_max_registers" batch modules: register cap per thread of every compiled part (0 = none;
+ *                       default 128: the indirect calls of the persistent kernel otherwise take the
+ *                       largest part's registers and one block per SM)
+ *   "batch_inline"      batch modules: 0 = expressions and exp/log/tanh are called functions,
+ *                       1 = expressions inlined, exp/log/tanh called (default), 2 = all inlined
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
  *                       registers (FP32-level error at any K; default), 1 = 128x256 tiles, one
  *                       accumulator per tile (fastest, error grows with K), 2 = 128x128, one per tile
@@ -209,6 +213,66 @@ int cc_batch_release(cc_handle batch);
 /* GPU-free: generates and NVRTC-compiles a batch module for sm_<cc_major><cc_minor>a. */
 int cc_batch_compile_check(const char *const *irs, const size_t *ir_lens, int n_programs, int cc_major, int cc_minor,
                            int *n_structures, double *seconds);
+
+/* ---- tuner.  No reference counterpart: the reference lets the OpenCL runtime
+ *      choose the local size (Tensors.scala:1360-1375) and sizes reduction
+ *      groups as min(length, CL_KERNEL_WORK_GROUP_SIZE) (Tensors.scala:700).
+ *      A program's tunable form runs in CC_TUNE_CONFIGS launch configurations:
+ *      index i -> block {64,128,256,512}[i%4], vector width {1,4}[(i/4)%2],
+ *      work items per thread {1,2,4}[(i/8)%3], grid split {1,2}[(i/24)%2]
+ *      (1: at most one resident wave of blocks, the threads loop; 2: one batch
+ *      of work items per thread; for a sum, the number of partial sums).
+ *      Elementwise results are identical in every configuration; sums differ
+ *      in the order of their compensated partials.
+ *      With the "tuner" knob at 1 (exhaustive), cc_program_get compiles the
+ *      tunable form and the first launch times all configurations on its own
+ *      buffers (3 launches each after an L2 flush) and keeps the fastest; at 2
+ *      (learned) the cost model installed by cc_tuner_set_model predicts each
+ *      configuration's log-runtime and the least is kept. -------------------- */
+#define CC_TUNE_CONFIGS 48
+#define CC_FEATURES 64
+int cc_tune_config(int index, int *block, int *vec, int *ept, int *split);
+/* The cost model's features of (program, configuration) for a GPU of sm_count SMs: CC_FEATURES floats. */
+int cc_program_features(const char *ir, size_t ir_len, int config, int sm_count, float *out);
+/* The configuration the tuner chose for a program (-1: not launched yet or not tuned). */
+int cc_tuner_choice(cc_handle program, int *config);
+/* Installs network `mlp` (CC_FEATURES inputs, one output) as the learned tuner's
+ * model; inputs are normalised as (feature - mean) * inv_std.  mlp = 0 removes it. */
+int cc_tuner_set_model(cc_handle mlp, const float *mean, const float *inv_std);
+/* Tuning sets: many programs' tunable forms compiled together (NVRTC units of
+ * 16 programs, compiled on all host threads) and timed on request. */
+int cc_tune_create(const char *const *irs, const size_t *ir_lens, int n_programs, cc_handle *set);
+int cc_tune_info(cc_handle set, int *n_programs);
+/* ptrs: the program's inputs in parameter order, then its output. */
+int cc_tune_launch(cc_handle set, int program, const uint64_t *ptrs, size_t n_ptrs, int config, uint64_t stream);
+/* ms[i]: median device time of `reps` launches of configs[i] (after one untimed
+ * launch; with flush_l2, a 256 MiB write precedes each); -1 where a float4
+ * configuration meets a buffer that is not 16-byte aligned. */
+int cc_tune_time(cc_handle set, int program, const uint64_t *ptrs, size_t n_ptrs, const int *configs, int n_configs,
+                 int reps, int flush_l2, float *ms);
+int cc_tune_release(cc_handle set);
+/* GPU-free: generates and NVRTC-compiles the tunable forms for sm_<cc_major><cc_minor>a. */
+int cc_tune_compile_check(const char *const *irs, const size_t *ir_lens, int n_programs, int cc_major, int cc_minor,
+                          double *seconds);
+
+/* ---- the cost model's network: a multilayer perceptron with ReLU hidden
+ *      layers, trained by its own CUDA kernels (forward, backward, Adam) on a
+ *      mean-squared-error loss.  dims: widths, input first (the cost model is
+ *      {64, 256, 256, 256, 1}).  Parameters are packed per layer as W (rows =
+ *      inputs, row-major) then b.  x: batch x dims[0] floats, row-major, and
+ *      t / y: batch floats, all device pointers. ----------------------------- */
+int cc_mlp_create(const int *dims, int n_dims, cc_handle *mlp);
+int cc_mlp_info(cc_handle mlp, size_t *n_params, int *steps);
+/* Also zeroes the Adam moments and the step count. */
+int cc_mlp_set_params(cc_handle mlp, const float *host, size_t n);
+int cc_mlp_get_params(cc_handle mlp, float *host, size_t n);
+int cc_mlp_forward(cc_handle mlp, uint64_t x, int batch, uint64_t y, uint64_t stream);
+/* Loss (mean squared error) and the gradient of every parameter, copied to the host (either may be NULL). */
+int cc_mlp_gradients(cc_handle mlp, uint64_t x, uint64_t t, int batch, float *loss, float *grads);
+/* One Adam step on the batch's gradients; loss (may be NULL) is the loss before the step. */
+int cc_mlp_train_step(cc_handle mlp, uint64_t x, uint64_t t, int batch, float lr, float beta1, float beta2, float eps,
+                      float *loss);
+int cc_mlp_release(cc_handle mlp);
 
 /* ---- random numbers: Tensor.random / Tensor.randomNormal with the Wang hash
  *      (Tensors.scala:106-117, :397-524).  normal=0: uniform [0,1]; normal=1:
