@@ -364,6 +364,9 @@ def main():
     ap.add_argument("--programs", type=int, default=2048, help="c5: tuning workloads to time (the last 10%% held out)")
     ap.add_argument("--db", default=None, help="c5: append the timing records (JSON lines) to this file")
     ap.add_argument("--collect-budget-s", type=float, default=None, help="c5: stop collecting after this long")
+    ap.add_argument("--db-in", default=None, help="c5: train and evaluate on these timing records instead of timing")
+    ap.add_argument("--save-model", default=None, help="c5: write the trained cost model (.npz) here")
+    ap.add_argument("--epochs", type=int, default=40, help="c5: training epochs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true", help="skip the clock sampling (and its untimed busy loop)")
@@ -472,25 +475,32 @@ def main_tuner(args, warmup, rank, world, local_rank):
     rt = NativeRuntime(local_rank)
     sm = rt.device_info()["sm_count"]
     t0 = time.time()
-    progs = tuner.random_programs(args.programs, seed=0)
-    gen_s = time.time() - t0
-    log = open(args.db, "a") if args.db else None
-    t0 = time.time()
-    try:
-        recs = tuner.collect(rt, progs, reps=3, flush_l2=True, log=log, time_budget_s=args.collect_budget_s)
-    finally:
-        if log:
-            log.close()
-    collect_s = time.time() - t0
+    if args.db_in:
+        recs = [json.loads(line) for line in open(args.db_in)][:args.programs]
+        gen_s = 0.0
+        collect_s = 0.0
+    else:
+        progs = tuner.random_programs(args.programs, seed=0)
+        gen_s = time.time() - t0
+        log = open(args.db, "a") if args.db else None
+        t0 = time.time()
+        try:
+            recs = tuner.collect(rt, progs, reps=5, flush_l2=True, log=log, time_budget_s=args.collect_budget_s)
+        finally:
+            if log:
+                log.close()
+        collect_s = time.time() - t0
     split = int(len(recs) * 0.9)
     train, test = recs[:split], recs[split:]
     x, y = tuner.training_arrays(train, sm)
     model = tuner.CostModel(rt, seed=0)
     t0 = time.time()
-    losses = model.fit(x, y, epochs=40, batch=4096, lr=2e-3, lr_final=1e-4)
+    losses = model.fit(x, y, epochs=args.epochs, batch=4096, lr=2e-3, lr_final=1e-4)
     rt.synchronize()
     train_s = time.time() - t0
-    steps = 40 * max(1, x.shape[0] // 4096)
+    steps = args.epochs * max(1, x.shape[0] // 4096)
+    if args.save_model:
+        model.save(args.save_model)
     fixed = tuner.best_fixed_config(train)
     res = tuner.evaluate(model, test, sm, fixed=fixed)
     xt = tuner.feature_matrix([r["ir"] for r in test], sm)
@@ -508,8 +518,9 @@ def main_tuner(args, warmup, rank, world, local_rank):
                                    "random permute/broadcast/translate views, 3-12-node trees over "
                                    "+,-,*,/,exp,log,tanh,max, optional full or inner-axis sum; 48 configs each",
                        "programs_timed": len(recs), "train": len(train), "held_out": len(test), "kinds": kinds,
-                       "timing": "median of 3 launches per config, L2 flushed (256 MiB write) before each",
-                       "model": "MLP 64-256-256-256-1 ReLU, Adam, 40 epochs, batch 4096, own CUDA kernels"},
+                       "timing": "median of 5 launches per config, L2 flushed (256 MiB write) before each",
+                       "model": "MLP 64-256-256-256-1 ReLU, Adam, %d epochs, batch 4096, own CUDA kernels" % args.epochs,
+                       "timings_from": args.db_in or "collected in this run"},
             "tuner": res, "train_loss_first_last": [losses[0], losses[-1]],
             "seconds": {"generate": round(gen_s, 1), "compile_and_time": round(collect_s, 1),
                         "train": round(train_s, 2), "predict_held_out": round(predict_s, 3)},

@@ -189,7 +189,7 @@ def random_programs(count: int, seed: int = 0, max_points: int = MAX_POINTS, max
     return [random_program(r, d, max_points, max_dim) for _ in range(count)]
 
 
-def collect(runtime, programs: Sequence[dict], reps: int = 3, flush_l2: bool = True, chunk: int = 256,
+def collect(runtime, programs: Sequence[dict], reps: int = 5, flush_l2: bool = True, chunk: int = 256,
             log=None, time_budget_s: Optional[float] = None) -> List[dict]:
     """Times every configuration of every program; returns one record per program
     ({"ir", "params", "kind", "points", "ms": [48 floats]}), and appends them to
@@ -213,10 +213,20 @@ def collect(runtime, programs: Sequence[dict], reps: int = 3, flush_l2: bool = T
     ptr_out = out.device_ptr()
     records = []
     t0 = time.time()
+    firsts = list(range(0, len(programs), chunk))
+    # the next chunk compiles (host threads) while this one is timed (GPU)
+    from concurrent.futures import ThreadPoolExecutor
+    pool = ThreadPoolExecutor(1)
+    pending = None
     try:
-        for first in range(0, len(programs), chunk):
+        pending = pool.submit(TuneSet, runtime, [q["ir"] for q in programs[0:chunk]])
+        for i, first in enumerate(firsts):
+            ts = pending.result()
+            pending = None
+            if i + 1 < len(firsts) and not (time_budget_s is not None and time.time() - t0 > time_budget_s):
+                nxt = firsts[i + 1]
+                pending = pool.submit(TuneSet, runtime, [q["ir"] for q in programs[nxt:nxt + chunk]])
             part = programs[first:first + chunk]
-            ts = TuneSet(runtime, [q["ir"] for q in part])
             try:
                 for k, q in enumerate(part):
                     ptrs = ptr_in[:len(q["params"])] + [ptr_out]
@@ -228,9 +238,15 @@ def collect(runtime, programs: Sequence[dict], reps: int = 3, flush_l2: bool = T
                         log.write(json.dumps(rec) + "\n")
             finally:
                 ts.close()
-            if time_budget_s is not None and time.time() - t0 > time_budget_s:
+            if pending is None:
                 break
     finally:
+        if pending is not None:
+            try:
+                pending.result().close()
+            except Exception:
+                pass
+        pool.shutdown()
         for b in bufs:
             b.release()
         out.release()

@@ -4,7 +4,7 @@ tuning workloads on the GPU this runs on (a GB300 for the committed file).
     python tests/golden/make_tuning_fixture.py [count] [seed]
 
 Each line: the program's IR text, its inputs' shapes, its kind, its points, and
-the median time in ms of each of the 48 launch configurations (L2 flushed
+the median time in ms of 5 launches of each of the 48 configurations (L2 flushed
 before every timed launch), rounded to four significant digits."""
 
 import json
@@ -24,7 +24,7 @@ def main():
     seed = int(sys.argv[2]) if len(sys.argv) > 2 else 7
     rt = NativeRuntime(0)
     progs = tuner.random_programs(count, seed=seed)
-    recs = tuner.collect(rt, progs, reps=3, flush_l2=True)
+    recs = tuner.collect(rt, progs, reps=5, flush_l2=True)
     with open(os.path.join(HERE, "tuning_gb300.jsonl"), "w") as f:
         for r in recs:
             r = dict(r)
