@@ -345,6 +345,53 @@ def time_e2e(d, st, steps):
     return dt, h2d, d2h
 
 
+def time_e2e_batch(d, b, progs, nbytes, steps):
+    """The batch through the C ABI with host buffers: every input uploaded from
+    pinned memory, one persistent launch, every output downloaded, per step."""
+    import ctypes
+    import numpy as np
+    from compute._native import call
+    rt = d.runtime
+    bufs = []
+    for _, inputs in progs:
+        for t in inputs:
+            bufs.append(t._cached)
+    hosts = []
+    h2d = 0
+    for buf in bufs:
+        ptr = ctypes.c_void_p()
+        call("cc_host_alloc", ctypes.c_size_t(buf.nbytes), ctypes.byref(ptr))
+        ctypes.memmove(ptr, rt.download(buf, buf.nbytes // 4).ctypes.data, buf.nbytes)
+        hosts.append(ptr)
+        h2d += buf.nbytes
+    outs = []
+    d2h = 0
+    for out in b.outputs:
+        ptr = ctypes.c_void_p()
+        call("cc_host_alloc", ctypes.c_size_t(out.nbytes), ctypes.byref(ptr))
+        outs.append(ptr)
+        d2h += out.nbytes
+
+    def step():
+        for ptr, buf in zip(hosts, bufs):
+            call("cc_buf_upload", ctypes.c_uint64(buf.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(buf.nbytes))
+        b.run(0)
+        for ptr, out in zip(outs, b.outputs):
+            call("cc_buf_download", ctypes.c_uint64(out.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(out.nbytes))
+
+    try:
+        step()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            step()
+        dt = (time.perf_counter() - t0) / steps
+    finally:
+        for ptr in hosts + outs:
+            call("cc_host_free", ptr)
+    return {"value": nbytes / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_step": dt * 1e3}
+
+
 def cpu_reference(workload, budget_s=15.0, threads=None):
     """Times the reference's CPU implementation (the oracle's C restatement of the
     generated OpenCL C, OpenMP over all host threads) on a bounded sample."""
@@ -361,7 +408,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s", "c4", "c5"])
-    ap.add_argument("--programs", type=int, default=2048, help="c5: tuning workloads to time (the last 10%% held out)")
+    ap.add_argument("--programs", type=int, default=2048,
+                    help="c4: programs in the batch; c5: tuning workloads to time (the last 10%% held out)")
+    ap.add_argument("--max-len", type=int, default=4194304, help="c4: longest program (lengths log-uniform from 1024)")
     ap.add_argument("--db", default=None, help="c5: append the timing records (JSON lines) to this file")
     ap.add_argument("--collect-budget-s", type=float, default=None, help="c5: stop collecting after this long")
     ap.add_argument("--db-in", default=None, help="c5: train and evaluate on these timing records instead of timing")
@@ -539,7 +588,7 @@ def main_batch(args, warmup, rank, world, local_rank):
     rt = d.runtime
     T = d.Tensor
     t0 = time.time()
-    progs = c4_programs(T, seed=0)
+    progs = c4_programs(T, seed=0, count=args.programs, hi=args.max_len)
     tensors = [t for t, _ in progs]
     b = Batch(d, tensors).bind()
     setup_s = time.time() - t0
@@ -580,12 +629,24 @@ def main_batch(args, warmup, rank, world, local_rank):
     ms_each = timed(Batch.PER_PROGRAM, k2)
     ms_graph = timed(Batch.GRAPH, k2)
     gbs = nbytes / (ms_persistent * 1e-3) / 1e9
+    e2e = None
+    if not args.no_e2e:
+        e2e = time_e2e_batch(d, b, progs, nbytes, steps=3)
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            from oracle import cref
+            r = cref.time_programs(lambda T_: c4_programs(T_, seed=0, count=48, hi=args.max_len), budget_s=12.0)
+            cpu = {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port", "sample": r["sample"]}
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": "GB/s", "cores": None, "kind": "port", "sample": "failed: %s" % e}
     peak, peak_kind = _peaks()
     line = {"metric": "fused-op GB/s", "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms_persistent, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
-            "config": {"workload": "batched uneven programs: 2048 random fused programs (3-12 nodes over "
-                                   "+,-,*,/,exp,log,tanh,max; 1-4 inputs U[0.1,2]), lengths log-uniform [1K,4M]",
+            "config": {"workload": "batched uneven programs: %d random fused programs (3-12 nodes over "
+                                   "+,-,*,/,exp,log,tanh,max; 1-4 inputs U[0.1,2]), lengths log-uniform [1K,%d]"
+                                   % (args.programs, args.max_len),
                        "programs": n_progs, "distinct_structures": n_structs, "bytes_per_step": nbytes,
                        "persistent_registers": regs, "persistent_blocks_per_sm": resident,
                        "l2": "inputs %.1f GB > L2" % (nbytes / 1e9), "setup_s": round(setup_s, 1),
@@ -594,7 +655,7 @@ def main_batch(args, warmup, rank, world, local_rank):
                          "traffic": _traffic("c4"), "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes},
             "batch": {"persistent_ms": ms_persistent, "per_program_ms": ms_each, "graph_ms": ms_graph,
                       "speedup_vs_per_program": ms_each / ms_persistent, "speedup_vs_graph": ms_graph / ms_persistent},
-            "cpu_baseline": None, "e2e": None, "gpu_launches": args.steps, "clocks": clocks}
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clocks}
     print(json.dumps(line), flush=True)
     b.close()
 

@@ -318,7 +318,8 @@ class Mlp:
 
 
 class CostModel:
-    """Predicts log(ms) of (program, configuration) from its features."""
+    """Predicts the log-runtime of (program, configuration) from its features
+    (relative to the program's other configurations when trained so)."""
 
     def __init__(self, runtime, seed: int = 0):
         self.rt = runtime
@@ -414,12 +415,22 @@ class CostModel:
 
 # ---------------------------------------------------------------- evaluation
 
-def training_arrays(records: Sequence[dict], sm_count: int):
-    """Features and log(ms) of every (program, configuration) that ran."""
+def training_arrays(records: Sequence[dict], sm_count: int, relative: bool = True):
+    """Features and targets of every (program, configuration) that ran.
+
+    The target is log(ms); with ``relative`` it is taken relative to the mean
+    log(ms) of the program's configurations, so the network spends its capacity
+    on how the configurations of one program differ (all a choice needs)
+    rather than on each program's overall scale."""
     x = feature_matrix([r["ir"] for r in records], sm_count)
-    ms = np.array([r["ms"] for r in records], dtype=np.float64).reshape(-1)
+    ms = np.array([r["ms"] for r in records], dtype=np.float64)
     ok = ms > 0
-    return x[ok], np.log(ms[ok]).astype(np.float32)
+    lg = np.log(np.where(ok, ms, 1.0))
+    if relative:
+        mean = (lg * ok).sum(axis=1, keepdims=True) / np.maximum(ok.sum(axis=1, keepdims=True), 1)
+        lg = lg - mean
+    ok = ok.reshape(-1)
+    return x[ok], lg.reshape(-1)[ok].astype(np.float32)
 
 
 def regret(records: Sequence[dict], picks: Sequence[int]) -> np.ndarray:

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <set>
 #include <sstream>
 #include <initializer_list>
 #include <utility>
@@ -324,6 +325,13 @@ class Generator {
         std::string ok = index_rows(node, p.dims, f, idx);
         std::string off = offset_expr(p.dims, idx);
         std::string ptr = "in" + std::to_string(p.param_index) + (p.dims.empty() ? "" : " + " + off);
+        // A load whose address depends on no output coordinate reads the same
+        // word in every thread (an L1 hit after the first): it is emitted where
+        // it is used, so the lookahead window holds only loads that go to DRAM.
+        bool uniform = true;
+        for (const std::string &i : idx)
+          if (!uniform_.count(i)) uniform = false;
+        const Cat load_cat = uniform ? Cat::Compute : Cat::Load;
         if (prefetch_min_bytes_ >= 0) {
           int64_t bytes = 4;
           for (int64_t d : p.dims) bytes *= d;
@@ -333,12 +341,12 @@ class Generator {
         if (asm_loads_) {
           // A predicated non-coherent load in volatile inline PTX: the compiler
           // keeps these in the order emit() places them, so the lookahead holds.
-          add(Cat::Load, "float " + v + " = " + lit_code(p.bits) + "; cc_ld(" + v + ", " + ptr + ", " +
-                             (ok.empty() ? std::string("1") : "(" + ok + ")") + ");");
+          add(load_cat, "float " + v + " = " + lit_code(p.bits) + "; cc_ld(" + v + ", " + ptr + ", " +
+                            (ok.empty() ? std::string("1") : "(" + ok + ")") + ");");
         } else if (ok.empty()) {
-          add(Cat::Load, "const float " + v + " = __ldg(" + ptr + ");");
+          add(load_cat, "const float " + v + " = __ldg(" + ptr + ");");
         } else {
-          add(Cat::Load, "const float " + v + " = (" + ok + ") ? __ldg(" + ptr + ") : " + lit_code(p.bits) + ";");
+          add(load_cat, "const float " + v + " = (" + ok + ") ? __ldg(" + ptr + ") : " + lit_code(p.bits) + ";");
         }
         break;
       }
@@ -432,6 +440,10 @@ class Generator {
         any = true;
       }
       std::string name = "_i" + std::to_string(next_var_++);
+      bool row_uniform = true;
+      for (int x = 0; x < cols - 1; ++x)
+        if (node.m[(size_t)y * cols + x] != 0.0 && !uniform_.count(f.gid[x])) row_uniform = false;
+      if (row_uniform) uniform_.insert(name);
       if (!any) {
         add(Cat::Index, "const int " + name + " = 0;");
         if (dims[y] == 0) ok += std::string(ok.empty() ? "" : " && ") + "false";
@@ -474,6 +486,7 @@ class Generator {
   int next_frame_ = 1;
   std::map<std::pair<int, int>, std::string> memo_;
   std::vector<Stmt> stmts_;
+  std::set<std::string> uniform_;  // index variables that depend on no output coordinate
 };
 
 bool is_contiguous_identity(const IrNode &x, const IrNode &p, const std::vector<int64_t> &out_shape) {

@@ -257,6 +257,37 @@ def time_workload(workload: str, budget_s: float = 15.0, threads=None):
     raise ValueError(workload)
 
 
+def time_programs(make_programs, budget_s: float = 15.0, threads=None, max_programs: int = 64):
+    """GB/s of the reference's CPU path over a sample of independent programs:
+    ``make_programs(T)`` returns (tensor, inputs) pairs built with the given
+    Tensor companion; each program is its own kernel, as in the reference
+    (Tensors.scala:1331-1381).  The first ``max_programs`` are compiled and
+    warmed up, then evaluated in turn until the budget is spent."""
+    root = os.path.dirname(HERE)
+    sys.path.insert(0, os.path.join(root, "compute.scala_gb300"))
+    from compute import Tensors, trees
+    threads = threads or _threads()
+    d = Tensors(runtime=CRuntime(threads), planner=trees.Planner(enabled=False))
+    progs = make_programs(d.Tensor)[:max_programs]
+    nbytes = 0
+    for t, inputs in progs:
+        t.flatArray()  # compile and warm up
+        nbytes += 4 * int(np.prod(t.shape)) * (len(inputs) + 1)
+    t0 = time.perf_counter()
+    rounds = 0
+    while True:
+        for t, _ in progs:
+            t.flatArray()
+        rounds += 1
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 2 or rounds >= 20:
+            break
+    per = dt / rounds
+    return {"gbs": nbytes / per / 1e9, "ms_per_round": per * 1e3, "threads": threads,
+            "sample": "the first %d programs (%.0f MB per round), %d rounds; one reference kernel per program"
+                      % (len(progs), nbytes / 1e6, rounds)}
+
+
 FOLD_GEMM_C = r"""
 /* The reference's matmul semantics (TensorsSpec.scala:468-485): each output is
  * the left fold over k of separately rounded float products, in k order.
