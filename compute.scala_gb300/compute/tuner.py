@@ -26,6 +26,7 @@ from __future__ import annotations
 import ctypes
 import json
 import math
+import os
 import time
 from typing import Dict, List, Optional, Sequence
 
@@ -41,6 +42,8 @@ MODEL_DIMS = (64, 256, 256, 256, 1)
 # a grid covering the domain (the reference's ND-range with a typical local size).
 DEFAULT_CONFIG = 26
 MAX_POINTS = 64 * 1024 * 1024
+# The cost model trained on GB300 timings of 18,000 tuning workloads (seed 0).
+DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "costmodel_gb300.npz")
 
 
 def config(index: int) -> Dict[str, int]:
@@ -475,3 +478,15 @@ def evaluate(model: CostModel, records: Sequence[dict], sm_count: int, fixed: Op
         out["best_fixed"] = summary([fixed] * len(records))
         out["best_fixed"]["config"] = fixed
     return out
+
+
+def use_learned_tuner(runtime, path: str = DEFAULT_MODEL) -> CostModel:
+    """Loads a cost model (by default the one shipped with the library),
+    installs it, and turns the learned tuner on: programs obtained from now on
+    compile in their tunable form and launch in the configuration the model
+    ranks fastest.  Keep the returned model alive while the tuner uses it."""
+    model = CostModel(runtime)
+    model.load(path)
+    model.install()
+    runtime.config_set("tuner", 2)
+    return model

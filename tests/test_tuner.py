@@ -115,3 +115,13 @@ def test_tuning_fixture_is_well_formed():
     for r in recs:
         assert len(r["ms"]) == 48
         assert any(v > 0 for v in r["ms"])
+
+
+def test_shipped_cost_model_file():
+    if not os.path.exists(tuner.DEFAULT_MODEL):
+        pytest.skip("no shipped cost model")
+    z = np.load(tuner.DEFAULT_MODEL)
+    assert tuple(int(v) for v in z["dims"]) == tuner.MODEL_DIMS
+    n = sum(k * m + m for k, m in zip(tuner.MODEL_DIMS[:-1], tuner.MODEL_DIMS[1:]))
+    assert z["params"].shape == (n,) and np.all(np.isfinite(z["params"]))
+    assert z["mean"].shape == (64,) and z["inv_std"].shape == (64,)

@@ -185,3 +185,33 @@ def test_runtime_tuner_modes(cuda_device):
     finally:
         rt.config_set("tuner", 0)
         model.close()
+
+
+def test_shipped_model_drives_the_learned_tuner(cuda_device):
+    if not os.path.exists(tuner.DEFAULT_MODEL):
+        pytest.skip("no shipped cost model")
+    rt = cuda_device.runtime
+    model = tuner.use_learned_tuner(rt)
+    try:
+        progs = tuner.random_programs(3, seed=17, max_points=1 << 20)
+        for k, p in enumerate(progs):
+            _, bufs = _inputs(rt, p, k)
+            n_out = 1 if p["kind"] == "sum" else p["points"]
+            out = rt.alloc(max(1, n_out) * 4)
+            prog = rt.program(p["ir"])
+            rt.launch(prog, bufs, out)
+            assert 0 <= rt.tuner_choice(prog) < 48
+            rt.config_set("tuner", 0)
+            ref = rt.alloc(max(1, n_out) * 4)
+            rt.launch(rt.program(p["ir"]), bufs, ref)
+            got, want = rt.download(out, n_out), rt.download(ref, n_out)
+            if p["kind"] == "sum":
+                assert np.allclose(got, want, rtol=1e-5, equal_nan=True)
+            else:
+                assert _same(got, want)
+            rt.config_set("tuner", 2)
+            for b in bufs + [out, ref]:
+                b.release()
+    finally:
+        rt.config_set("tuner", 0)
+        model.close()
