@@ -217,13 +217,15 @@ class NativeRuntime:
         call("cc_event_release", c_handle(ev))
 
 
-def codegen(ir_text: str) -> str:
-    """The CUDA C the runtime generates for an IR text (no GPU needed)."""
+def codegen(ir_text: str, options: str = None) -> str:
+    """The CUDA C the runtime generates for an IR text (no GPU needed); options
+    as "key=value" words (block, lookahead, ring, unroll, min_blocks, asm)."""
     raw = ir_text.encode()
+    opts = options.encode() if options else None
     need = ctypes.c_size_t()
-    call("cc_codegen", raw, ctypes.c_size_t(len(raw)), None, 0, ctypes.byref(need))
+    call("cc_codegen_with", raw, ctypes.c_size_t(len(raw)), opts, None, 0, ctypes.byref(need))
     buf = ctypes.create_string_buffer(need.value)
-    call("cc_codegen", raw, ctypes.c_size_t(len(raw)), buf, need.value, ctypes.byref(need))
+    call("cc_codegen_with", raw, ctypes.c_size_t(len(raw)), opts, buf, need.value, ctypes.byref(need))
     return buf.value.decode()
 
 
@@ -237,7 +239,8 @@ def batch_compile_check(texts, cc=(10, 3)):
     return k.value, secs.value
 
 
-def compile_check(ir_text: str, cc=(10, 3), flags: int = 0) -> None:
+def compile_check(ir_text: str, cc=(10, 3), flags: int = 0, options: str = None) -> None:
     """NVRTC-compiles the generated CUDA C for sm_<cc>a (no GPU needed); raises BuildProgramFailure."""
     raw = ir_text.encode()
-    call("cc_compile_check", raw, ctypes.c_size_t(len(raw)), int(cc[0]), int(cc[1]), ctypes.c_uint32(flags))
+    call("cc_compile_check_with", raw, ctypes.c_size_t(len(raw)), int(cc[0]), int(cc[1]), ctypes.c_uint32(flags),
+         options.encode() if options else None)

@@ -261,6 +261,11 @@ enum class Cat : uint8_t { Index, Prefetch, Load, Compute };
 struct Stmt {
   Cat cat;
   std::string text;
+  // A load staged through the shared-memory ring: its order among ring loads,
+  // the variable it defines, its address, its bounds condition ("" = none)
+  // and the input it reads (an in-bounds address when the condition fails).
+  int ring = -1;
+  std::string var, ptr, ok, base;
 };
 
 class Generator {
@@ -332,6 +337,17 @@ class Generator {
         for (const std::string &i : idx)
           if (!uniform_.count(i)) uniform = false;
         const Cat load_cat = uniform ? Cat::Compute : Cat::Load;
+        if (ring_ > 0 && !uniform && asm_loads_ && (ok.empty() || p.bits == 0)) {
+          // zero padding is the copy's zero fill
+          Stmt st{Cat::Load, std::string()};
+          st.ring = ring_loads_++;
+          st.var = v;
+          st.ptr = ptr;
+          st.ok = ok;
+          st.base = "in" + std::to_string(p.param_index);
+          stmts_.push_back(std::move(st));
+          break;
+        }
         if (prefetch_min_bytes_ >= 0) {
           int64_t bytes = 4;
           for (int64_t d : p.dims) bytes *= d;
@@ -391,17 +407,39 @@ class Generator {
     }
     for (size_t i = 0; i < stmts_.size(); ++i)
       if (stmts_[i].cat == Cat::Prefetch) os << pad << stmts_[i].text << "\n";
+    // Ring loads: issued (cp.async into slot r % ring_) where a register load
+    // would be issued, read back where it would be consumed after waiting for
+    // its copy group.  At most `lookahead` loads are in flight, so with
+    // lookahead <= ring_ a slot is read before it is reused.
+    if (ring_ > 0 && lookahead > ring_) lookahead = ring_;
     size_t emitted = 0, seen = 0;
+    int ring_issued = 0;
+    auto slot = [&](int r) { return "cc_ring[" + std::to_string(r % ring_) + " * blockDim.x + threadIdx.x]"; };
     auto emit_loads_to = [&](size_t n) {
       if (n > loads.size()) n = loads.size();
-      while (emitted < n) os << pad << stmts_[loads[emitted++]].text << "\n";
+      while (emitted < n) {
+        const Stmt &l = stmts_[loads[emitted++]];
+        if (l.ring < 0) {
+          os << pad << l.text << "\n";
+          continue;
+        }
+        const std::string src = l.ok.empty() ? l.ptr : "(" + l.ok + ") ? " + l.ptr + " : " + l.base;
+        os << pad << "cc_cp4(&" << slot(l.ring) << ", " << src << ", " << (l.ok.empty() ? "1" : "(" + l.ok + ")")
+           << ");\n";
+        ++ring_issued;
+      }
     };
     for (size_t i = 0; i < stmts_.size(); ++i) {
       const Stmt &s = stmts_[i];
       if (s.cat == Cat::Index || s.cat == Cat::Prefetch) continue;
       if (s.cat == Cat::Load) {
         ++seen;
-        emit_loads_to(seen);
+        // a ring load waits here, so first fill the window (one short of the
+        // ring: this load's slot is still unread)
+        emit_loads_to(s.ring >= 0 && lookahead > 1 ? seen - 1 + (size_t)lookahead : seen);
+        if (s.ring >= 0)
+          os << pad << "cc_cp_wait<" << (ring_issued - s.ring - 1) << ">();\n"
+             << pad << "const float " << s.var << " = " << slot(s.ring) << ";\n";
         continue;
       }
       emit_loads_to(seen + (size_t)(lookahead > 0 ? lookahead : 0));
@@ -409,6 +447,11 @@ class Generator {
     }
     emit_loads_to(loads.size());
   }
+
+  // Stage zero-padded loads that vary per thread through a shared-memory ring
+  // of `slots` entries per thread (0: registers only).
+  void set_ring(int slots) { ring_ = slots; }
+  int ring_loads() const { return ring_loads_; }
 
   bool uses_fp64() const { return fp64_; }
 
@@ -487,6 +530,8 @@ class Generator {
   std::map<std::pair<int, int>, std::string> memo_;
   std::vector<Stmt> stmts_;
   std::set<std::string> uniform_;  // index variables that depend on no output coordinate
+  int ring_ = 0;
+  int ring_loads_ = 0;
 };
 
 bool is_contiguous_identity(const IrNode &x, const IrNode &p, const std::vector<int64_t> &out_shape) {
@@ -740,18 +785,23 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   // Generic per-point body (frame 0 at coordinates decoded from `lin`).
   std::ostringstream generic;
   std::vector<std::string> results;
+  int ring_slots = 0;
   {
     Generator gen(ir, false, opt.asm_loads, opt.prefetch_min_bytes);
+    gen.set_ring(contiguous ? 0 : opt.smem_ring);  // contiguous programs use the float4 kernels
     decode(generic, 4);
     if (root.kind == NodeKind::Tuple) {
       for (int e : root.elems) results.push_back(gen.gen(e, f0));
     } else {
       results.push_back(gen.gen(ir.root, f0));
     }
-    gen.emit(generic, 4, opt.load_lookahead);
+    gen.emit(generic, 4, opt.smem_ring > 0 ? std::min(opt.load_lookahead, opt.smem_ring) : opt.load_lookahead);
     fp64 |= gen.uses_fp64();
+    if (gen.ring_loads() > 0) ring_slots = opt.smem_ring;
   }
   g.uses_fp64_index = fp64;
+  g.smem_bytes = ring_slots * opt.block * 4;
+  const std::string ring_decl = ring_slots > 0 ? "  extern __shared__ float cc_ring[];\n" : "";
 
   std::string call_args;
   auto contig_call = [&](const std::string &lane) {
@@ -838,7 +888,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
   } else if (ir.kind == ProgramKind::Elementwise) {
     src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_ew(" << params
-        << "float *__restrict__ out, cc_i64 n) {\n"
+        << "float *__restrict__ out, cc_i64 n) {\n" << ring_decl
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << generic.str();
@@ -857,7 +907,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   } else {
     src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_sum(" << params
         << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
-        << "  float s_ = 0.0f, c_ = 0.0f;\n"
+        << ring_decl << "  float s_ = 0.0f, c_ = 0.0f;\n"
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << generic.str() << "    cc_acc(s_, c_, " << results[0] << ");\n  }\n"

@@ -87,6 +87,24 @@ __device__ __forceinline__ void cc_ld(float &v, const float *p, int ok) {
       : "l"(p), "r"(ok));
 }
 
+// Asynchronous 4-byte copy from global memory into a shared-memory slot
+// (cp.async): the load holds no register while it is in flight, so a thread
+// can have as many loads outstanding as its slots allow.  Each copy is its own
+// commit group.  ok = 0 copies no byte and the slot reads +0.0f (zero fill);
+// the caller then passes an address inside the buffer.
+__device__ __forceinline__ void cc_cp4(float *slot, const float *p, int ok) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(slot);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n cp.async.commit_group;\n" ::"r"(s), "l"(p),
+               "r"(ok ? 4 : 0)
+               : "memory");
+}
+
+// Waits until at most N of this thread's most recent copy groups are pending.
+template <int N>
+__device__ __forceinline__ void cc_cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // L2 prefetch of the line holding *p, skipped when `ok` is false (so no
 // address outside a buffer is ever touched).  It needs no register, so a
 // thread can have all of its future loads' lines requested at once.

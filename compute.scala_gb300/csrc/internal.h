@@ -87,6 +87,7 @@ struct CodegenOptions {
   int min_blocks = 0;       // __launch_bounds__ minimum blocks per SM of the generic kernels (0: none)
   int vec_unroll = 4;       // float4 positions per thread per batch in the contiguous kernels
   int64_t prefetch_min_bytes = -1;  // L2-prefetch loads from inputs at least this large (-1: never)
+  int smem_ring = 0;        // generic kernels: shared-memory ring slots per thread for staged loads (0: none)
 };
 
 // Minimum resident blocks per SM to request for a generic kernel over `domain`
@@ -105,6 +106,7 @@ struct Generated {
   int64_t domain = 0;      // points evaluated
   bool uses_fp64_index = false;
   int vec_unroll = 1;      // positions per thread per batch of the float4 variant
+  int smem_bytes = 0;      // dynamic shared memory of the generic kernel (its load ring)
 };
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);

@@ -190,6 +190,7 @@ struct Module {
   int resident_scalar = 0;      // blocks one SM holds at once, per variant
   int resident_vec4 = 0;
   int vec_unroll = 1;
+  int smem_bytes = 0;           // dynamic shared memory of the scalar kernel (its load ring)
   std::string source;
   ~Module() {
     if (module && g_drv.ModuleUnload) g_drv.ModuleUnload(module);
@@ -317,6 +318,7 @@ struct Context {
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
   int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
+  int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
 
@@ -518,7 +520,8 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   }
   args.push_back(&out_ptr);
   args.push_back(&nn);
-  check_cu(g_drv.LaunchKernel(f, grid, 1, 1, block, 1, 1, 0, (CUstream)stream, args.data(), nullptr),
+  check_cu(g_drv.LaunchKernel(f, grid, 1, 1, block, 1, 1, vec ? 0 : (unsigned)m.smem_bytes, (CUstream)stream,
+                              args.data(), nullptr),
            "cuLaunchKernel");
 }
 
@@ -701,6 +704,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "sum_block") {
     if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
     c.sum_block = (int)value;
+  } else if (k == "ew_smem_ring") {
+    if (value != 0 && (value < 4 || value > 64)) fail(CC_ERR_INVALID_VALUE, "ew_smem_ring must be 0 or in [4, 64]");
+    c.ew_smem_ring = (int)value;
   } else if (k == "tuner") {
     if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "tuner must be 0 (off), 1 (exhaustive) or 2 (learned)");
     c.tuner = (int)value;
@@ -747,6 +753,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "contraction") *value = c.contraction;
   else if (k == "batch_inline") *value = c.batch_inline;
   else if (k == "tuner") *value = c.tuner;
+  else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
   else if (k == "batch_max_registers") *value = c.batch_max_registers;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END
@@ -906,10 +913,12 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     opt.block = c.block;
     opt.vec_unroll = c.vec_unroll;
     opt.prefetch_min_bytes = c.prefetch_min_bytes;
+    opt.smem_ring = c.ew_smem_ring;
   }
   key += "#lookahead " + std::to_string(opt.load_lookahead) + " asm " + std::to_string((int)opt.asm_loads) +
          " blocks " + std::to_string(-opt.min_blocks) + " block " + std::to_string(opt.block) + " unroll " + std::to_string(opt.vec_unroll) +
-         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " sumblock " + std::to_string(c.sum_block) +
+         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " ring " + std::to_string(opt.smem_ring) +
+         " sumblock " + std::to_string(c.sum_block) +
          " contraction " + std::to_string(c.contraction) + " tc " + std::to_string(c.tc_variant) + " tuner " +
          std::to_string(c.tuner) + "\n";
   {
@@ -1013,7 +1022,11 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     if (p->gen.has_vec4) check_cu(g_drv.ModuleGetFunction(&mod->vec4, mod->module, vname), "cuModuleGetFunction");
     mod->block = opt.block;
     mod->vec_unroll = p->gen.vec_unroll;
-    check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_scalar, mod->scalar, mod->block, 0),
+    mod->smem_bytes = p->gen.smem_bytes;
+    if (mod->smem_bytes > 48 * 1024)
+      check_cu(g_drv.FuncSetAttribute(mod->scalar, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, mod->smem_bytes),
+               "cuFuncSetAttribute");
+    check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_scalar, mod->scalar, mod->block, mod->smem_bytes),
              "cuOccupancyMaxActiveBlocks");
     if (mod->vec4)
       check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_vec4, mod->vec4, mod->block, 0),
@@ -1033,11 +1046,39 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   CC_API_END
 }
 
+namespace {
+// "block=128 lookahead=8 ring=32 unroll=4 min_blocks=11 asm=1" (any subset; NULL = defaults).
+CodegenOptions parse_codegen_options(const char *text) {
+  CodegenOptions o;
+  if (!text) return o;
+  std::istringstream in(text);
+  std::string item;
+  while (in >> item) {
+    size_t eq = item.find('=');
+    if (eq == std::string::npos) fail(CC_ERR_INVALID_VALUE, "option '" + item + "' is not key=value");
+    std::string k = item.substr(0, eq);
+    long long v = std::strtoll(item.c_str() + eq + 1, nullptr, 10);
+    if (k == "block") o.block = (int)v;
+    else if (k == "lookahead") o.load_lookahead = (int)v;
+    else if (k == "ring") o.smem_ring = (int)v;
+    else if (k == "unroll") o.vec_unroll = (int)v;
+    else if (k == "min_blocks") o.min_blocks = (int)v;
+    else if (k == "asm") o.asm_loads = v != 0;
+    else fail(CC_ERR_INVALID_VALUE, "unknown code-generation option '" + k + "'");
+  }
+  return o;
+}
+}  // namespace
+
 int cc_codegen(const char *ir_text, size_t ir_len, char *buf, size_t len, size_t *needed) {
+  return cc_codegen_with(ir_text, ir_len, nullptr, buf, len, needed);
+}
+
+int cc_codegen_with(const char *ir_text, size_t ir_len, const char *options, char *buf, size_t len, size_t *needed) {
   CC_API_BEGIN
   if (!ir_text) fail(CC_ERR_INVALID_VALUE, "null pointer");
   Ir ir = parse_ir(ir_text, ir_len);
-  Generated gen = generate_cuda(ir, CodegenOptions{});
+  Generated gen = generate_cuda(ir, parse_codegen_options(options));
   Contraction con;
   if (match_contraction(ir, &con))
     gen.source = "// contraction m=" + std::to_string(con.m) + " n=" + std::to_string(con.n) + " k=" +
@@ -1053,10 +1094,15 @@ int cc_codegen(const char *ir_text, size_t ir_len, char *buf, size_t len, size_t
 }
 
 int cc_compile_check(const char *ir_text, size_t ir_len, int cc_major, int cc_minor, uint32_t flags) {
+  return cc_compile_check_with(ir_text, ir_len, cc_major, cc_minor, flags, nullptr);
+}
+
+int cc_compile_check_with(const char *ir_text, size_t ir_len, int cc_major, int cc_minor, uint32_t flags,
+                          const char *options) {
   CC_API_BEGIN
   if (!ir_text) fail(CC_ERR_INVALID_VALUE, "null pointer");
   Ir ir = parse_ir(ir_text, ir_len);
-  Generated gen = generate_cuda(ir, CodegenOptions{});
+  Generated gen = generate_cuda(ir, parse_codegen_options(options));
   compile_cubin(gen.source, cc_major, cc_minor, flags);
   CC_API_END
 }

@@ -83,6 +83,8 @@ int cc_synchronize(void);
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
  *                       3 = CC_GEMM_BF16X6
+ *   "ew_smem_ring"      generic kernels: per-thread slots of a shared-memory ring through which loads
+ *                       with zero padding are staged by cp.async (0 = loads into registers; 4..64)
  *   "tuner"             0 = generated kernels with the fixed launch shape (default), 1 = exhaustive
  *                       tuner, 2 = learned tuner (see the tuner section)
  *   "batch_max_registers" batch modules: register cap per thread of every compiled part (0 = none;
@@ -138,6 +140,11 @@ int cc_program_cache_stats(uint64_t *hits, uint64_t *misses, uint64_t *entries);
  * failure carries the NVRTC log, like cc_program_get. */
 int cc_codegen(const char *ir, size_t ir_len, char *buf, size_t len, size_t *needed);
 int cc_compile_check(const char *ir, size_t ir_len, int cc_major, int cc_minor, uint32_t flags);
+/* The same with code-generation options as "key=value" words (NULL = defaults):
+ * block, lookahead, ring (shared-memory ring slots), unroll, min_blocks, asm. */
+int cc_codegen_with(const char *ir, size_t ir_len, const char *options, char *buf, size_t len, size_t *needed);
+int cc_compile_check_with(const char *ir, size_t ir_len, int cc_major, int cc_minor, uint32_t flags,
+                          const char *options);
 
 /* ---- launch: replaces Kernel.update + Kernel.enqueue + dispatch
  *      (OpenCL.scala:751-844, :1298-1329) as driven by CompiledKernel.run

@@ -137,3 +137,20 @@ def test_batch_module_compiles_for_sm103a():
         texts.append(d.serialize(e.closure, e.shape).text)
     structures, seconds = batch_compile_check(texts)
     assert structures == 4  # programs 0 and 3 share code although their lengths differ
+
+
+def test_shared_memory_ring_codegen_compiles():
+    import bench
+    from compute import Tensors, runtime
+    from compute.tensors import NonInlineTensor
+    d = Tensors(device=0)
+    n, c, h, w = 64, 128, 56, 56
+    x = NonInlineTensor(d, (n, c, h, w), 0.0, None)
+    bias = NonInlineTensor(d, (1, 1, 1, c), 0.0, None)
+    s = bench.build_c2(d.Tensor, x, bias, n, c, h, w)
+    text = d.serialize(s.closure, s.shape).text
+    src = runtime.codegen(text, "block=128 ring=32 lookahead=32 min_blocks=11")
+    assert "extern __shared__ float cc_ring[];" in src
+    assert src.count("cc_cp4(&cc_ring") == 128  # every x load staged; the bias loads (uniform) are not
+    assert "cc_cp4(&cc_ring" not in runtime.codegen(text)
+    runtime.compile_check(text, options="block=128 ring=32 lookahead=32 min_blocks=11")
