@@ -921,6 +921,12 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     }
   }
   g.source = src.str();
+  // every kernel starts by ordering itself after the kernels it depends on
+  const std::string sig_end = ", cc_i64 n) {\n";
+  for (size_t at = g.source.find(sig_end); at != std::string::npos; at = g.source.find(sig_end, at)) {
+    at += sig_end.size();
+    g.source.insert(at, "  cc_pdl_enter();\n");
+  }
   return g;
 }
 

@@ -87,6 +87,15 @@ __device__ __forceinline__ void cc_ld(float &v, const float *p, int ok) {
       : "l"(p), "r"(ok));
 }
 
+// Programmatic dependent launch: allow the next kernel in the stream to be
+// scheduled now (its blocks become resident as this grid's retire), then wait
+// until every kernel this one depends on has completed and its writes are
+// visible.  Generated kernels call this before touching global memory, so
+// stream order is kept; without the launch attribute both steps are no-ops.
+__device__ __forceinline__ void cc_pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;\n griddepcontrol.wait;\n" ::: "memory");
+}
+
 // Asynchronous 4-byte copy from global memory into a shared-memory slot
 // (cp.async): the load holds no register while it is in flight, so a thread
 // can have as many loads outstanding as its slots allow.  Each copy is its own

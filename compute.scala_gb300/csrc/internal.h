@@ -32,6 +32,7 @@ struct Driver {
   decltype(&::cuModuleGetFunction) ModuleGetFunction = nullptr;
   decltype(&::cuModuleUnload) ModuleUnload = nullptr;
   decltype(&::cuLaunchKernel) LaunchKernel = nullptr;
+  decltype(&::cuLaunchKernelEx) LaunchKernelEx = nullptr;
   decltype(&::cuGetErrorName) GetErrorName = nullptr;
   decltype(&::cuGetErrorString) GetErrorString = nullptr;
   decltype(&::cuCtxGetCurrent) CtxGetCurrent = nullptr;

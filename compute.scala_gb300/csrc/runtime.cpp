@@ -71,6 +71,7 @@ void load_driver() {
   resolve(g_drv.ModuleGetFunction, "cuModuleGetFunction");
   resolve(g_drv.ModuleUnload, "cuModuleUnload");
   resolve(g_drv.LaunchKernel, "cuLaunchKernel");
+  resolve(g_drv.LaunchKernelEx, "cuLaunchKernelEx");
   resolve(g_drv.GetErrorName, "cuGetErrorName");
   resolve(g_drv.GetErrorString, "cuGetErrorString");
   resolve(g_drv.CtxGetCurrent, "cuCtxGetCurrent");
@@ -319,6 +320,7 @@ struct Context {
   int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
+  int pdl = 0;           // launch generated kernels with programmatic dependent launch
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
 
@@ -520,8 +522,28 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   }
   args.push_back(&out_ptr);
   args.push_back(&nn);
-  check_cu(g_drv.LaunchKernel(f, grid, 1, 1, block, 1, 1, vec ? 0 : (unsigned)m.smem_bytes, (CUstream)stream,
-                              args.data(), nullptr),
+  const unsigned smem = vec ? 0 : (unsigned)m.smem_bytes;
+  if (c.pdl) {
+    // programmatic dependent launch: this grid may be scheduled while the
+    // previous kernel in the stream drains; its cc_pdl_enter() keeps the order
+    CUlaunchAttribute attr;
+    memset(&attr, 0, sizeof attr);
+    attr.id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
+    attr.value.programmaticStreamSerializationAllowed = 1;
+    CUlaunchConfig cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.gridDimX = grid;
+    cfg.gridDimY = cfg.gridDimZ = 1;
+    cfg.blockDimX = (unsigned)block;
+    cfg.blockDimY = cfg.blockDimZ = 1;
+    cfg.sharedMemBytes = smem;
+    cfg.hStream = (CUstream)stream;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    check_cu(g_drv.LaunchKernelEx(&cfg, f, args.data(), nullptr), "cuLaunchKernelEx");
+    return;
+  }
+  check_cu(g_drv.LaunchKernel(f, grid, 1, 1, block, 1, 1, smem, (CUstream)stream, args.data(), nullptr),
            "cuLaunchKernel");
 }
 
@@ -704,6 +726,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "sum_block") {
     if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
     c.sum_block = (int)value;
+  } else if (k == "pdl") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "pdl must be 0 or 1");
+    c.pdl = (int)value;
   } else if (k == "ew_smem_ring") {
     if (value != 0 && (value < 4 || value > 64)) fail(CC_ERR_INVALID_VALUE, "ew_smem_ring must be 0 or in [4, 64]");
     c.ew_smem_ring = (int)value;
@@ -754,6 +779,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "batch_inline") *value = c.batch_inline;
   else if (k == "tuner") *value = c.tuner;
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
+  else if (k == "pdl") *value = c.pdl;
   else if (k == "batch_max_registers") *value = c.batch_max_registers;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END

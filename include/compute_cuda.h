@@ -83,6 +83,9 @@ int cc_synchronize(void);
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
  *                       3 = CC_GEMM_BF16X6
+ *   "pdl"               1 = launch generated kernels with programmatic dependent launch: a kernel is
+ *                       scheduled while the previous one drains and waits (griddepcontrol.wait)
+ *                       before its first memory access, so results and ordering are unchanged
  *   "ew_smem_ring"      generic kernels: per-thread slots of a shared-memory ring through which loads
  *                       with zero padding are staged by cp.async (0 = loads into registers; 4..64)
  *   "tuner"             0 = generated kernels with the fixed launch shape (default), 1 = exhaustive
