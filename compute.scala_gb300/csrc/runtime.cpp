@@ -320,7 +320,7 @@ struct Context {
   int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
-  int pdl = 0;           // launch generated kernels with programmatic dependent launch
+  int pdl = 1;           // launch generated kernels with programmatic dependent launch
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
 
