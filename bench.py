@@ -392,6 +392,31 @@ def time_e2e_batch(d, b, progs, nbytes, steps):
             "ms_per_step": dt * 1e3}
 
 
+_KNOBS = []
+
+
+def emit(line):
+    """Prints the result line; runtime settings changed by --knob are recorded in its config."""
+    if _KNOBS and isinstance(line.get("config"), dict):
+        line["config"]["knobs"] = list(_KNOBS)
+    print(json.dumps(line), flush=True)
+
+
+def apply_knobs(rt, knobs):
+    _KNOBS[:] = list(knobs)
+    for kv in knobs:
+        k, v = kv.split("=", 1)
+        rt.config_set(k, int(v))
+
+
+def max_over_ranks(dist, value: float) -> float:
+    """The largest of every rank's value (the replicas' slowest timing)."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_reference(workload, budget_s=15.0, threads=None):
     """Times the reference's CPU implementation (the oracle's C restatement of the
     generated OpenCL C, OpenMP over all host threads) on a bounded sample."""
@@ -416,6 +441,8 @@ def main():
     ap.add_argument("--db-in", default=None, help="c5: train and evaluate on these timing records instead of timing")
     ap.add_argument("--save-model", default=None, help="c5: write the trained cost model (.npz) here")
     ap.add_argument("--epochs", type=int, default=40, help="c5: training epochs")
+    ap.add_argument("--knob", action="append", default=[], metavar="KEY=VALUE",
+                    help="runtime setting (cc_config_set) applied before the run; repeatable")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true", help="skip the clock sampling (and its untimed busy loop)")
@@ -444,7 +471,7 @@ def main():
                 "cpu_baseline": {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port",
                                  "sample": r["sample"]},
                 "e2e": {"value": r["gbs"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
+        emit(line)
         return
 
     dist = None
@@ -456,6 +483,7 @@ def main():
     from compute import Tensors
     d = Tensors(device=local_rank)
     rt = d.runtime
+    apply_knobs(rt, args.knob)
     st = setup(args.workload, d)
     sampler = ClockSampler(local_rank)
     if dist:
@@ -469,10 +497,7 @@ def main():
         keep_busy(rt, st, 1.5)
         clocks = sampler.stop()
     if dist:
-        import torch
-        t = torch.tensor([ms_total], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+        ms_total = max_over_ranks(dist, ms_total)
         dist.barrier()
     ms_step = ms_total / args.steps
     gbs_step = st["bytes"] / (ms_step * 1e-3) / 1e9
@@ -504,7 +529,7 @@ def main():
                 "config": dict(st["config"], parallelism="replicas" if world > 1 else "single GPU"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
                 "clocks": clocks, "hot_l2": hot}
-        print(json.dumps(line), flush=True)
+        emit(line)
     if dist:
         dist.destroy_process_group()
 
@@ -525,6 +550,7 @@ def main_tuner(args, warmup, rank, world, local_rank):
     from compute.runtime import NativeRuntime
     from compute import tuner
     rt = NativeRuntime(local_rank)
+    apply_knobs(rt, args.knob)
     sm = rt.device_info()["sm_count"]
     t0 = time.time()
     if args.db_in:
@@ -577,7 +603,7 @@ def main_tuner(args, warmup, rank, world, local_rank):
             "seconds": {"generate": round(gen_s, 1), "compile_and_time": round(collect_s, 1),
                         "train": round(train_s, 2), "predict_held_out": round(predict_s, 3)},
             "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": None}
-    print(json.dumps(line), flush=True)
+    emit(line)
     model.close()
 
 
@@ -589,6 +615,7 @@ def main_batch(args, warmup, rank, world, local_rank):
     from compute.batch import Batch
     d = Tensors(device=local_rank)
     rt = d.runtime
+    apply_knobs(rt, args.knob)
     T = d.Tensor
     t0 = time.time()
     progs = c4_programs(T, seed=0, count=args.programs, hi=args.max_len)
@@ -659,7 +686,7 @@ def main_batch(args, warmup, rank, world, local_rank):
             "batch": {"persistent_ms": ms_persistent, "per_program_ms": ms_each, "graph_ms": ms_graph,
                       "speedup_vs_per_program": ms_each / ms_persistent, "speedup_vs_graph": ms_graph / ms_persistent},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clocks}
-    print(json.dumps(line), flush=True)
+    emit(line)
     b.close()
 
 
@@ -679,11 +706,12 @@ def main_contraction(args, warmup, rank, world, local_rank):
                 "cpu_baseline": {"value": r["tflops"], "unit": "TFLOP/s", "cores": r["threads"], "kind": "port",
                                  "sample": r["sample"]},
                 "e2e": {"value": r["tflops"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
+        emit(line)
         return
     from compute import Tensors
     d = Tensors(device=local_rank)
     rt = d.runtime
+    apply_knobs(rt, args.knob)
     st = setup(args.workload, d)
     sampler = ClockSampler(local_rank)
     rt.synchronize()
@@ -724,7 +752,7 @@ def main_contraction(args, warmup, rank, world, local_rank):
             "vs_baseline": None, "dtype": "bf16x3 split of f32 (fp32 accumulate)", "data": "synthetic (seeded reference RNG)",
             "config": dict(st["config"], parallelism="single GPU"), "roofline": roofline, "accuracy": extras,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * 3, "clocks": clocks}
-    print(json.dumps(line), flush=True)
+    emit(line)
 
 
 if __name__ == "__main__":

@@ -716,9 +716,23 @@ std::string decode_coordinates(const std::vector<int64_t> &shape, int64_t domain
 
 }  // namespace
 
+namespace {
+std::vector<int64_t> param_bytes_of(const Ir &ir) {
+  std::vector<int64_t> out(ir.n_params, 0);
+  for (const IrNode &n : ir.nodes)
+    if (n.kind == NodeKind::Param && n.param_index >= 0 && n.param_index < ir.n_params) {
+      int64_t b = 4;
+      for (int64_t d : n.dims) b *= d;
+      out[n.param_index] = b;
+    }
+  return out;
+}
+}  // namespace
+
 Generated describe_program(const Ir &ir) {
   Generated g;
   g.n_inputs = ir.n_params;
+  g.param_bytes = param_bytes_of(ir);
   const IrNode &root = ir.nodes[ir.root];
   g.tuple_len = root.kind == NodeKind::Tuple ? (int)root.elems.size() : 1;
   int64_t domain = 1;
@@ -732,6 +746,7 @@ Generated describe_program(const Ir &ir) {
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   Generated g;
   g.n_inputs = ir.n_params;
+  g.param_bytes = param_bytes_of(ir);
   const IrNode &root = ir.nodes[ir.root];
   g.tuple_len = root.kind == NodeKind::Tuple ? (int)root.elems.size() : 1;
   int64_t domain = 1;
@@ -825,6 +840,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
       for (int i = 0; i < nin; ++i)
         o << "    const float4 v" << i << "_" << u << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q + "
           << u << " * stride);\n";
+    if (store) o << "    cc_pdl_gate(cc_early);\n";
     for (int u = 0; u < u_count; ++u) {
       auto lane_call = [&](const char *lane) {
         std::string c = "cc_point(";
@@ -843,7 +859,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     for (int i = 0; i < nin; ++i)
       o << "    const float4 v" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
     if (store) {
-      o << "    float4 r;\n";
+      o << "    cc_pdl_gate(cc_early);\n    float4 r;\n";
       for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    r" << lane << " = " << call(lane) << ";\n";
       o << "    reinterpret_cast<float4 *>(out)[q] = r;\n";
     } else {
@@ -852,7 +868,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     o << "  }\n  for (cc_i64 lin = (n4 << 2) + (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n";
     for (int i = 0; i < nin; ++i) o << "    const float v" << i << " = __ldg(in" << i << " + lin);\n";
     if (store)
-      o << "    out[lin] = " << call("") << ";\n  }\n";
+      o << "    cc_pdl_gate(cc_early);\n    out[lin] = " << call("") << ";\n  }\n";
     else
       o << "    cc_acc(s_, c_, " << call("") << ");\n  }\n";
     return o.str();
@@ -869,7 +885,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << "float *__restrict__ out, cc_i64 n) {\n"
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
-        << contig_scalar << "    out[lin] = " << contig_call("") << ";\n  }\n}\n\n"
+        << contig_scalar << "    cc_pdl_gate(cc_early);\n    out[lin] = " << contig_call("") << ";\n  }\n}\n\n"
         << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_ew_v4(" << params
         << "float *__restrict__ out, cc_i64 n) {\n"
         << vec4_loop(ir.n_params, U, true, contig_call) << "}\n\n";
@@ -880,18 +896,19 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << contig_scalar << "    cc_acc(s_, c_, " << contig_call("") << ");\n  }\n"
-        << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n"
+        << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n"
         << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum_v4(" << params
         << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
         << "  float s_ = 0.0f, c_ = 0.0f;\n"
         << vec4_loop(ir.n_params, U, false, contig_call)
-        << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+        << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
   } else if (ir.kind == ProgramKind::Elementwise) {
     src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_ew(" << params
         << "float *__restrict__ out, cc_i64 n) {\n" << ring_decl
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << generic.str();
+    src << "    cc_pdl_gate(cc_early);\n";
     if (g.tuple_len == 1) {
       src << "    out[lin] = " << results[0] << ";\n";
     } else {
@@ -911,21 +928,22 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << generic.str() << "    cc_acc(s_, c_, " << results[0] << ");\n  }\n"
-        << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+        << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
     if (contiguous) {
       src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum_v4(" << params
           << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
           << "  float s_ = 0.0f, c_ = 0.0f;\n"
           << vec4_loop(ir.n_params, U, false, contig_call)
-          << "  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+          << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
     }
   }
   g.source = src.str();
-  // every kernel starts by ordering itself after the kernels it depends on
+  // every kernel orders itself after the kernels it depends on (cc_pdl_begin / cc_pdl_gate)
   const std::string sig_end = ", cc_i64 n) {\n";
+  const std::string with_flag = ", cc_i64 n, int cc_early) {\n  cc_pdl_begin(cc_early);\n";
   for (size_t at = g.source.find(sig_end); at != std::string::npos; at = g.source.find(sig_end, at)) {
-    at += sig_end.size();
-    g.source.insert(at, "  cc_pdl_enter();\n");
+    g.source.replace(at, sig_end.size(), with_flag);
+    at += with_flag.size();
   }
   return g;
 }

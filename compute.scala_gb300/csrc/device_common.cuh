@@ -87,13 +87,29 @@ __device__ __forceinline__ void cc_ld(float &v, const float *p, int ok) {
       : "l"(p), "r"(ok));
 }
 
-// Programmatic dependent launch: allow the next kernel in the stream to be
-// scheduled now (its blocks become resident as this grid's retire), then wait
-// until every kernel this one depends on has completed and its writes are
-// visible.  Generated kernels call this before touching global memory, so
-// stream order is kept; without the launch attribute both steps are no-ops.
-__device__ __forceinline__ void cc_pdl_enter() {
-  asm volatile("griddepcontrol.launch_dependents;\n griddepcontrol.wait;\n" ::: "memory");
+// Programmatic dependent launch (griddepcontrol).  A generated kernel waits
+// until the kernels it depends on have completed and their writes are
+// visible, and only then lets the next kernel in the stream be scheduled, so a
+// dependent of this kernel never starts before this kernel's own inputs exist.
+// Without the launch attribute both steps are no-ops.
+__device__ __forceinline__ void cc_pdl_wait_then_release() {
+  asm volatile("griddepcontrol.wait;\n griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+// At entry.  early = 0: the kernel may read what the previous kernel wrote, so
+// it waits before its first load.  early = 1 (the runtime checked that no input
+// overlaps the previous kernel's output): the loads and arithmetic proceed
+// while the previous kernel drains, and cc_pdl_gate waits before the first
+// store, which keeps write-after-read and write-after-write order.
+__device__ __forceinline__ void cc_pdl_begin(int early) {
+  if (!early) cc_pdl_wait_then_release();
+}
+
+__device__ __forceinline__ void cc_pdl_gate(int &early) {
+  if (early) {
+    cc_pdl_wait_then_release();
+    early = 0;
+  }
 }
 
 // Asynchronous 4-byte copy from global memory into a shared-memory slot

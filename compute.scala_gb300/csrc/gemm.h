@@ -29,7 +29,8 @@ constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 32;
 // 2 = 128-column tiles, one pair per tile.  gemm_tc_box_n: the tile width.
 int gemm_tc_box_n(int variant);
 // maps: A planes 0..2 (box 32 x 128), B^T planes 0..2 (box 32 x gemm_tc_box_n), 64-byte swizzle.
+// group_m: output tiles are visited in groups of this many tile rows (1 = row-major).
 cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
-                               int sm_count, int *err, int variant, cudaStream_t stream);
+                               int sm_count, int *err, int variant, int group_m, cudaStream_t stream);
 
 }  // namespace cc

@@ -177,6 +177,18 @@ __device__ __forceinline__ void store_row_chunk(float *crow, int row, int M, int
   }
 }
 
+// Origin of output tile `tile` in tile units.  Tiles are numbered in groups of
+// `group_m` tile rows, columns outermost within a group, so the CTAs working at
+// the same time share a few A and B panels in L2 (group_m = 1: row-major).
+__device__ __forceinline__ void tile_origin(int tile, int tiles_m, int tiles_n, int group_m, int &tm, int &tn) {
+  const int per_group = group_m * tiles_n;
+  const int first = (tile / per_group) * group_m;
+  const int rows = tiles_m - first < group_m ? tiles_m - first : group_m;
+  const int in = tile - (tile / per_group) * per_group;
+  tm = first + in % rows;
+  tn = in / rows;
+}
+
 // The six (A plane, B plane) products, largest first.
 __device__ __constant__ int kProdA[6] = {0, 0, 1, 1, 0, 2};
 __device__ __constant__ int kProdB[6] = {0, 1, 0, 1, 2, 0};
@@ -187,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                        const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap tb0,
                        const __grid_constant__ CUtensorMap tb1, const __grid_constant__ CUtensorMap tb2,
                        float *__restrict__ C, int M, int N, long long ldc, int num_kb, int tiles_n, int num_tiles,
-                       int *err) {
+                       int group_m, int *err) {
   using Cfg = TcCfg<BN, STAGES, ACC_BUFS>;
   constexpr int kStages = STAGES;
   constexpr int kStageBytes = Cfg::kStageBytes;
@@ -242,7 +254,9 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int s = 0; s < kStages; ++s) filled[s] = false;
       for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
-        const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+        int tm, tn;
+        tile_origin(tile, num_tiles / tiles_n, tiles_n, group_m, tm, tn);
+        const int m0 = tm * BM, n0 = tn * BN;
         for (int kb = 0; kb < num_kb; ++kb) {
           if (!mbar_wait(bar_empty + 8 * stage, phase ^ 1u, abort_flag, err, 1)) {
             ok = false;
@@ -345,7 +359,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
         if (!mbar_wait(bar_accfull + 8 * acc, acc_phase, abort_flag, err, 4)) break;
         tc_fence_after();
-        const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+        int tm, tn;
+        tile_origin(tile, num_tiles / tiles_n, tiles_n, group_m, tm, tn);
+        const int m0 = tm * BM, n0 = tn * BN;
         const int row = m0 + row_in_tile;
         float *crow = C + (long long)row * ldc;
 #pragma unroll 1
@@ -398,7 +414,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
         if (!ok) break;
-        const int m0 = (tile / tiles_n) * BM, n0 = (tile % tiles_n) * BN;
+        int tm, tn;
+        tile_origin(tile, num_tiles / tiles_n, tiles_n, group_m, tm, tn);
+        const int m0 = tm * BM, n0 = tn * BN;
         const int row = m0 + row_in_tile;
         float *crow = C + (long long)row * ldc;
 #pragma unroll
@@ -417,7 +435,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 template <int BN, int STAGES, int ACC_BUFS, int KC>
 cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc, int sm_count,
-                           int *err, cudaStream_t stream) {
+                           int group_m, int *err, cudaStream_t stream) {
   using Cfg = TcCfg<BN, STAGES, ACC_BUFS>;
   static bool attr_set = false;
   if (!attr_set) {
@@ -431,7 +449,8 @@ cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int 
   const int num_kb = K_padded / BK;
   const int grid = num_tiles < sm_count ? num_tiles : sm_count;
   gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS, KC><<<grid, kThreads, Cfg::kSmemBytes, stream>>>(
-      maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], C, M, N, ldc, num_kb, tiles_n, num_tiles, err);
+      maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], C, M, N, ldc, num_kb, tiles_n, num_tiles,
+      group_m < 1 ? 1 : group_m, err);
   return cudaGetLastError();
 }
 
@@ -440,10 +459,10 @@ cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int 
 int gemm_tc_box_n(int variant) { return variant == 1 ? 256 : 128; }
 
 cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
-                               int sm_count, int *err, int variant, cudaStream_t stream) {
-  if (variant == 1) return launch_variant<256, 3, 1, 0>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
-  if (variant == 2) return launch_variant<128, 4, 2, 0>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
-  return launch_variant<128, 4, 2, 4>(maps, C, M, N, K_padded, ldc, sm_count, err, stream);
+                               int sm_count, int *err, int variant, int group_m, cudaStream_t stream) {
+  if (variant == 1) return launch_variant<256, 3, 1, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
+  if (variant == 2) return launch_variant<128, 4, 2, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
+  return launch_variant<128, 4, 2, 4>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
 }
 
 }  // namespace cc

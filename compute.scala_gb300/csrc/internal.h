@@ -108,6 +108,7 @@ struct Generated {
   bool uses_fp64_index = false;
   int vec_unroll = 1;      // positions per thread per batch of the float4 variant
   int smem_bytes = 0;      // dynamic shared memory of the generic kernel (its load ring)
+  std::vector<int64_t> param_bytes;  // bytes of each input buffer the kernel may read
 };
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);

@@ -321,6 +321,14 @@ struct Context {
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int pdl = 1;           // launch generated kernels with programmatic dependent launch
+  // The output range of the last generated kernel launched, and its stream: a
+  // kernel that reads none of it may start its loads before that kernel ends.
+  struct {
+    cudaStream_t stream = nullptr;
+    uint64_t lo = 0, hi = 0;
+    bool valid = false;
+  } last_write;
+  int tc_group_m = 1;    // tensor-core GEMM: tile rows per group of the tile order (1 = row-major)
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
 
@@ -468,7 +476,7 @@ void run_gemm(Context &c, const float *A, const float *B, float *C, int m, int n
       c.pool.release(pb, cls_b);
       throw;
     }
-    e = launch_gemm_bf16x6(maps, C, m, n, Kp, ldc, c.sm_count, c.error_flag(), c.tc_variant, s);
+    e = launch_gemm_bf16x6(maps, C, m, n, Kp, ldc, c.sm_count, c.error_flag(), c.tc_variant, c.tc_group_m, s);
   }
   if (s != c.stream && e == cudaSuccess) e = cudaStreamSynchronize(s);  // the pool is ordered on the context stream
   c.pool.release(pa, cls_a);
@@ -482,6 +490,7 @@ std::shared_ptr<TuneModule> load_tune_module(const std::vector<char> &cubin);
 void load_tune_entry(TuneEntry &e, const Ir &ir, std::shared_ptr<TuneModule> mod, const std::string &suffix);
 
 void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
+  if (p.tune || p.is_contraction) c.last_write.valid = false;
   if (p.tune) {
     launch_tuned_program(c, p, in, out, stream);
     return;
@@ -522,6 +531,22 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   }
   args.push_back(&out_ptr);
   args.push_back(&nn);
+  // early start: none of this kernel's inputs overlaps what the previous
+  // generated kernel on this stream writes (its stores still wait for it)
+  int early = 0;
+  if (c.pdl && c.last_write.valid && c.last_write.stream == stream) {
+    early = 1;
+    for (size_t i = 0; i < in.size(); ++i) {
+      const uint64_t lo = in[i];
+      const uint64_t hi = lo + (uint64_t)(i < p.gen.param_bytes.size() ? p.gen.param_bytes[i] : 0);
+      if (lo < c.last_write.hi && c.last_write.lo < hi) early = 0;
+    }
+  }
+  args.push_back(&early);
+  c.last_write.stream = stream;
+  c.last_write.lo = out;
+  c.last_write.hi = out + (uint64_t)(p.gen.out_elems > 0 ? p.gen.out_elems : 1) * sizeof(float);
+  c.last_write.valid = c.pdl != 0;
   const unsigned smem = vec ? 0 : (unsigned)m.smem_bytes;
   if (c.pdl) {
     // programmatic dependent launch: this grid may be scheduled while the
@@ -726,6 +751,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "sum_block") {
     if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
     c.sum_block = (int)value;
+  } else if (k == "tc_group_m") {
+    if (value < 1 || value > 64) fail(CC_ERR_INVALID_VALUE, "tc_group_m must be in [1, 64]");
+    c.tc_group_m = (int)value;
   } else if (k == "pdl") {
     if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "pdl must be 0 or 1");
     c.pdl = (int)value;
@@ -780,6 +808,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "tuner") *value = c.tuner;
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
   else if (k == "pdl") *value = c.pdl;
+  else if (k == "tc_group_m") *value = c.tc_group_m;
   else if (k == "batch_max_registers") *value = c.batch_max_registers;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END

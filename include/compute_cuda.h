@@ -83,6 +83,8 @@ int cc_synchronize(void);
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
  *                       3 = CC_GEMM_BF16X6
+ *   "tc_group_m"        tensor-core GEMM: output tiles visited in groups of this many tile rows, so the
+ *                       CTAs running together share A and B panels in L2 (1 = row-major; default 1)
  *   "pdl"               1 (default) = launch generated kernels with programmatic dependent launch: a kernel is
  *                       scheduled while the previous one drains and waits (griddepcontrol.wait)
  *                       before its first memory access, so results and ordering are unchanged

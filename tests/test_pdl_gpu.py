@@ -29,6 +29,52 @@ def test_pdl_chain_matches_plain_launches(cuda_device):
         try:
             got, got_s = _chain(cuda_device, n)
         finally:
-            rt.config_set("pdl", 0)
+            rt.config_set("pdl", 1)
         assert np.array_equal(got.view(np.int32), want.view(np.int32))
         assert got_s == want_s
+
+
+def test_early_start_keeps_write_after_read_and_write_after_write(cuda_device):
+    """Kernels whose inputs do not overlap the previous kernel's output start
+    early; their stores still wait, so a kernel that overwrites what the
+    previous one reads (or writes) leaves the same bits as plain launches."""
+    from compute.tensors import NonInlineTensor
+    d = cuda_device
+    rt = d.runtime
+    T = d.Tensor
+    n = 1 << 24
+    p = NonInlineTensor(d, (n,), 0.0, None)
+    f = rt.program(d.serialize((T.exp(p) * T.fill(0.5, [n])).closure, (n,)).text)     # C = exp(A) / 2
+    g = rt.program(d.serialize((p * T.fill(3.0, [n]) + T.fill(1.0, [n])).closure, (n,)).text)  # A = 3B + 1
+    h = rt.program(d.serialize(T.tanh(p).closure, (n,)).text)                          # C = tanh(B)
+    r = np.random.RandomState(0)
+    a0 = r.uniform(-1, 1, n).astype(np.float32)
+    b0 = r.uniform(-1, 1, n).astype(np.float32)
+
+    def run(pdl):
+        rt.config_set("pdl", pdl)
+        A, B, C = rt.alloc(4 * n), rt.alloc(4 * n), rt.alloc(4 * n)
+        rt.upload(A, a0)
+        rt.upload(B, b0)
+        pa, pb, pc = A.device_ptr(), B.device_ptr(), C.device_ptr()
+        outs = []
+        for _ in range(20):
+            rt.launch_ptrs(f, [pa], pc)   # reads A, writes C
+            rt.launch_ptrs(g, [pb], pa)   # early (B not written by f); overwrites A, which f reads
+            rt.launch_ptrs(f, [pa], pc)   # reads g's output: waits at entry
+            rt.launch_ptrs(h, [pb], pc)   # early; writes C, which the previous kernel writes
+            rt.launch_ptrs(g, [pc], pb)   # reads h's output: waits at entry; overwrites B, which h reads
+        outs = [rt.download(buf, n) for buf in (A, B, C)]
+        for buf in (A, B, C):
+            buf.release()
+        return outs
+
+    try:
+        want = run(0)
+        got = run(1)
+    finally:
+        rt.config_set("pdl", 1)
+    for w, g_ in zip(want, got):
+        nan = np.isnan(w)
+        assert np.array_equal(nan, np.isnan(g_))
+        assert np.array_equal(w[~nan].view(np.int32), g_[~nan].view(np.int32))
