@@ -293,6 +293,24 @@ def time_device(rt, st, steps, warmup):
     return ms
 
 
+def time_isolated(rt, st, reps):
+    """Median device time of single launches, each alone between two synchronisations."""
+    prog, sets, out = st["prog"], st["sets"], st["out"]
+    ptr_sets = [[b.device_ptr() for b in s] for s in sets]
+    out_ptr = out.device_ptr()
+    times = []
+    for i in range(reps):
+        rt.synchronize()
+        e0 = rt.event()
+        rt.launch_ptrs(prog, ptr_sets[i % len(sets)], out_ptr)
+        e1 = rt.event()
+        rt.event_wait(e1, 60 * 10 ** 9)
+        times.append(rt.event_elapsed_ms(e0, e1))
+        rt.event_release(e0)
+        rt.event_release(e1)
+    return statistics.median(times)
+
+
 def keep_busy(rt, st, seconds):
     """Untimed launches of the same kernel so the clock sampler sees the GPU under this load."""
     prog, sets, out = st["prog"], st["sets"], st["out"]
@@ -505,6 +523,12 @@ def main():
     # the same launches on one input set, which then stays in L2 (reported beside, never as the value)
     hot_ms = time_device(rt, dict(st, sets=st["sets"][:1]), args.steps, warmup) / args.steps
     hot = {"value": st["bytes"] / (hot_ms * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": hot_ms}
+    iso_ms = time_isolated(rt, st, 50)
+    overlap = {"pdl": rt.config_get("pdl") == 1,
+               "rule": "programmatic dependent launch: a launch whose inputs do not overlap the previous "
+                       "kernel's output issues its loads while that kernel drains; its stores wait for it",
+               "isolated_launch": {"value": st["bytes"] / (iso_ms * 1e-3) / 1e9, "unit": "GB/s",
+                                   "ms": iso_ms, "note": "one launch between two synchronisations, median of 50"}}
 
     e2e = None
     if not args.no_e2e:
@@ -528,7 +552,7 @@ def main():
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
                 "config": dict(st["config"], parallelism="replicas" if world > 1 else "single GPU"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-                "clocks": clocks, "hot_l2": hot}
+                "clocks": clocks, "hot_l2": hot, "launch_overlap": overlap}
         emit(line)
     if dist:
         dist.destroy_process_group()
