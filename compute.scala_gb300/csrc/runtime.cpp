@@ -1391,6 +1391,7 @@ namespace {
 constexpr int kBatchBlock = 256;
 constexpr int kBatchUnroll = 4;
 constexpr int64_t kBatchTile = (int64_t)kBatchBlock * 4 * kBatchUnroll;  // floats per tile (4096)
+constexpr int kBatchChunkTiles = 8;  // tiles a persistent block claims at once
 
 // The device table entry; must match the struct in the generated module.
 struct BatchEntry {
@@ -1489,18 +1490,34 @@ std::string batch_main_source(size_t n_structs) {
   o << "__device__ cc_tile_fn const cc_tiles[" << n_structs << "] = {\n";
   for (size_t s = 0; s < n_structs; ++s) o << "  cc_tile_" << s << ",\n";
   o << "};\n"
+    // Blocks claim runs of kBatchChunkTiles consecutive tiles from a work
+    // counter (zeroed before each launch): a block stays in one program's code
+    // for a run, and the uneven per-point cost of programs still balances.
     << "extern \"C\" __global__ void __launch_bounds__(" << kBatchBlock
-    << ") cc_batch(const cc_entry *__restrict__ table, int nprog, long long total_tiles) {\n"
+    << ") cc_batch(const cc_entry *__restrict__ table, int nprog, long long total_tiles,\n"
+    << "                unsigned long long *__restrict__ work) {\n"
     << "  extern __shared__ long long s_begin[];\n"
+    << "  __shared__ long long s_run;\n"
     << "  for (int i = threadIdx.x; i < nprog; i += blockDim.x) s_begin[i] = table[i].tile_begin;\n"
-    << "  __syncthreads();\n"
-    << "  for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {\n"
+    << "  for (;;) {\n"
+    << "    __syncthreads();\n"
+    << "    if (threadIdx.x == 0) s_run = (long long)atomicAdd(work, " << kBatchChunkTiles << "ULL);\n"
+    << "    __syncthreads();\n"
+    << "    const long long t0 = s_run;\n"
+    << "    if (t0 >= total_tiles) break;\n"
+    << "    const long long t1 = t0 + " << kBatchChunkTiles << "LL < total_tiles ? t0 + " << kBatchChunkTiles
+    << "LL : total_tiles;\n"
     << "    int lo = 0, hi = nprog - 1;\n"
     << "    while (lo < hi) {\n      const int mid = (lo + hi + 1) >> 1;\n"
-    << "      if (s_begin[mid] <= t) lo = mid; else hi = mid - 1;\n    }\n"
-    << "    const cc_entry e = table[lo];\n"
-    << "    const long long base = (t - e.tile_begin) * " << kBatchTile << "LL;\n"
-    << "    if (e.sid >= 0 && e.sid < " << n_structs << ") cc_tiles[e.sid](e.in[0], e.in[1], e.in[2], e.in[3], e.out, e.n, base);\n"
+    << "      if (s_begin[mid] <= t0) lo = mid; else hi = mid - 1;\n    }\n"
+    << "    long long next = lo + 1 < nprog ? s_begin[lo + 1] : total_tiles;\n"
+    << "    for (long long t = t0; t < t1; ++t) {\n"
+    << "      while (t >= next && lo + 1 < nprog) {\n        ++lo;\n"
+    << "        next = lo + 1 < nprog ? s_begin[lo + 1] : total_tiles;\n      }\n"
+    << "      const cc_entry e = table[lo];\n"
+    << "      const long long base = (t - e.tile_begin) * " << kBatchTile << "LL;\n"
+    << "      if (e.sid >= 0 && e.sid < " << n_structs << ") cc_tiles[e.sid](e.in[0], e.in[1], e.in[2], e.in[3], e.out, e.n, base);\n"
+    << "    }\n"
     << "  }\n}\n";
   return o.str();
 }
@@ -1720,7 +1737,8 @@ int cc_batch_bind(cc_handle batch, const uint64_t *ptrs, size_t n_ptrs) {
     e.sid = b.sid[p];
     tiles += (b.length[p] + kBatchTile - 1) / kBatchTile;
   }
-  if (!b.table) b.table = c.pool.alloc(sizeof(BatchEntry) * table.size(), &b.table_cls);
+  // one extra entry at the end holds the persistent kernel's work counter
+  if (!b.table) b.table = c.pool.alloc(sizeof(BatchEntry) * (table.size() + 1), &b.table_cls);
   check_cuda(cudaMemcpyAsync(b.table, table.data(), sizeof(BatchEntry) * table.size(), cudaMemcpyHostToDevice, c.stream),
              "upload batch table");
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
@@ -1743,7 +1761,9 @@ int cc_batch_run(cc_handle batch, int mode, uint64_t stream) {
     uint64_t table = reinterpret_cast<uint64_t>(b.table);
     int nprog = (int)b.sid.size();
     long long total = b.total_tiles;
-    void *args[] = {&table, &nprog, &total};
+    uint64_t work = table + sizeof(BatchEntry) * b.sid.size();
+    check_cuda(cudaMemsetAsync(reinterpret_cast<void *>(work), 0, sizeof(unsigned long long), s), "cudaMemsetAsync");
+    void *args[] = {&table, &nprog, &total, &work};
     int64_t cap = (int64_t)c.sm_count * (b.resident > 0 ? b.resident : 4);
     unsigned grid = (unsigned)(b.total_tiles < cap ? b.total_tiles : cap);
     check_cu(g_drv.LaunchKernel(b.persistent, grid, 1, 1, kBatchBlock, 1, 1, (unsigned)(sizeof(int64_t) * nprog),
