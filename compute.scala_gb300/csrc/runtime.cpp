@@ -321,6 +321,7 @@ struct Context {
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int pdl = 1;           // launch generated kernels with programmatic dependent launch
+  int copy_kernel = 0;   // copies between pinned host memory and the device by the SMs
   // The output range of the last generated kernel launched, and its stream: a
   // kernel that reads none of it may start its loads before that kernel ends.
   struct {
@@ -574,7 +575,40 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
 
 // Upload striped over the context's copy streams, ordered after the work
 // queued on the main stream and joined back into it.
+// The device-side address of a pinned host buffer (nullptr for pageable memory).
+const void *pinned_device_alias(const void *host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return a.devicePointer;
+}
+
+// Copies with the SMs (launch_copy16) when the knob is on, the host side is
+// pinned and both ends are 16-byte aligned; returns false to let the caller
+// use the DMA engines instead.
+bool sm_copy(Context &c, void *dst, const void *src, size_t bytes, bool to_device) {
+  if (!c.copy_kernel || bytes < (size_t(1) << 20)) return false;
+  const void *host = to_device ? src : dst;
+  const void *alias = pinned_device_alias(host);
+  if (!alias) return false;
+  void *d = to_device ? dst : const_cast<void *>(alias);
+  const void *s = to_device ? alias : src;
+  if ((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(s)) & 15u) return false;
+  const size_t body = bytes & ~size_t(15);
+  check_cuda(launch_copy16(d, s, body, c.sm_count, c.stream), "copy kernel");
+  if (body < bytes)
+    check_cuda(cudaMemcpyAsync(static_cast<char *>(dst) + body, static_cast<const char *>(src) + body, bytes - body,
+                               to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, c.stream),
+               "cudaMemcpyAsync");
+  c.last_write.valid = false;
+  return true;
+}
+
 void striped_upload(Context &c, char *dst, const char *src, size_t bytes) {
+  if (sm_copy(c, dst, src, bytes, true)) return;
   const int k = c.upload_streams;
   if (k <= 1 || bytes < (size_t(8) << 20)) {
     check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c.stream), "cudaMemcpyAsync H2D");
@@ -751,6 +785,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "sum_block") {
     if (value != 64 && value != 128 && value != 256) fail(CC_ERR_INVALID_VALUE, "sum_block must be 64, 128 or 256");
     c.sum_block = (int)value;
+  } else if (k == "copy_kernel") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "copy_kernel must be 0 or 1");
+    c.copy_kernel = (int)value;
   } else if (k == "tc_group_m") {
     if (value < 1 || value > 64) fail(CC_ERR_INVALID_VALUE, "tc_group_m must be in [1, 64]");
     c.tc_group_m = (int)value;
@@ -809,6 +846,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
   else if (k == "pdl") *value = c.pdl;
   else if (k == "tc_group_m") *value = c.tc_group_m;
+  else if (k == "copy_kernel") *value = c.copy_kernel;
   else if (k == "batch_max_registers") *value = c.batch_max_registers;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END
@@ -904,7 +942,8 @@ int cc_buf_download(cc_handle h, size_t offset, void *host, size_t bytes) {
   }
   if (bytes == 0) return CC_OK;
   if (!host) fail(CC_ERR_INVALID_VALUE, "null host pointer");
-  check_cuda(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, c.stream), "cudaMemcpyAsync D2H");
+  if (!sm_copy(c, host, src, bytes, false))
+    check_cuda(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, c.stream), "cudaMemcpyAsync D2H");
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
   CC_API_END
 }

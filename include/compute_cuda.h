@@ -83,6 +83,9 @@ int cc_synchronize(void);
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
  *                       3 = CC_GEMM_BF16X6
+ *   "copy_kernel"       1 = cc_buf_upload / cc_buf_download of 1 MiB or more between pinned host memory
+ *                       (cc_host_alloc) and the device are done by a copy kernel on the SMs instead of
+ *                       the DMA engines (16-byte aligned ends; default 0)
  *   "tc_group_m"        tensor-core GEMM: output tiles visited in groups of this many tile rows, so the
  *                       CTAs running together share A and B panels in L2 (1 = row-major; default 1)
  *   "pdl"               1 (default) = launch generated kernels with programmatic dependent launch: a kernel is
