@@ -123,6 +123,31 @@ def build_c2(T, x, bias, n, c, h, w):
     return y.translate([0, 0, 1, 0]).split(3).reduce(lambda a, b: a + b)
 
 
+C6 = {"n": 128, "h": 32, "w": 32, "c": 8, "k": 3}
+
+
+def conv_expr(T, x, weight, bias, parts=False):
+    """The library's 3x3 convolution idiom (benchmarks.scala:463-556): per filter,
+    the sum over kernel offsets and input channels of translated channel views
+    times broadcast weight scalars, plus the bias, joined along a new last axis
+    (``parts``: the per-filter tensors instead of their join)."""
+    n, h, w, depth = x.shape
+    kh, kw, _, filters = weight.shape
+    channels = x.split(3)
+    out = []
+    for f_weights, f_bias in zip(weight.split(3), bias.split(0)):
+        terms = []
+        for oy, row in zip(range(-(kh // 2), kh // 2 + 1), f_weights.split(0)):
+            for ox, pixel in zip(range(-(kw // 2), kw // 2 + 1), row.split(0)):
+                for ch, wch in zip(channels, pixel.split(0)):
+                    terms.append(ch.translate([0, oy, ox]) * wch.broadcast([n, h, w]))
+        acc = terms[0]
+        for t in terms[1:]:
+            acc = acc + t
+        out.append(f_bias.broadcast([n, h, w]) + acc)
+    return out if parts else T.join(out)
+
+
 C3 = {"c3": (4096, 4096, 4096), "c3s": (16384, 256, 16384)}
 # Exactly one index per seed makes the Wang hash 0 (log(0) = -inf in Box-Muller);
 # seeds with bit 30 set move it past 2^30, beyond these matrices.
@@ -225,6 +250,32 @@ def setup(workload, d):
                     config={"workload": "fused elementwise+sum: ((a*b+c).tanh).sum, a,b,c [1024,1024] U[-1,1]",
                             "l2": "inputs rotate over %d copies of (a,b,c) (%.0f MB > 4x L2)"
                                   % (copies, copies * 3 * n * m * 4 / 1e6)})
+    if workload == "c6":
+        from compute import trees
+        n, h, w, c, k = C6["n"], C6["h"], C6["w"], C6["c"], C6["k"]
+        x = T.randomNormal([n, h, w, c], seed=0).doCache()
+        weight = T.randomNormal([k, k, c, c], seed=1).doCache()
+        bias = T.randomNormal([c], seed=2).doCache()
+        chans = conv_expr(T, x, weight, bias, parts=True)
+        ser = d.serialize(trees.Concatenate([t.closure for t in chans]), chans[0].shape)
+        assert [id(p) for p in ser.params] == [id(x), id(weight), id(bias)]
+        prog = rt.program(ser.text)
+        xbytes = n * h * w * c * 4
+        copies = max(2, -(-4 * L2_BYTES // xbytes))
+        sets = []
+        for i in range(copies):
+            buf = rt.alloc(xbytes)
+            rt.random(buf, n * h * w * c, 0, True)
+            sets.append([buf, weight._cached, bias._cached])
+        out = rt.alloc(n * h * w * c * 4)
+        nbytes = 2 * xbytes + k * k * c * c * 4 + c * 4
+        return dict(prog=prog, sets=sets, out=out, bytes=nbytes, copies=copies, keep=(x, weight, bias), ser=ser,
+                    shape=(n, h, w, c),
+                    config={"workload": "3x3 convolution via translate/split/join: x[128,32,32,8] NHWC ~N(0,1), "
+                                        "weight[3,3,8,8], bias[8] -> [128,32,32,8]",
+                            "flops_per_step": 2 * n * h * w * c * k * k * c,
+                            "l2": "inputs rotate over %d copies of x (%.0f MB > 4x L2)"
+                                  % (copies, copies * xbytes / 1e6)})
     if workload in C3:
         m, k, n = C3[workload]
         rt.config_set("contraction", 3)  # split-BF16 on the tensor cores
@@ -439,6 +490,20 @@ def cpu_reference(workload, budget_s=15.0, threads=None):
     """Times the reference's CPU implementation (the oracle's C restatement of the
     generated OpenCL C, OpenMP over all host threads) on a bounded sample."""
     from oracle import cref
+    if workload == "c6":
+        n, h, w, c, k = C6["n"], C6["h"], C6["w"], C6["c"], C6["k"]
+
+        def make(T):
+            x = T.randomNormal([n, h, w, c], seed=0).doCache()
+            weight = T.randomNormal([k, k, c, c], seed=1).doCache()
+            bias = T.randomNormal([c], seed=2).doCache()
+            return conv_expr(T, x, weight, bias)
+
+        r = cref.time_expression(make, 2 * n * h * w * c * 4 + k * k * c * c * 4 + c * 4, budget_s=budget_s,
+                                 threads=threads)
+        r["config"] = {"workload": "3x3 convolution (reference CPU path, OpenCL C on host cores)"}
+        r["sample"] = "full workload, %d reps; one kernel joins the 8 filters, 576 loads per point" % r["reps"]
+        return r
     return cref.time_workload(workload, budget_s=budget_s, threads=threads)
 
 
@@ -450,7 +515,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s", "c4", "c5", "c6"])
     ap.add_argument("--programs", type=int, default=2048,
                     help="c4: programs in the batch; c5: tuning workloads to time (the last 10%% held out)")
     ap.add_argument("--max-len", type=int, default=4194304, help="c4: longest program (lengths log-uniform from 1024)")

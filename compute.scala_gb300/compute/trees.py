@@ -144,9 +144,12 @@ class Planner:
     times the tensor's own size.
     """
 
-    def __init__(self, max_recompute: float = 1.5, enabled: bool = True):
+    def __init__(self, max_recompute: float = 1.5, enabled: bool = True, merge_common: bool = None):
         self.max_recompute = max_recompute
         self.enabled = enabled
+        # write structurally identical subexpressions once (see serialize); off with
+        # fusion off, which keeps the reference's kernel structure
+        self.merge_common = enabled if merge_common is None else merge_common
 
     def inline(self, tensor, uses: int, frame_elements: int) -> bool:
         if not self.enabled:
@@ -220,9 +223,24 @@ def serialize(root: Node, out_shape: Sequence[int], kind: str = "ew",
     inline_memo: Dict[int, bool] = {}
     counts_memo: Dict[int, Dict[int, int]] = {}
 
+    # Identical lines (children already numbered canonically) denote the same
+    # function of the frame coordinates, so each is written once: common
+    # subexpressions -- the same translated input channel used by every filter
+    # of a convolution -- become one node, which the code generator evaluates
+    # (and loads) once per point.  Parameter lines are never merged.
+    line_ids: Dict[str, int] = {}
+    merge = planner is None or planner.merge_common
+
     def emit(line: str) -> int:
+        if merge and not line.startswith("p "):
+            got = line_ids.get(line)
+            if got is not None:
+                return got
         lines.append(line)
-        return len(lines) - 3  # node numbers start after the two header lines
+        nid = len(lines) - 3  # node numbers start after the two header lines
+        if merge and not line.startswith("p "):
+            line_ids[line] = nid
+        return nid
 
     def elements(shape) -> int:
         return int(np.prod(shape, dtype=np.int64)) if shape else 1

@@ -257,6 +257,28 @@ def time_workload(workload: str, budget_s: float = 15.0, threads=None):
     raise ValueError(workload)
 
 
+def time_expression(make, nbytes: int, budget_s: float = 15.0, threads=None):
+    """GB/s of the reference's CPU path evaluating ``make(T)`` (a tensor built with
+    the given Tensor companion, fusion off: the reference's kernel structure)."""
+    root = os.path.dirname(HERE)
+    sys.path.insert(0, os.path.join(root, "compute.scala_gb300"))
+    from compute import Tensors, trees
+    threads = threads or _threads()
+    d = Tensors(runtime=CRuntime(threads), planner=trees.Planner(enabled=False))
+    t = make(d.Tensor)
+    t.flatArray()  # compile and warm up
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        t.flatArray()
+        reps += 1
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 2 or reps >= 100:
+            break
+    per = dt / reps
+    return {"gbs": nbytes / per / 1e9, "ms_per_step": per * 1e3, "threads": threads, "reps": reps}
+
+
 def time_programs(make_programs, budget_s: float = 15.0, threads=None, max_programs: int = 64):
     """GB/s of the reference's CPU path over a sample of independent programs:
     ``make_programs(T)`` returns (tensor, inputs) pairs built with the given

@@ -254,3 +254,26 @@ def test_random_expression_trees(cuda_device):
             pool.append(t)
         e = pool[-1]
         assert np.array_equal(bits(e.flatArray()), bits(oracle_of(cuda_device, e))), trial
+
+
+@pytest.mark.parametrize("shape", [(2, 6, 5, 3, 4), (3, 32, 32, 8, 8)])
+def test_convolution_idiom_bit_exact(cuda_device, shape):
+    """The library's 3x3 convolution (translate + split + join), with its shared
+    translated channels written once, against the oracle and against the same
+    expression without merged subexpressions."""
+    import bench
+    from compute import Tensors, trees
+    n, h, w, c, f = shape
+    T = cuda_device.Tensor
+    x = T.randomNormal([n, h, w, c], seed=3).doCache()
+    wt = T.randomNormal([3, 3, c, f], seed=4).doCache()
+    b = T.randomNormal([f], seed=5).doCache()
+    parts = bench.conv_expr(T, x, wt, b, parts=True)
+    ser = cuda_device.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape)
+    got = bench.conv_expr(T, x, wt, b).flatArray()
+    want = interp.evaluate(ser.text, [p.flatArray() for p in ser.params])
+    assert np.array_equal(bits(got), bits(want))
+    plain = Tensors(device=0, runtime=cuda_device.runtime, planner=trees.Planner(merge_common=False))
+    unmerged = plain.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape)
+    assert unmerged.text.count("\nx ") > ser.text.count("\nx ")
+    assert np.array_equal(bits(bench.conv_expr(plain.Tensor, x, wt, b).flatArray()), bits(got))
