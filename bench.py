@@ -150,7 +150,7 @@ def conv_expr(T, x, weight, bias, parts=False):
 
 C3 = {"c3": (4096, 4096, 4096), "c3s": (16384, 256, 16384)}
 # Exactly one index per seed makes the Wang hash 0 (log(0) = -inf in Box-Muller);
-# seeds with bit 30 set move it past 2^30, beyond these matrices.
+# seeds with bit 30 set move it past 2^30, beyond these tensors.
 C3_SEED = 0x40000000
 
 
@@ -253,9 +253,9 @@ def setup(workload, d):
     if workload == "c6":
         from compute import trees
         n, h, w, c, k = C6["n"], C6["h"], C6["w"], C6["c"], C6["k"]
-        x = T.randomNormal([n, h, w, c], seed=0).doCache()
-        weight = T.randomNormal([k, k, c, c], seed=1).doCache()
-        bias = T.randomNormal([c], seed=2).doCache()
+        x = T.randomNormal([n, h, w, c], seed=C3_SEED).doCache()
+        weight = T.randomNormal([k, k, c, c], seed=C3_SEED + 1).doCache()
+        bias = T.randomNormal([c], seed=C3_SEED + 2).doCache()
         chans = conv_expr(T, x, weight, bias, parts=True)
         ser = d.serialize(trees.Concatenate([t.closure for t in chans]), chans[0].shape)
         assert [id(p) for p in ser.params] == [id(x), id(weight), id(bias)]
@@ -265,7 +265,7 @@ def setup(workload, d):
         sets = []
         for i in range(copies):
             buf = rt.alloc(xbytes)
-            rt.random(buf, n * h * w * c, 0, True)
+            rt.random(buf, n * h * w * c, C3_SEED, True)
             sets.append([buf, weight._cached, bias._cached])
         out = rt.alloc(n * h * w * c * 4)
         nbytes = 2 * xbytes + k * k * c * c * 4 + c * 4
@@ -494,9 +494,9 @@ def cpu_reference(workload, budget_s=15.0, threads=None):
         n, h, w, c, k = C6["n"], C6["h"], C6["w"], C6["c"], C6["k"]
 
         def make(T):
-            x = T.randomNormal([n, h, w, c], seed=0).doCache()
-            weight = T.randomNormal([k, k, c, c], seed=1).doCache()
-            bias = T.randomNormal([c], seed=2).doCache()
+            x = T.randomNormal([n, h, w, c], seed=C3_SEED).doCache()
+            weight = T.randomNormal([k, k, c, c], seed=C3_SEED + 1).doCache()
+            bias = T.randomNormal([c], seed=C3_SEED + 2).doCache()
             return conv_expr(T, x, weight, bias)
 
         r = cref.time_expression(make, 2 * n * h * w * c * 4 + k * k * c * c * 4 + c * 4, budget_s=budget_s,

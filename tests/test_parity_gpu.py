@@ -265,9 +265,11 @@ def test_convolution_idiom_bit_exact(cuda_device, shape):
     from compute import Tensors, trees
     n, h, w, c, f = shape
     T = cuda_device.Tensor
-    x = T.randomNormal([n, h, w, c], seed=3).doCache()
-    wt = T.randomNormal([3, 3, c, f], seed=4).doCache()
-    b = T.randomNormal([f], seed=5).doCache()
+    # seeds with bit 30 set: the reference's randomNormal of small seeds meets a zero
+    # hash (log 0) at some index, and NaN payloads are not comparable bit for bit
+    x = T.randomNormal([n, h, w, c], seed=0x40000003).doCache()
+    wt = T.randomNormal([3, 3, c, f], seed=0x40000004).doCache()
+    b = T.randomNormal([f], seed=0x40000005).doCache()
     parts = bench.conv_expr(T, x, wt, b, parts=True)
     ser = cuda_device.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape)
     got = bench.conv_expr(T, x, wt, b).flatArray()
