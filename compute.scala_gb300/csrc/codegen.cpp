@@ -266,6 +266,11 @@ struct Stmt {
   // and the input it reads (an in-bounds address when the condition fails).
   int ring = -1;
   std::string var, ptr, ok, base;
+  // A load at an index that depends on no output coordinate: its parameter,
+  // offset expression and padding, so it can be redirected to a shared copy.
+  int uparam = -1;
+  std::string uoff;
+  uint32_t ubits = 0;
 };
 
 class Generator {
@@ -337,6 +342,7 @@ class Generator {
         for (const std::string &i : idx)
           if (!uniform_.count(i)) uniform = false;
         const Cat load_cat = uniform ? Cat::Compute : Cat::Load;
+        if (!uniform) varying_params_.insert(p.param_index);
         if (ring_ > 0 && !uniform && asm_loads_ && (ok.empty() || p.bits == 0)) {
           // zero padding is the copy's zero fill
           Stmt st{Cat::Load, std::string()};
@@ -363,6 +369,14 @@ class Generator {
           add(load_cat, "const float " + v + " = __ldg(" + ptr + ");");
         } else {
           add(load_cat, "const float " + v + " = (" + ok + ") ? __ldg(" + ptr + ") : " + lit_code(p.bits) + ";");
+        }
+        if (uniform) {
+          Stmt &st = stmts_.back();
+          st.uparam = p.param_index;
+          st.uoff = p.dims.empty() ? std::string("0") : off;
+          st.ok = ok;
+          st.var = v;
+          st.ubits = p.bits;
         }
         break;
       }
@@ -446,6 +460,33 @@ class Generator {
       os << pad << s.text << "\n";
     }
     emit_loads_to(loads.size());
+  }
+
+  // Parameters read only at indices that depend on no output coordinate, of at
+  // most `max_bytes` together, are copied into shared memory once per block
+  // (`cc_sp<k>`) and read from there: a broadcast shared load instead of a
+  // global load through L1 for every use.  Returns (parameter, floats) pairs.
+  std::vector<std::pair<int, int64_t>> stage_uniform_params(int64_t max_bytes) {
+    std::vector<std::pair<int, int64_t>> staged;
+    std::set<int> chosen;
+    int64_t total = 0;
+    for (const Stmt &st : stmts_) {
+      if (st.uparam < 0 || varying_params_.count(st.uparam) || chosen.count(st.uparam)) continue;
+      const IrNode &p = ir_.nodes[ir_.param_nodes[st.uparam]];
+      int64_t elems = 1;
+      for (int64_t d : p.dims) elems *= d;
+      if (elems <= 0 || total + 4 * elems > max_bytes) continue;
+      total += 4 * elems;
+      chosen.insert(st.uparam);
+      staged.emplace_back(st.uparam, elems);
+    }
+    for (Stmt &st : stmts_) {
+      if (st.uparam < 0 || !chosen.count(st.uparam)) continue;
+      const std::string sp = "cc_sp" + std::to_string(st.uparam) + "[" + st.uoff + "]";
+      st.text = "const float " + st.var + " = " +
+                (st.ok.empty() ? sp : "(" + st.ok + ") ? " + sp + " : " + lit_code(st.ubits)) + ";";
+    }
+    return staged;
   }
 
   // Stage zero-padded loads that vary per thread through a shared-memory ring
@@ -532,6 +573,7 @@ class Generator {
   std::set<std::string> uniform_;  // index variables that depend on no output coordinate
   int ring_ = 0;
   int ring_loads_ = 0;
+  std::set<int> varying_params_;  // parameters read at least once at a per-thread index
 };
 
 bool is_contiguous_identity(const IrNode &x, const IrNode &p, const std::vector<int64_t> &out_shape) {
@@ -743,6 +785,10 @@ Generated describe_program(const Ir &ir) {
   return g;
 }
 
+// Shared memory a generic kernel may use for copies of small parameters read at
+// thread-independent indices.
+constexpr int64_t kMaxStagedBytes = 16 * 1024;
+
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   Generated g;
   g.n_inputs = ir.n_params;
@@ -801,6 +847,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   std::ostringstream generic;
   std::vector<std::string> results;
   int ring_slots = 0;
+  std::vector<std::pair<int, int64_t>> staged;
   {
     Generator gen(ir, false, opt.asm_loads, opt.prefetch_min_bytes);
     gen.set_ring(contiguous ? 0 : opt.smem_ring);  // contiguous programs use the float4 kernels
@@ -810,10 +857,18 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     } else {
       results.push_back(gen.gen(ir.root, f0));
     }
+    if (!contiguous) staged = gen.stage_uniform_params(kMaxStagedBytes);
     gen.emit(generic, 4, opt.smem_ring > 0 ? std::min(opt.load_lookahead, opt.smem_ring) : opt.load_lookahead);
     fp64 |= gen.uses_fp64();
     if (gen.ring_loads() > 0) ring_slots = opt.smem_ring;
   }
+  std::string stage_code;
+  for (auto &sp : staged) {
+    const std::string k = std::to_string(sp.first), n = std::to_string(sp.second);
+    stage_code += "  __shared__ float cc_sp" + k + "[" + n + "];\n  for (int i_ = threadIdx.x; i_ < " + n +
+                  "; i_ += blockDim.x) cc_sp" + k + "[i_] = __ldg(in" + k + " + i_);\n";
+  }
+  if (!stage_code.empty()) stage_code += "  __syncthreads();\n";
   g.uses_fp64_index = fp64;
   g.smem_bytes = ring_slots * opt.block * 4;
   const std::string ring_decl = ring_slots > 0 ? "  extern __shared__ float cc_ring[];\n" : "";
@@ -904,13 +959,24 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
   } else if (ir.kind == ProgramKind::Elementwise) {
     src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_ew(" << params
-        << "float *__restrict__ out, cc_i64 n) {\n" << ring_decl
+        << "float *__restrict__ out, cc_i64 n) {\n" << ring_decl << stage_code
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << generic.str();
     src << "    cc_pdl_gate(cc_early);\n";
     if (g.tuple_len == 1) {
       src << "    out[lin] = " << results[0] << ";\n";
+    } else if (g.tuple_len % 4 == 0) {
+      // a point's tuple is tuple_len consecutive floats: float4 stores when aligned
+      src << "    if ((reinterpret_cast<unsigned long long>(out) & 15ull) == 0) {\n"
+          << "      float4 *o4_ = reinterpret_cast<float4 *>(out + lin * " << g.tuple_len << "LL);\n";
+      for (int k = 0; k < g.tuple_len; k += 4)
+        src << "      o4_[" << k / 4 << "] = make_float4(" << results[k] << ", " << results[k + 1] << ", "
+            << results[k + 2] << ", " << results[k + 3] << ");\n";
+      src << "    } else {\n";
+      for (int k = 0; k < g.tuple_len; ++k)
+        src << "      out[lin * " << g.tuple_len << "LL + " << k << "] = " << results[k] << ";\n";
+      src << "    }\n";
     } else {
       for (int k = 0; k < g.tuple_len; ++k)
         src << "    out[lin * " << g.tuple_len << "LL + " << k << "] = " << results[k] << ";\n";
@@ -924,7 +990,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   } else {
     src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_sum(" << params
         << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
-        << ring_decl << "  float s_ = 0.0f, c_ = 0.0f;\n"
+        << ring_decl << stage_code << "  float s_ = 0.0f, c_ = 0.0f;\n"
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << generic.str() << "    cc_acc(s_, c_, " << results[0] << ");\n  }\n"
