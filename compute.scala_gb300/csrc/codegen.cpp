@@ -470,6 +470,14 @@ class Generator {
     std::vector<std::pair<int, int64_t>> staged;
     std::set<int> chosen;
     int64_t total = 0;
+    // Worth it only when such loads dominate: the copy and its barrier delay
+    // the first per-thread load, which a short one-wave kernel feels.
+    int uniform_loads = 0, varying_loads = 0;
+    for (const Stmt &st : stmts_) {
+      if (st.uparam >= 0 && !varying_params_.count(st.uparam)) ++uniform_loads;
+      if (st.cat == Cat::Load) ++varying_loads;
+    }
+    if (uniform_loads < 2 * varying_loads) return staged;
     for (const Stmt &st : stmts_) {
       if (st.uparam < 0 || varying_params_.count(st.uparam) || chosen.count(st.uparam)) continue;
       const IrNode &p = ir_.nodes[ir_.param_nodes[st.uparam]];
