@@ -154,3 +154,30 @@ def test_shared_memory_ring_codegen_compiles():
     assert src.count("cc_cp4(&cc_ring") == 128  # every x load staged; the bias loads (uniform) are not
     assert "cc_cp4(&cc_ring" not in runtime.codegen(text)
     runtime.compile_check(text, options="block=128 ring=32 lookahead=32 min_blocks=11")
+
+
+def test_merged_subexpressions_keep_the_oracle_bits():
+    """Structurally identical subexpressions are written once in the IR; the
+    oracle gives the same bits for the merged and the unmerged text."""
+    import bench
+    import numpy as np
+    from compute import Tensors, trees
+    from compute.tensors import NonInlineTensor
+    from oracle import interp
+    d = Tensors(device=0)
+    plain = Tensors(device=0, planner=trees.Planner(merge_common=False))
+    shapes = [(2, 5, 4, 3), (3, 3, 3, 2), (2,)]
+    r = np.random.RandomState(0)
+    arrays = [r.normal(size=int(np.prod(s))).astype(np.float32) for s in shapes]
+    texts = []
+    for dev in (d, plain):
+        x, w, b = (NonInlineTensor(dev, s, 0.0, None) for s in shapes)
+        parts = bench.conv_expr(dev.Tensor, x, w, b, parts=True)
+        ser = dev.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape)
+        order = {id(x): 0, id(w): 1, id(b): 2}
+        texts.append((ser.text, [arrays[order[id(p)]] for p in ser.params]))
+    (merged, m_in), (unmerged, u_in) = texts
+    assert merged.count("\nx ") < unmerged.count("\nx ")
+    a = interp.evaluate(merged, m_in)
+    b_ = interp.evaluate(unmerged, u_in)
+    assert np.array_equal(a.view(np.int32), b_.view(np.int32))
