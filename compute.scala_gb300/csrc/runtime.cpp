@@ -712,6 +712,27 @@ int cc_shutdown(void) {
   cudaStreamSynchronize(c->stream);
   for (auto &kv : c->programs) delete kv.second;
   c->modules.clear();
+  for (auto &kv : c->batches) {
+    Batch *b = kv.second;
+    if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->table) c->pool.release(b->table, b->table_cls);
+    if (b->module) g_drv.ModuleUnload(b->module);
+    delete b;
+  }
+  c->batches.clear();
+  for (auto &kv : c->tune_sets) {
+    if (kv.second->flush) c->pool.release(kv.second->flush, kv.second->flush_cls);
+    delete kv.second;
+  }
+  c->tune_sets.clear();
+  for (auto &kv : c->mlps) {
+    if (kv.second->scratch) c->pool.release(kv.second->scratch, kv.second->scratch_cls);
+    if (kv.second->state) c->pool.release(kv.second->state, kv.second->state_cls);
+    delete kv.second;
+  }
+  c->mlps.clear();
+  c->cost_model = 0;
   for (auto &kv : c->buffers) {
     cudaFree(kv.second->ptr);
     delete kv.second;
