@@ -26,7 +26,8 @@ constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 32;
 // Kernel variants: 0 = 128-column tiles, accumulators restarted every 4
 // k-blocks and summed in registers (FP32-level error at any K); 1 = 256-column
 // tiles, one accumulator pair per tile (fastest; error grows with K);
-// 2 = 128-column tiles, one pair per tile.  gemm_tc_box_n: the tile width.
+// 2 = 128-column tiles, one pair per tile; 3 / 4 = as 0 with accumulators restarted
+// every 8 / 16 k-blocks.  gemm_tc_box_n: the tile width.
 int gemm_tc_box_n(int variant);
 // maps: A planes 0..2 (box 32 x 128), B^T planes 0..2 (box 32 x gemm_tc_box_n), 64-byte swizzle.
 // group_m: output tiles are visited in groups of this many tile rows (1 = row-major).

@@ -462,6 +462,8 @@ cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, 
                                int sm_count, int *err, int variant, int group_m, cudaStream_t stream) {
   if (variant == 1) return launch_variant<256, 3, 1, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   if (variant == 2) return launch_variant<128, 4, 2, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
+  if (variant == 3) return launch_variant<128, 4, 2, 8>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
+  if (variant == 4) return launch_variant<128, 4, 2, 16>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   return launch_variant<128, 4, 2, 4>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
 }
 

@@ -831,7 +831,7 @@ int cc_config_set(const char *key, int64_t value) {
     if (value < 0 || value > 3) fail(CC_ERR_INVALID_VALUE, "contraction must be in [0, 3]");
     c.contraction = (int)value;
   } else if (k == "tc_variant") {
-    if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "tc_variant must be 0, 1 or 2");
+    if (value < 0 || value > 4) fail(CC_ERR_INVALID_VALUE, "tc_variant must be in [0, 4]");
     c.tc_variant = (int)value;
   } else if (k == "vec_unroll") {
     if (value < 1 || value > 8) fail(CC_ERR_INVALID_VALUE, "vec_unroll must be in [1, 8]");

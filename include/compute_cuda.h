@@ -102,7 +102,8 @@ int cc_synchronize(void);
  *                       1 = expressions inlined, exp/log/tanh called (default), 2 = all inlined
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
  *                       registers (FP32-level error at any K; default), 1 = 128x256 tiles, one
- *                       accumulator per tile (fastest, error grows with K), 2 = 128x128, one per tile
+ *                       accumulator per tile (fastest, error grows with K), 2 = 128x128, one per tile,
+ *                       3 / 4 = as 0 with K chunks of 256 / 512
  *   "vec_unroll"        float4 positions a thread of a contiguous kernel loads before computing (1..8; default 4)
  * Unknown keys or values out of range return CC_ERR_INVALID_VALUE. */
 int cc_config_set(const char *key, int64_t value);
