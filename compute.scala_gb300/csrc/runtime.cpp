@@ -314,7 +314,7 @@ struct Context {
   int vec_unroll = 4;
   int64_t prefetch_min_bytes = -1;
   int sum_block = 256;
-  int tc_variant = 0;
+  int tc_variant = 3;  // 128x128 tiles, accumulators restarted every 256 of K
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
   int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel

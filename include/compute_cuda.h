@@ -101,9 +101,9 @@ int cc_synchronize(void);
  *   "batch_inline"      batch modules: 0 = expressions and exp/log/tanh are called functions,
  *                       1 = expressions inlined, exp/log/tanh called (default), 2 = all inlined
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
- *                       registers (FP32-level error at any K; default), 1 = 128x256 tiles, one
- *                       accumulator per tile (fastest, error grows with K), 2 = 128x128, one per tile,
- *                       3 / 4 = as 0 with K chunks of 256 / 512
+ *                       registers (error ~1.6e-7 at any K), 1 = 128x256 tiles, one accumulator
+ *                       per tile (error grows with K), 2 = 128x128, one per tile, 3 = as 0 with
+ *                       chunks of 256 (default: ~2.4e-7), 4 = chunks of 512 (~4.7e-7)
  *   "vec_unroll"        float4 positions a thread of a contiguous kernel loads before computing (1..8; default 4)
  * Unknown keys or values out of range return CC_ERR_INVALID_VALUE. */
 int cc_config_set(const char *key, int64_t value);
