@@ -460,6 +460,11 @@ int gemm_tc_box_n(int variant) { return variant == 1 ? 256 : 128; }
 
 cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
                                int sm_count, int *err, int variant, int group_m, cudaStream_t stream) {
+  // When K fits in one chunk the running sum only adds the pair to zero, which
+  // changes no value (at most the sign of a zero result): the one-pair-per-tile
+  // kernel computes the same without the running sum's registers.
+  const int num_kb = K_padded / BK;
+  if ((variant == 0 && num_kb <= 4) || (variant == 3 && num_kb <= 8) || (variant == 4 && num_kb <= 16)) variant = 2;
   if (variant == 1) return launch_variant<256, 3, 1, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   if (variant == 2) return launch_variant<128, 4, 2, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   if (variant == 3) return launch_variant<128, 4, 2, 8>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
