@@ -20,7 +20,9 @@
 //               "empty" mbarrier and, after a tile's last stage, to the
 //               accumulator pair's "full";
 //   warps 2..5  epilogue: tcgen05.ld both accumulators (each warp reads its own
-//               32-lane quarter of TMEM), add, store to C, release the pair.
+//               32-lane quarter of TMEM), add, store to C, release the pair;
+//               kernels that sum K chunks in registers have a second group,
+//               warps 6..9, and each group takes half of the columns.
 // Every mbarrier wait gives up after kWaitNs of %globaltimer time: it records
 // an error code in *err, raises the CTA's abort flag, and all roles leave their
 // loops, so the CTA still frees its TMEM and returns.
@@ -39,7 +41,12 @@ constexpr int BM = 128, BK = 32;  // BK bf16 = 64 bytes = one 64-byte swizzle ro
 constexpr int kAPlaneBytes = BM * BK * 2;  // 8 KiB
 constexpr int kTmemCols = 512;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s
-constexpr int kThreads = 192;
+// Warps: 0 = TMA, 1 = MMA and TMEM allocation, then the epilogue: one group of
+// four warps (one per 32-lane quarter of TMEM) for kernels that store each
+// accumulator pair directly, two groups splitting the columns for kernels that
+// keep a running sum per row (half the registers each).
+__host__ __device__ constexpr int epilogue_groups(int kc) { return kc > 0 ? 2 : 1; }
+__host__ __device__ constexpr int threads_for(int kc) { return 64 + 128 * epilogue_groups(kc); }
 
 template <int BN, int STAGES, int ACC_BUFS>
 struct TcCfg {
@@ -194,7 +201,7 @@ __device__ __constant__ int kProdA[6] = {0, 0, 1, 1, 0, 2};
 __device__ __constant__ int kProdB[6] = {0, 1, 0, 1, 2, 0};
 
 template <int BN, int STAGES, int ACC_BUFS, int KC>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(threads_for(KC), 1)
     gemm_bf16x6_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
                        const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap tb0,
                        const __grid_constant__ CUtensorMap tb1, const __grid_constant__ CUtensorMap tb2,
@@ -224,7 +231,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int a = 0; a < ACC_BUFS; ++a) {
       mbar_init(bar_accfull + 8 * a, 1);
-      mbar_init(bar_accempty + 8 * a, 128);
+      mbar_init(bar_accempty + 8 * a, 128 * epilogue_groups(KC));
     }
     mbar_init(bar_drain, 1);
     *abort_flag = 0;
@@ -386,11 +393,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       // registers, round-to-nearest), so no FP32 accumulator inside the tensor
       // core takes more than KC k-blocks of additions.
       const int nchunks = (num_kb + KC - 1) / KC;
+      constexpr int kCols = BN / epilogue_groups(KC);      // columns of this thread's group
+      const int col0 = ((warp - 2) >> 2) * kCols;           // group 0: warps 2-5, group 1: warps 6-9
       bool ok = true;
       for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
-        float sum[BN];
+        float sum[kCols];
 #pragma unroll
-        for (int j = 0; j < BN; ++j) sum[j] = 0.0f;
+        for (int j = 0; j < kCols; ++j) sum[j] = 0.0f;
         for (int ch = 0; ch < nchunks; ++ch) {
           if (!mbar_wait(bar_accfull + 8 * acc, acc_phase, abort_flag, err, 4)) {
             ok = false;
@@ -398,9 +407,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           tc_fence_after();
 #pragma unroll
-          for (int c32 = 0; c32 < BN / 32; ++c32) {
+          for (int c32 = 0; c32 < kCols / 32; ++c32) {
             float v[32], w[32];
-            const uint32_t t = lane_tmem + (uint32_t)(acc * 2 * BN + c32 * 32);
+            const uint32_t t = lane_tmem + (uint32_t)(acc * 2 * BN + col0 + c32 * 32);
             tmem_ld32(t, v);
             tmem_ld32(t + BN, w);
 #pragma unroll
@@ -420,7 +429,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int row = m0 + row_in_tile;
         float *crow = C + (long long)row * ldc;
 #pragma unroll
-        for (int c32 = 0; c32 < BN / 32; ++c32) store_row_chunk(crow, row, M, N, ldc, n0 + c32 * 32, sum + c32 * 32);
+        for (int c32 = 0; c32 < kCols / 32; ++c32)
+          store_row_chunk(crow, row, M, N, ldc, n0 + col0 + c32 * 32, sum + c32 * 32);
       }
     }
   }
@@ -448,7 +458,7 @@ cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int 
   const int num_tiles = tiles_m * tiles_n;
   const int num_kb = K_padded / BK;
   const int grid = num_tiles < sm_count ? num_tiles : sm_count;
-  gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS, KC><<<grid, kThreads, Cfg::kSmemBytes, stream>>>(
+  gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS, KC><<<grid, threads_for(KC), Cfg::kSmemBytes, stream>>>(
       maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], C, M, N, ldc, num_kb, tiles_n, num_tiles,
       group_m < 1 ? 1 : group_m, err);
   return cudaGetLastError();
