@@ -951,6 +951,22 @@ int cc_buf_upload(cc_handle h, size_t offset, const void *host, size_t bytes) {
   CC_API_END
 }
 
+int cc_buf_upload_async(cc_handle h, size_t offset, const void *host, size_t bytes) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  void *dst;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    Buffer &b = buffer_of(c, h);
+    if (offset > b.bytes || bytes > b.bytes - offset) fail(CC_ERR_INVALID_VALUE, "upload range exceeds the buffer");
+    dst = static_cast<char *>(b.ptr) + offset;
+  }
+  if (bytes == 0) return CC_OK;
+  if (!host) fail(CC_ERR_INVALID_VALUE, "null host pointer");
+  striped_upload(c, static_cast<char *>(dst), static_cast<const char *>(host), bytes);
+  CC_API_END
+}
+
 int cc_buf_download(cc_handle h, size_t offset, void *host, size_t bytes) {
   CC_API_BEGIN
   Context &c = ctx();

@@ -120,6 +120,10 @@ int cc_buf_size(cc_handle buf, size_t *bytes);
 int cc_buf_device_ptr(cc_handle buf, uint64_t *device_ptr);
 /* Host -> device copy into [offset, offset+bytes).  Returns when the host memory may be reused. */
 int cc_buf_upload(cc_handle buf, size_t offset, const void *host, size_t bytes);
+/* The same, ordered on the context stream without waiting for it (OpenCL's
+ * non-blocking enqueueWriteBuffer): the host memory must stay unchanged until
+ * the copy is complete (cc_synchronize, or an event recorded after it). */
+int cc_buf_upload_async(cc_handle buffer, size_t offset, const void *host, size_t bytes);
 /* Device -> host copy of [offset, offset+bytes) after all work queued so far; blocking. */
 int cc_buf_download(cc_handle buf, size_t offset, void *host, size_t bytes);
 /* Page-locked host memory for fast transfers (the staging of Tensor.apply / flatArray). */

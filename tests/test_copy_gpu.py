@@ -38,3 +38,35 @@ def test_copy_kernel_round_trips(cuda_device):
         rt.config_set("copy_kernel", 0)
         call("cc_host_free", host)
         call("cc_host_free", back)
+
+
+def test_async_uploads_are_ordered_before_launches(cuda_device):
+    """cc_buf_upload_async copies many buffers without waiting; a launch and a
+    download queued after them see the uploaded bytes."""
+    rt = cuda_device.runtime
+    d = cuda_device
+    from compute.tensors import NonInlineTensor
+    n = (1 << 22) + 3
+    p = NonInlineTensor(d, (n,), 0.0, None)
+    prog = rt.program(d.serialize((p * d.Tensor.fill(2.0, [n])).closure, (n,)).text)
+    hosts, bufs = [], []
+    for k in range(6):
+        h = ctypes.c_void_p()
+        call("cc_host_alloc", ctypes.c_size_t(4 * n), ctypes.byref(h))
+        arr = np.ctypeslib.as_array((ctypes.c_float * n).from_address(h.value))
+        arr[:] = np.arange(n, dtype=np.float32) + k
+        hosts.append((h, arr))
+        bufs.append(rt.alloc(4 * n))
+    outs = [rt.alloc(4 * n) for _ in bufs]
+    try:
+        for (h, _), b in zip(hosts, bufs):
+            call("cc_buf_upload_async", ctypes.c_uint64(b.handle), ctypes.c_size_t(0), h, ctypes.c_size_t(4 * n))
+        for b, o in zip(bufs, outs):
+            rt.launch(prog, [b], o)
+        for k, o in enumerate(outs):
+            assert np.array_equal(rt.download(o, n), 2 * (np.arange(n, dtype=np.float32) + k))
+    finally:
+        for h, _ in hosts:
+            call("cc_host_free", h)
+        for b in bufs + outs:
+            b.release()
