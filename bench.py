@@ -247,7 +247,7 @@ def setup(workload, d):
         out = rt.alloc(4)
         return dict(prog=prog, sets=sets, out=out, bytes=c1_bytes(n, m), copies=copies, keep=abc, ser=ser,
                     shape=(n, m),
-                    config={"workload": "fused elementwise+sum: ((a*b+c).tanh).sum, a,b,c [1024,1024] U[-1,1]",
+                    config={"workload": "fused elementwise+sum: ((a*b+c).tanh).sum, a,b,c [%d,%d] U[-1,1]" % (n, m),
                             "l2": "inputs rotate over %d copies of (a,b,c) (%.0f MB > 4x L2)"
                                   % (copies, copies * 3 * n * m * 4 / 1e6)})
     if workload == "c6":
@@ -524,6 +524,7 @@ def main():
     ap.add_argument("--programs", type=int, default=2048,
                     help="c4: programs in the batch; c5: tuning workloads to time (the last 10%% held out)")
     ap.add_argument("--max-len", type=int, default=4194304, help="c4: longest program (lengths log-uniform from 1024)")
+    ap.add_argument("--c1-side", type=int, default=1024, help="c1: side of the square inputs (1024 = the benchmark)")
     ap.add_argument("--db", default=None, help="c5: append the timing records (JSON lines) to this file")
     ap.add_argument("--collect-budget-s", type=float, default=None, help="c5: stop collecting after this long")
     ap.add_argument("--db-in", default=None, help="c5: train and evaluate on these timing records instead of timing")
@@ -572,6 +573,8 @@ def main():
     d = Tensors(device=local_rank)
     rt = d.runtime
     apply_knobs(rt, args.knob)
+    if args.workload == "c1":
+        C1["n"] = C1["m"] = args.c1_side
     st = setup(args.workload, d)
     sampler = ClockSampler(local_rank)
     if dist:
@@ -806,6 +809,8 @@ def main_contraction(args, warmup, rank, world, local_rank):
     d = Tensors(device=local_rank)
     rt = d.runtime
     apply_knobs(rt, args.knob)
+    if args.workload == "c1":
+        C1["n"] = C1["m"] = args.c1_side
     st = setup(args.workload, d)
     sampler = ClockSampler(local_rank)
     rt.synchronize()
