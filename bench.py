@@ -224,8 +224,8 @@ def setup(workload, d):
         out = rt.alloc(n * h * w * 4)
         return dict(prog=prog, sets=sets, out=out, bytes=c2_bytes(n, c, h, w), copies=copies,
                     keep=[x, bias], ser=ser, shape=(n, c, h, w),
-                    config={"workload": "view-heavy fused op: x[64,128,56,56] permute->+bias[128]->max0"
-                                        "->translate W+1->channel sum [64,56,56]",
+                    config={"workload": ("view-heavy fused op: x[%d,128,56,56] permute->+bias[128]->max0"
+                                         "->translate W+1->channel sum [%d,56,56]") % (n, n),
                             "x": [n, c, h, w], "bias": [c], "out": [n, h, w],
                             "l2": "inputs rotate over %d copies of x (%.0f MB > 4x L2)" % (copies, copies * xbytes / 1e6)})
     if workload == "c1":
@@ -525,6 +525,7 @@ def main():
                     help="c4: programs in the batch; c5: tuning workloads to time (the last 10%% held out)")
     ap.add_argument("--max-len", type=int, default=4194304, help="c4: longest program (lengths log-uniform from 1024)")
     ap.add_argument("--c1-side", type=int, default=1024, help="c1: side of the square inputs (1024 = the benchmark)")
+    ap.add_argument("--c2-batch", type=int, default=64, help="c2: images in x (64 = the benchmark)")
     ap.add_argument("--db", default=None, help="c5: append the timing records (JSON lines) to this file")
     ap.add_argument("--collect-budget-s", type=float, default=None, help="c5: stop collecting after this long")
     ap.add_argument("--db-in", default=None, help="c5: train and evaluate on these timing records instead of timing")
@@ -575,6 +576,8 @@ def main():
     apply_knobs(rt, args.knob)
     if args.workload == "c1":
         C1["n"] = C1["m"] = args.c1_side
+    if args.workload == "c2":
+        C2["n"] = args.c2_batch
     st = setup(args.workload, d)
     sampler = ClockSampler(local_rank)
     if dist:
@@ -811,6 +814,8 @@ def main_contraction(args, warmup, rank, world, local_rank):
     apply_knobs(rt, args.knob)
     if args.workload == "c1":
         C1["n"] = C1["m"] = args.c1_side
+    if args.workload == "c2":
+        C2["n"] = args.c2_batch
     st = setup(args.workload, d)
     sampler = ClockSampler(local_rank)
     rt.synchronize()
