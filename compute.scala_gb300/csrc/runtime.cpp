@@ -551,7 +551,7 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   const unsigned smem = vec ? 0 : (unsigned)m.smem_bytes;
   if (c.pdl) {
     // programmatic dependent launch: this grid may be scheduled while the
-    // previous kernel in the stream drains; its cc_pdl_enter() keeps the order
+    // previous kernel in the stream drains; its cc_pdl_begin / cc_pdl_gate keep the order
     CUlaunchAttribute attr;
     memset(&attr, 0, sizeof attr);
     attr.id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;

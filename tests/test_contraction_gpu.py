@@ -6,7 +6,7 @@
 * CC_GEMM_FP32 (fused multiply-adds) and CC_GEMM_BF16X6 (three bfloat16 planes,
   six products, FP32 accumulation on the tensor cores) are measured by their
   relative Frobenius error against float64: at most 1e-6 for the split-BF16
-  path (BASELINE: <= 1e-6 relative error).
+  path (the bar: <= 1e-6 relative error).
 """
 
 import numpy as np
