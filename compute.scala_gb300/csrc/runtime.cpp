@@ -1488,7 +1488,7 @@ static_assert(sizeof(BatchEntry) == 64, "batch entry layout");
 //   - the main unit: a device table of the tile functions and the persistent
 //     kernel, which finds a tile's program by binary search and calls its tile
 //     function through the table.
-// The parts compile in parallel (relocatable code) and the driver links them.
+// The parts compile in parallel (relocatable code) and the CUDA driver API links them (cuLink*).
 constexpr int kBatchChunk = 32;
 
 const char *kTileParams =
