@@ -531,6 +531,9 @@ def main():
     ap.add_argument("--db-in", default=None, help="c5: train and evaluate on these timing records instead of timing")
     ap.add_argument("--save-model", default=None, help="c5: write the trained cost model (.npz) here")
     ap.add_argument("--epochs", type=int, default=40, help="c5: training epochs")
+    ap.add_argument("--seed", type=int, default=0, help="c5: seed of the generated tuning workloads")
+    ap.add_argument("--eval-model", default=None,
+                    help="c5: evaluate this trained model (.npz) on all timed programs instead of training one")
     ap.add_argument("--knob", action="append", default=[], metavar="KEY=VALUE",
                     help="runtime setting (cc_config_set) applied before the run; repeatable")
     ap.add_argument("--no-e2e", action="store_true")
@@ -658,7 +661,7 @@ def main_tuner(args, warmup, rank, world, local_rank):
         gen_s = 0.0
         collect_s = 0.0
     else:
-        progs = tuner.random_programs(args.programs, seed=0)
+        progs = tuner.random_programs(args.programs, seed=args.seed)
         gen_s = time.time() - t0
         log = open(args.db, "a") if args.db else None
         t0 = time.time()
@@ -668,6 +671,22 @@ def main_tuner(args, warmup, rank, world, local_rank):
             if log:
                 log.close()
         collect_s = time.time() - t0
+    if args.eval_model:
+        model = tuner.CostModel(rt, seed=0)
+        model.load(args.eval_model)
+        res = tuner.evaluate(model, recs, sm, fixed=30)
+        line = {"metric": "learned-tuner regret (geometric-mean slowdown vs exhaustive best), trained model on "
+                          "unseen programs",
+                "value": res["learned"]["geomean_slowdown"], "unit": "fraction", "n_gpus": 1, "steps": 0,
+                "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic (seeded tuning workloads, seed %d)" % args.seed,
+                "config": {"workload": "tuning workloads as c5, all %d programs evaluated" % len(recs),
+                           "model": args.eval_model, "timing": "median of 5 launches per config, L2 flushed"},
+                "tuner": res, "seconds": {"compile_and_time": round(collect_s, 1)},
+                "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": None}
+        emit(line)
+        model.close()
+        return
     split = int(len(recs) * 0.9)
     train, test = recs[:split], recs[split:]
     x, y = tuner.training_arrays(train, sm)
