@@ -1491,9 +1491,10 @@ static_assert(sizeof(BatchEntry) == 64, "batch entry layout");
 // The parts compile in parallel (relocatable code) and the CUDA driver API links them (cuLink*).
 constexpr int kBatchChunk = 32;
 
+// A tile function evaluates `count` consecutive tiles of one program from `base`.
 const char *kTileParams =
     "(const float *__restrict__ in0, const float *__restrict__ in1, const float *__restrict__ in2, "
-    "const float *__restrict__ in3, float *__restrict__ out, long long n, long long base)";
+    "const float *__restrict__ in3, float *__restrict__ out, long long n, long long base, int count)";
 
 // inline_level: 0 = the expression is a called function and so are exp/log/tanh;
 // 1 = the expression is inlined into its tile function, exp/log/tanh called;
@@ -1521,6 +1522,7 @@ std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector
     // has kBatchUnroll loads per input in flight; the ragged last tile of a
     // program takes the plain loops.
     o << "extern \"C\" __device__ __noinline__ void cc_tile_" << S << kTileParams << " {\n"
+      << "  for (; count > 0; --count, base += " << kBatchTile << "LL) {\n"
       << "  if (base + " << kBatchTile << "LL <= n) {\n"
       << "    const long long q0 = (base >> 2) + threadIdx.x;\n";
     for (int i = 0; i < nin; ++i)
@@ -1535,7 +1537,7 @@ std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector
     }
     for (int u = 0; u < kBatchUnroll; ++u)
       o << "    reinterpret_cast<float4 *>(out)[q0 + " << u * kBatchBlock << "] = r_" << u << ";\n";
-    o << "    return;\n  }\n"
+    o << "    continue;\n  }\n"
       << "  const long long end = base + " << kBatchTile << "LL < n ? base + " << kBatchTile << "LL : n;\n"
       << "  const long long end4 = end & ~3LL;\n"
       << "  for (long long q = (base >> 2) + threadIdx.x; (q << 2) < end4; q += " << B << ") {\n";
@@ -1546,13 +1548,13 @@ std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector
     o << "    reinterpret_cast<float4 *>(out)[q] = r;\n  }\n"
       << "  for (long long i = end4 + threadIdx.x; i < end; i += " << B << ") {\n";
     for (int i = 0; i < nin; ++i) o << "    const float v" << i << " = __ldg(in" << i << " + i);\n";
-    o << "    out[i] = " << call("") << ";\n  }\n}\n";
+    o << "    out[i] = " << call("") << ";\n  }\n  }\n}\n";
     o << "extern \"C\" __global__ void __launch_bounds__(" << B << ") cc_prog_" << S
       << "(const float *__restrict__ in0, const float *__restrict__ in1, const float *__restrict__ in2, "
          "const float *__restrict__ in3, float *__restrict__ out, long long n) {\n"
       << "  const long long tiles = (n + " << kBatchTile - 1 << "LL) / " << kBatchTile << "LL;\n"
       << "  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) cc_tile_" << S
-      << "(in0, in1, in2, in3, out, n, t * " << kBatchTile << "LL);\n}\n";
+      << "(in0, in1, in2, in3, out, n, t * " << kBatchTile << "LL, 1);\n}\n";
   }
   return o.str();
 }
@@ -1587,12 +1589,15 @@ std::string batch_main_source(size_t n_structs) {
     << "    while (lo < hi) {\n      const int mid = (lo + hi + 1) >> 1;\n"
     << "      if (s_begin[mid] <= t0) lo = mid; else hi = mid - 1;\n    }\n"
     << "    long long next = lo + 1 < nprog ? s_begin[lo + 1] : total_tiles;\n"
-    << "    for (long long t = t0; t < t1; ++t) {\n"
+    // one call per program the run touches, for all of its tiles in the run
+    << "    for (long long t = t0; t < t1;) {\n"
     << "      while (t >= next && lo + 1 < nprog) {\n        ++lo;\n"
     << "        next = lo + 1 < nprog ? s_begin[lo + 1] : total_tiles;\n      }\n"
+    << "      const long long stop = next < t1 ? next : t1;\n"
     << "      const cc_entry e = table[lo];\n"
     << "      const long long base = (t - e.tile_begin) * " << kBatchTile << "LL;\n"
-    << "      if (e.sid >= 0 && e.sid < " << n_structs << ") cc_tiles[e.sid](e.in[0], e.in[1], e.in[2], e.in[3], e.out, e.n, base);\n"
+    << "      if (e.sid >= 0 && e.sid < " << n_structs << ") cc_tiles[e.sid](e.in[0], e.in[1], e.in[2], e.in[3], e.out, e.n, base, (int)(stop - t));\n"
+    << "      t = stop;\n"
     << "    }\n"
     << "  }\n}\n";
   return o.str();
