@@ -318,6 +318,7 @@ struct Context {
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
   int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel
+  int batch_run_tiles = 16;       // tiles a persistent block claims at once
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int pdl = 1;           // launch generated kernels with programmatic dependent launch
@@ -821,6 +822,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "tuner") {
     if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "tuner must be 0 (off), 1 (exhaustive) or 2 (learned)");
     c.tuner = (int)value;
+  } else if (k == "batch_run_tiles") {
+    if (value < 1 || value > 4096) fail(CC_ERR_INVALID_VALUE, "batch_run_tiles must be in [1, 4096]");
+    c.batch_run_tiles = (int)value;
   } else if (k == "batch_max_registers") {
     if (value < 0 || value > 255) fail(CC_ERR_INVALID_VALUE, "batch_max_registers must be in [0, 255]");
     c.batch_max_registers = (int)value;
@@ -869,6 +873,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "tc_group_m") *value = c.tc_group_m;
   else if (k == "copy_kernel") *value = c.copy_kernel;
   else if (k == "batch_max_registers") *value = c.batch_max_registers;
+  else if (k == "batch_run_tiles") *value = c.batch_run_tiles;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END
 }
@@ -1467,7 +1472,7 @@ namespace {
 constexpr int kBatchBlock = 256;
 constexpr int kBatchUnroll = 4;
 constexpr int64_t kBatchTile = (int64_t)kBatchBlock * 4 * kBatchUnroll;  // floats per tile (4096)
-constexpr int kBatchChunkTiles = 8;  // tiles a persistent block claims at once
+
 
 // The device table entry; must match the struct in the generated module.
 struct BatchEntry {
@@ -1568,23 +1573,22 @@ std::string batch_main_source(size_t n_structs) {
   o << "__device__ cc_tile_fn const cc_tiles[" << n_structs << "] = {\n";
   for (size_t s = 0; s < n_structs; ++s) o << "  cc_tile_" << s << ",\n";
   o << "};\n"
-    // Blocks claim runs of kBatchChunkTiles consecutive tiles from a work
+    // Blocks claim runs of `run` consecutive tiles from a work
     // counter (zeroed before each launch): a block stays in one program's code
     // for a run, and the uneven per-point cost of programs still balances.
     << "extern \"C\" __global__ void __launch_bounds__(" << kBatchBlock
     << ") cc_batch(const cc_entry *__restrict__ table, int nprog, long long total_tiles,\n"
-    << "                unsigned long long *__restrict__ work) {\n"
+    << "                unsigned long long *__restrict__ work, int run) {\n"
     << "  extern __shared__ long long s_begin[];\n"
     << "  __shared__ long long s_run;\n"
     << "  for (int i = threadIdx.x; i < nprog; i += blockDim.x) s_begin[i] = table[i].tile_begin;\n"
     << "  for (;;) {\n"
     << "    __syncthreads();\n"
-    << "    if (threadIdx.x == 0) s_run = (long long)atomicAdd(work, " << kBatchChunkTiles << "ULL);\n"
+    << "    if (threadIdx.x == 0) s_run = (long long)atomicAdd(work, (unsigned long long)run);\n"
     << "    __syncthreads();\n"
     << "    const long long t0 = s_run;\n"
     << "    if (t0 >= total_tiles) break;\n"
-    << "    const long long t1 = t0 + " << kBatchChunkTiles << "LL < total_tiles ? t0 + " << kBatchChunkTiles
-    << "LL : total_tiles;\n"
+    << "    const long long t1 = t0 + run < total_tiles ? t0 + run : total_tiles;\n"
     << "    int lo = 0, hi = nprog - 1;\n"
     << "    while (lo < hi) {\n      const int mid = (lo + hi + 1) >> 1;\n"
     << "      if (s_begin[mid] <= t0) lo = mid; else hi = mid - 1;\n    }\n"
@@ -1844,7 +1848,8 @@ int cc_batch_run(cc_handle batch, int mode, uint64_t stream) {
     long long total = b.total_tiles;
     uint64_t work = table + sizeof(BatchEntry) * b.sid.size();
     check_cuda(cudaMemsetAsync(reinterpret_cast<void *>(work), 0, sizeof(unsigned long long), s), "cudaMemsetAsync");
-    void *args[] = {&table, &nprog, &total, &work};
+    int run = c.batch_run_tiles;
+    void *args[] = {&table, &nprog, &total, &work, &run};
     int64_t cap = (int64_t)c.sm_count * (b.resident > 0 ? b.resident : 4);
     unsigned grid = (unsigned)(b.total_tiles < cap ? b.total_tiles : cap);
     check_cu(g_drv.LaunchKernel(b.persistent, grid, 1, 1, kBatchBlock, 1, 1, (unsigned)(sizeof(int64_t) * nprog),

@@ -98,6 +98,8 @@ int cc_synchronize(void);
  *   "batch_max_registers" batch modules: register cap per thread of every compiled part (0 = none;
  *                       default 128: the indirect calls of the persistent kernel otherwise take the
  *                       largest part's registers and one block per SM)
+ *   "batch_run_tiles"   consecutive 4096-float tiles a block of the persistent batch kernel claims at once
+ *                       (default 16)
  *   "batch_inline"      batch modules: 0 = expressions and exp/log/tanh are called functions,
  *                       1 = expressions inlined, exp/log/tanh called (default), 2 = all inlined
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
