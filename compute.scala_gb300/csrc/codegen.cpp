@@ -253,6 +253,7 @@ struct Frame {
   int id;
   std::vector<std::string> gid;   // index variable names
   std::vector<int64_t> shape;
+  std::vector<int64_t> goff = {};  // constant added to each index variable (empty: none)
 };
 
 // One generated statement.  Index statements are integer view arithmetic (they
@@ -271,6 +272,9 @@ struct Stmt {
   int uparam = -1;
   std::string uoff;
   uint32_t ubits = 0;
+  // Emission order of loads and arithmetic (stable; creation order unless
+  // statements are merged across points, see Generator::set_point).
+  int64_t key = 0;
 };
 
 class Generator {
@@ -291,11 +295,13 @@ class Generator {
     switch (node.kind) {
       case NodeKind::Literal:
         v = fresh();
+        if (reuse("K " + lit_code(node.bits), v)) break;
         add(Cat::Compute, "const float " + v + " = " + lit_code(node.bits) + ";");
         break;
       case NodeKind::Unary: {
         std::string a = gen(node.a, f);
         v = fresh();
+        if (reuse("U " + std::to_string(node.op) + " " + a, v)) break;
         static const char *fn[] = {"-", "expf", "logf", "tanhf", "fabsf", "sqrtf"};
         static const char *shared_fn[] = {"-", "cc_expf", "cc_logf", "cc_tanhf", "fabsf", "sqrtf"};
         if (node.op == (uint8_t)UnOp::Neg)
@@ -319,6 +325,7 @@ class Generator {
           case BinOp::Min: e = "fminf(" + a + ", " + b + ")"; break;
           case BinOp::Max: e = "fmaxf(" + a + ", " + b + ")"; break;
         }
+        if (reuse("B " + e, v)) break;
         add(Cat::Compute, "const float " + v + " = " + e + ";");
         break;
       }
@@ -331,8 +338,8 @@ class Generator {
           add(Cat::Compute, "const float " + v + " = a" + std::to_string(p.param_index) + ";");
           break;
         }
-        std::vector<std::string> idx;
-        std::string ok = index_rows(node, p.dims, f, idx);
+        std::vector<std::string> idx, row_ok;
+        std::string ok = index_rows(node, p.dims, f, idx, &row_ok);
         std::string off = offset_expr(p.dims, idx);
         std::string ptr = "in" + std::to_string(p.param_index) + (p.dims.empty() ? "" : " + " + off);
         // A load whose address depends on no output coordinate reads the same
@@ -343,6 +350,10 @@ class Generator {
           if (!uniform_.count(i)) uniform = false;
         const Cat load_cat = uniform ? Cat::Compute : Cat::Load;
         if (!uniform) varying_params_.insert(p.param_index);
+        if (vec_loads_ && asm_loads_ && merge_ && (!uniform || staged_.count(p.param_index)) &&
+            vector_load(node, p, idx, row_ok, !uniform, v))
+          break;
+        if (reuse("L " + ptr + " " + ok + " " + lit_code(p.bits), v)) break;
         if (ring_ > 0 && !uniform && asm_loads_ && (ok.empty() || p.bits == 0)) {
           // zero padding is the copy's zero fill
           Stmt st{Cat::Load, std::string()};
@@ -351,7 +362,7 @@ class Generator {
           st.ptr = ptr;
           st.ok = ok;
           st.base = "in" + std::to_string(p.param_index);
-          stmts_.push_back(std::move(st));
+          push(std::move(st));
           break;
         }
         if (prefetch_min_bytes_ >= 0) {
@@ -393,6 +404,7 @@ class Generator {
         std::string ok = index_rows(node, node.dims, f, idx);
         Frame inner{next_frame_++, idx, node.dims};
         std::string sub = gen(node.a, inner);
+        if (reuse("V " + ok + " " + sub + " " + lit_code(node.bits), v)) break;
         if (!ok.empty())
           add(Cat::Compute, "const float " + v + " = (" + ok + ") ? " + sub + " : " + lit_code(node.bits) + ";");
         else
@@ -414,11 +426,14 @@ class Generator {
   // float statements still execute in the tree's order.
   void emit(std::ostringstream &os, int ind, int lookahead) const {
     std::string pad(ind, ' ');
+    std::vector<size_t> order(stmts_.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return stmts_[a].key < stmts_[b].key; });
     std::vector<size_t> loads;
-    for (size_t i = 0; i < stmts_.size(); ++i) {
+    for (size_t i = 0; i < stmts_.size(); ++i)
       if (stmts_[i].cat == Cat::Index) os << pad << stmts_[i].text << "\n";
+    for (size_t i : order)
       if (stmts_[i].cat == Cat::Load) loads.push_back(i);
-    }
     for (size_t i = 0; i < stmts_.size(); ++i)
       if (stmts_[i].cat == Cat::Prefetch) os << pad << stmts_[i].text << "\n";
     // Ring loads: issued (cp.async into slot r % ring_) where a register load
@@ -443,7 +458,7 @@ class Generator {
         ++ring_issued;
       }
     };
-    for (size_t i = 0; i < stmts_.size(); ++i) {
+    for (size_t i : order) {
       const Stmt &s = stmts_[i];
       if (s.cat == Cat::Index || s.cat == Cat::Prefetch) continue;
       if (s.cat == Cat::Load) {
@@ -488,39 +503,144 @@ class Generator {
       chosen.insert(st.uparam);
       staged.emplace_back(st.uparam, elems);
     }
+    read_staged(staged);
+    return staged;
+  }
+  // Reads these staged parameters from their shared-memory copies.
+  void read_staged(const std::vector<std::pair<int, int64_t>> &staged) {
+    std::set<int> chosen;
+    for (auto &sp : staged) chosen.insert(sp.first);
     for (Stmt &st : stmts_) {
       if (st.uparam < 0 || !chosen.count(st.uparam)) continue;
       const std::string sp = "cc_sp" + std::to_string(st.uparam) + "[" + st.uoff + "]";
       st.text = "const float " + st.var + " = " +
                 (st.ok.empty() ? sp : "(" + st.ok + ") ? " + sp + " : " + lit_code(st.ubits)) + ";";
     }
-    return staged;
   }
 
   // Stage zero-padded loads that vary per thread through a shared-memory ring
   // of `slots` entries per thread (0: registers only).
   void set_ring(int slots) { ring_ = slots; }
+  // Merge statements with identical right-hand sides (the frames of several
+  // points per thread share index arithmetic, loads and arithmetic).
+  void set_merge(bool on) { merge_ = on; }
+  // Group reads of the same 16 bytes into float4 loads (needs merging on).
+  void set_vector_loads(bool on) { vec_loads_ = on; }
+  // Parameters with shared-memory copies (cc_sp<k>, 16-byte aligned).
+  void set_staged(const std::vector<std::pair<int, int64_t>> &staged) {
+    for (auto &sp : staged) staged_.insert(sp.first);
+  }
+  int vector_loads() const { return vector_loads_; }
+  // Statements generated next belong to point k of `points`: statement i of
+  // every point is ordered as (i, k), so the points advance together.
+  void set_point(int k, int points) {
+    point_ = k;
+    points_ = points;
+    pos_ = 0;
+  }
   int ring_loads() const { return ring_loads_; }
 
   bool uses_fp64() const { return fp64_; }
 
  private:
   std::string fresh() { return "_" + std::to_string(next_var_++); }
-  void add(Cat c, std::string t) { stmts_.push_back(Stmt{c, std::move(t)}); }
+  // With merging on, a statement whose right-hand side (`key`) was emitted
+  // before reuses that variable: `v` becomes its name and true is returned.
+  // The merged statement moves up to where this point would have created it,
+  // so the points' statements interleave (short live ranges) and every
+  // statement still follows its operands.
+  bool reuse(const std::string &key, std::string &v) {
+    if (!merge_) return false;
+    auto it = merged_.find(key);
+    if (it == merged_.end()) {
+      merged_.emplace(key, v);
+      pending_var_ = v;
+      return false;
+    }
+    v = it->second;
+    const int64_t here = pos_++ * points_ + point_;
+    auto s = stmt_of_.find(v);
+    if (s != stmt_of_.end() && stmts_[s->second].key > here) stmts_[s->second].key = here;
+    return true;
+  }
+  void add(Cat c, std::string t) {
+    Stmt st{c, std::move(t)};
+    push(std::move(st));
+  }
+  void push(Stmt st) {
+    st.key = pos_++ * points_ + point_;
+    if (!pending_var_.empty() && st.cat != Cat::Prefetch) {
+      stmt_of_[pending_var_] = stmts_.size();  // the statement defining the last unmerged value
+      pending_var_.clear();
+    }
+    stmts_.push_back(std::move(st));
+  }
+
+  // A read whose innermost index is a constant c, from a parameter whose
+  // innermost extent is a multiple of 4, becomes component c % 4 of a float4
+  // load at c - c % 4 that the other reads of the same group share: one
+  // 16-byte load where a view splits a short innermost axis (channels, say)
+  // into separate reads.  Needs 16-byte aligned inputs (cc_ew_vl).
+  // A thread-independent read of a staged parameter groups the same way into
+  // a float4 read of its (16-byte aligned) shared-memory copy.
+  bool vector_load(const IrNode &node, const IrNode &p, const std::vector<std::string> &idx,
+                   const std::vector<std::string> &row_ok, bool global, std::string &v) {
+    const int r = (int)p.dims.size();
+    const int cols = node.cols;
+    if (r == 0 || p.dims[r - 1] % 4 != 0) return false;
+    for (int x = 0; x < cols - 1; ++x)
+      if (node.m[(size_t)(r - 1) * cols + x] != 0.0) return false;
+    const double c = node.m[(size_t)(r - 1) * cols + cols - 1];
+    if (c < 0.0 || c >= (double)p.dims[r - 1] || c != (double)(int64_t)c) return false;
+    const int64_t ci = (int64_t)c;
+    int64_t total = 1;
+    for (int64_t d : p.dims) total *= d;
+    const bool wide = total >= (int64_t(1) << 31);
+    std::string ok;
+    for (int y = 0; y < r - 1; ++y)
+      if (!row_ok[y].empty()) ok += std::string(ok.empty() ? "" : " && ") + row_ok[y];
+    const std::string D = std::to_string(p.dims[r - 1]) + (wide ? "LL" : "");
+    std::string prefix = r == 1 ? std::string() : offset_expr(std::vector<int64_t>(p.dims.begin(), p.dims.end() - 1),
+                                                                std::vector<std::string>(idx.begin(), idx.end() - 1));
+    std::string off = r == 1 ? std::to_string(ci - ci % 4)
+                             : "(" + std::string(wide ? "(cc_i64)" : "") + prefix + ") * " + D + " + " +
+                                   std::to_string(ci - ci % 4);
+    const std::string ptr = global ? "in" + std::to_string(p.param_index) + " + " + off
+                                   : "reinterpret_cast<const float4 *>(cc_sp" + std::to_string(p.param_index) + ")[(" +
+                                         off + ") / 4]";
+    std::string q = "_q" + std::to_string(next_var_++);
+    if (!reuse("G " + ptr + " " + ok + " " + lit_code(p.bits), q)) {
+      const std::string pad = lit_code(p.bits);
+      const std::string pad4 = "make_float4(" + pad + ", " + pad + ", " + pad + ", " + pad + ")";
+      if (global)
+        add(Cat::Load, "float4 " + q + " = " + pad4 + "; cc_ld4(" + q + ", " + ptr + ", " +
+                           (ok.empty() ? std::string("1") : "(" + ok + ")") + ");");
+      else
+        add(Cat::Compute, "const float4 " + q + " = " + (ok.empty() ? ptr : "(" + ok + ") ? " + ptr + " : " + pad4) +
+                              ";");
+      ++vector_loads_;
+    }
+    // merged through the group, so a merged component moves up only after it
+    const std::string comp = q + "." + "xyzw"[ci % 4];
+    if (!reuse("C " + comp, v)) add(Cat::Compute, "const float " + v + " = " + comp + ";");
+    return true;
+  }
 
   // One index variable per source dimension, the way ArrayView.extract
   // computes it (OpenCLKernelBuilder.scala:348-411); returns the bounds
   // condition ("" when every row is constant-zero and no check applies).
   std::string index_rows(const IrNode &node, const std::vector<int64_t> &dims, const Frame &f,
-                         std::vector<std::string> &idx) {
+                         std::vector<std::string> &idx, std::vector<std::string> *row_ok = nullptr) {
     const int rows = (int)dims.size();
     const int cols = node.cols;
     std::string ok;
     for (int y = 0; y < rows; ++y) {
       std::string sum;
       bool any = false;
+      double c = node.m[(size_t)y * cols + cols - 1];
+      for (int x = 0; x < cols - 1 && !f.goff.empty(); ++x) c += node.m[(size_t)y * cols + x] * (double)f.goff[x];
       for (int x = 0; x < cols; ++x) {
-        double s = node.m[(size_t)y * cols + x];
+        double s = x < cols - 1 ? node.m[(size_t)y * cols + x] : c;
         if (s == 0.0) continue;
         std::string term;
         if (x < cols - 1) {
@@ -532,18 +652,22 @@ class Generator {
         any = true;
       }
       std::string name = "_i" + std::to_string(next_var_++);
-      bool row_uniform = true;
-      for (int x = 0; x < cols - 1; ++x)
-        if (node.m[(size_t)y * cols + x] != 0.0 && !uniform_.count(f.gid[x])) row_uniform = false;
-      if (row_uniform) uniform_.insert(name);
-      if (!any) {
-        add(Cat::Index, "const int " + name + " = 0;");
-        if (dims[y] == 0) ok += std::string(ok.empty() ? "" : " && ") + "false";
-      } else {
-        add(Cat::Index, "const int " + name + " = (int)(" + sum + ");");
-        ok += std::string(ok.empty() ? "" : " && ") + "(" + name + " >= 0) && (" + name + " < " +
-              std::to_string(dims[y]) + ")";
+      const std::string rhs = any ? "(int)(" + sum + ")" : "0";
+      if (!reuse("I " + rhs, name)) {
+        bool row_uniform = true;
+        for (int x = 0; x < cols - 1; ++x)
+          if (node.m[(size_t)y * cols + x] != 0.0 && !uniform_.count(f.gid[x])) row_uniform = false;
+        if (row_uniform) uniform_.insert(name);
+        add(Cat::Index, "const int " + name + " = " + rhs + ";");
       }
+      std::string cond;
+      if (!any) {
+        if (dims[y] == 0) cond = "false";
+      } else {
+        cond = "(" + name + " >= 0) && (" + name + " < " + std::to_string(dims[y]) + ")";
+      }
+      if (!cond.empty()) ok += std::string(ok.empty() ? "" : " && ") + cond;
+      if (row_ok) row_ok->push_back(cond);
       idx.push_back(name);
     }
     return ok;
@@ -576,6 +700,15 @@ class Generator {
   bool fp64_ = false;
   int next_var_ = 0;
   int next_frame_ = 1;
+  bool merge_ = false;
+  bool vec_loads_ = false;
+  std::set<int> staged_;
+  int vector_loads_ = 0;
+  std::map<std::string, std::string> merged_;     // right-hand side -> variable
+  std::map<std::string, size_t> stmt_of_;         // variable -> defining statement
+  std::string pending_var_;
+  int64_t pos_ = 0;  // statement events of the current point
+  int point_ = 0, points_ = 1;
   std::map<std::pair<int, int>, std::string> memo_;
   std::vector<Stmt> stmts_;
   std::set<std::string> uniform_;  // index variables that depend on no output coordinate
@@ -797,6 +930,12 @@ Generated describe_program(const Ir &ir) {
 // thread-independent indices.
 constexpr int64_t kMaxStagedBytes = 16 * 1024;
 
+int points_for(const Ir &ir, int requested) {
+  const int rank = (int)ir.out_shape.size();
+  if (requested <= 1 || rank == 0 || ir.kind != ProgramKind::Elementwise || program_is_contiguous(ir)) return 1;
+  return ir.out_shape[rank - 1] % requested == 0 ? requested : 1;
+}
+
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   Generated g;
   g.n_inputs = ir.n_params;
@@ -870,13 +1009,58 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     fp64 |= gen.uses_fp64();
     if (gen.ring_loads() > 0) ring_slots = opt.smem_ring;
   }
-  std::string stage_code;
-  for (auto &sp : staged) {
-    const std::string k = std::to_string(sp.first), n = std::to_string(sp.second);
-    stage_code += "  __shared__ float cc_sp" + k + "[" + n + "];\n  for (int i_ = threadIdx.x; i_ < " + n +
-                  "; i_ += blockDim.x) cc_sp" + k + "[i_] = __ldg(in" + k + " + i_);\n";
-  }
-  if (!stage_code.empty()) stage_code += "  __syncthreads();\n";
+  // Several consecutive points per thread along the last output dimension
+  // (non-contiguous elementwise programs whose last extent P divides): one
+  // frame per point, the last coordinate offset by k, all generated with
+  // merging, so index rows, loads and arithmetic that do not depend on the
+  // offset (a weight read, say) are emitted once for the P points.
+  const int P = points_for(ir, opt.points_per_thread);
+  g.points_per_thread = P;
+  // Returns the number of float4 loads of the body (`vec`: grouped loads).
+  auto merged_body = [&](bool vec, std::ostringstream &os, std::vector<std::vector<std::string>> &res) {
+    Generator mg(ir, false, opt.asm_loads, opt.prefetch_min_bytes);
+    mg.set_merge(true);
+    mg.set_vector_loads(vec);
+    if (vec) mg.set_staged(staged);
+    decode(os, 4);
+    res.assign(P, {});
+    for (int k = 0; k < P; ++k) {
+      mg.set_point(k, P);
+      Frame fk{-1 - k, f0.gid, ir.out_shape, std::vector<int64_t>(rank, 0)};
+      if (rank > 0) fk.goff[rank - 1] = k;
+      if (root.kind == NodeKind::Tuple) {
+        for (int e : root.elems) res[k].push_back(mg.gen(e, fk));
+      } else {
+        res[k].push_back(mg.gen(ir.root, fk));
+      }
+    }
+    mg.read_staged(staged);
+    mg.emit(os, 4, opt.load_lookahead);
+    fp64 |= mg.uses_fp64();
+    return mg.vector_loads();
+  };
+  std::ostringstream multi;
+  std::vector<std::vector<std::string>> mres;
+  if (P > 1) merged_body(false, multi, mres);
+  // The same with reads of a short innermost axis grouped into float4 loads
+  // (cc_ew_vl, launched when every input is 16-byte aligned).
+  std::ostringstream vl_body;
+  std::vector<std::vector<std::string>> vl_res;
+  if (opt.vector_loads && !contiguous && ir.kind == ProgramKind::Elementwise)
+    g.has_vl = merged_body(true, vl_body, vl_res) > 0;
+  // (cc_ew_vl reads the copies as float4: 16-byte aligned there)
+  auto staging = [&](bool align16) {
+    std::string code;
+    for (auto &sp : staged) {
+      const std::string k = std::to_string(sp.first), n = std::to_string(sp.second);
+      code += std::string("  __shared__ ") + (align16 ? "__align__(16) " : "") + "float cc_sp" + k + "[" + n +
+              "];\n  for (int i_ = threadIdx.x; i_ < " + n + "; i_ += blockDim.x) cc_sp" + k + "[i_] = __ldg(in" + k +
+              " + i_);\n";
+    }
+    if (!code.empty()) code += "  __syncthreads();\n";
+    return code;
+  };
+  const std::string stage_code = staging(false);
   g.uses_fp64_index = fp64;
   g.smem_bytes = ring_slots * opt.block * 4;
   const std::string ring_decl = ring_slots > 0 ? "  extern __shared__ float cc_ring[];\n" : "";
@@ -966,30 +1150,46 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << vec4_loop(ir.n_params, U, false, contig_call)
         << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
   } else if (ir.kind == ProgramKind::Elementwise) {
-    src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_ew(" << params
-        << "float *__restrict__ out, cc_i64 n) {\n" << ring_decl << stage_code
-        << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
-        << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
-        << generic.str();
-    src << "    cc_pdl_gate(cc_early);\n";
-    if (g.tuple_len == 1) {
-      src << "    out[lin] = " << results[0] << ";\n";
-    } else if (g.tuple_len % 4 == 0) {
-      // a point's tuple is tuple_len consecutive floats: float4 stores when aligned
-      src << "    if ((reinterpret_cast<unsigned long long>(out) & 15ull) == 0) {\n"
-          << "      float4 *o4_ = reinterpret_cast<float4 *>(out + lin * " << g.tuple_len << "LL);\n";
-      for (int k = 0; k < g.tuple_len; k += 4)
-        src << "      o4_[" << k / 4 << "] = make_float4(" << results[k] << ", " << results[k + 1] << ", "
-            << results[k + 2] << ", " << results[k + 3] << ");\n";
-      src << "    } else {\n";
-      for (int k = 0; k < g.tuple_len; ++k)
-        src << "      out[lin * " << g.tuple_len << "LL + " << k << "] = " << results[k] << ";\n";
-      src << "    }\n";
-    } else {
-      for (int k = 0; k < g.tuple_len; ++k)
-        src << "    out[lin * " << g.tuple_len << "LL + " << k << "] = " << results[k] << ";\n";
-    }
-    src << "  }\n}\n\n";
+    auto ew_kernel = [&](const std::string &name, const std::string &ring, const std::string &body,
+                         const std::vector<std::vector<std::string>> &point_results) {
+      src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") " << name << "(" << params
+          << "float *__restrict__ out, cc_i64 n) {\n" << ring << (name == "cc_ew_vl" ? staging(true) : stage_code)
+          << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+          << (P > 1 ? "  for (cc_i64 lin = ((cc_i64)blockIdx.x * blockDim.x + threadIdx.x) * " + std::to_string(P) +
+                          "; lin < n; lin += stride * " + std::to_string(P) + ") {\n"
+                    : std::string("  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += "
+                                  "stride) {\n"))
+          << body;
+      src << "    cc_pdl_gate(cc_early);\n";
+      // point `p` of this thread (p = 0 .. P-1) stores `res`
+      auto store = [&](const std::string &p, const std::vector<std::string> &res) {
+        const std::string at = p == "0" ? std::string("lin") : "(lin + " + p + ")";
+        if (g.tuple_len == 1) {
+          src << "    out[" << at << "] = " << res[0] << ";\n";
+        } else if (g.tuple_len % 4 == 0) {
+          // a point's tuple is tuple_len consecutive floats: float4 stores when aligned
+          src << "    if ((reinterpret_cast<unsigned long long>(out) & 15ull) == 0) {\n"
+              << "      float4 *o4_ = reinterpret_cast<float4 *>(out + " << at << " * " << g.tuple_len << "LL);\n";
+          for (int k = 0; k < g.tuple_len; k += 4)
+            src << "      o4_[" << k / 4 << "] = make_float4(" << res[k] << ", " << res[k + 1] << ", " << res[k + 2]
+                << ", " << res[k + 3] << ");\n";
+          src << "    } else {\n";
+          for (int k = 0; k < g.tuple_len; ++k)
+            src << "      out[" << at << " * " << g.tuple_len << "LL + " << k << "] = " << res[k] << ";\n";
+          src << "    }\n";
+        } else {
+          for (int k = 0; k < g.tuple_len; ++k)
+            src << "    out[" << at << " * " << g.tuple_len << "LL + " << k << "] = " << res[k] << ";\n";
+        }
+      };
+      for (int k = 0; k < P; ++k) store(std::to_string(k), point_results[k]);
+      src << "  }\n}\n\n";
+    };
+    if (P > 1)
+      ew_kernel("cc_ew", ring_decl, multi.str(), mres);
+    else
+      ew_kernel("cc_ew", ring_decl, generic.str(), {results});
+    if (g.has_vl) ew_kernel("cc_ew_vl", "", vl_body.str(), vl_res);
     if (contiguous) {
       src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_ew_v4(" << params
           << "float *__restrict__ out, cc_i64 n) {\n"

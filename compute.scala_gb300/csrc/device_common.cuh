@@ -87,6 +87,14 @@ __device__ __forceinline__ void cc_ld(float &v, const float *p, int ok) {
       : "l"(p), "r"(ok));
 }
 
+// Four consecutive floats from a 16-byte aligned address, predicated like cc_ld.
+__device__ __forceinline__ void cc_ld4(float4 &v, const float *p, int ok) {
+  asm volatile(
+      "{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n @q ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%5];\n}\n"
+      : "+f"(v.x), "+f"(v.y), "+f"(v.z), "+f"(v.w)
+      : "r"(ok), "l"(p));
+}
+
 // Programmatic dependent launch (griddepcontrol).  A generated kernel waits
 // until the kernels it depends on have completed and their writes are
 // visible, and only then lets the next kernel in the stream be scheduled, so a

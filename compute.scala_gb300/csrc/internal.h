@@ -89,6 +89,8 @@ struct CodegenOptions {
   int vec_unroll = 4;       // float4 positions per thread per batch in the contiguous kernels
   int64_t prefetch_min_bytes = -1;  // L2-prefetch loads from inputs at least this large (-1: never)
   int smem_ring = 0;        // generic kernels: shared-memory ring slots per thread for staged loads (0: none)
+  int points_per_thread = 1;  // generic elementwise kernels: consecutive points a thread computes together
+  bool vector_loads = false;  // generic elementwise kernels: also cc_ew_vl, with float4 grouped reads
 };
 
 // Minimum resident blocks per SM to request for a generic kernel over `domain`
@@ -97,6 +99,9 @@ struct CodegenOptions {
 // kernel then loops over the domain with a resident grid).  More registers per
 // thread let the compiler keep more loads in flight.
 int choose_min_blocks(int64_t domain, int block, int sm_count, int override_blocks);
+// Points per thread a generic elementwise kernel takes for `requested`: 1 for
+// sums, contiguous programs and last extents that `requested` does not divide.
+int points_for(const Ir &ir, int requested);
 
 struct Generated {
   std::string source;
@@ -109,6 +114,8 @@ struct Generated {
   int vec_unroll = 1;      // positions per thread per batch of the float4 variant
   int smem_bytes = 0;      // dynamic shared memory of the generic kernel (its load ring)
   std::vector<int64_t> param_bytes;  // bytes of each input buffer the kernel may read
+  int points_per_thread = 1;         // of the generic elementwise kernel
+  bool has_vl = false;               // cc_ew_vl exists (float4 grouped reads; 16-byte aligned inputs)
 };
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);

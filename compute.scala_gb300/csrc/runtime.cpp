@@ -187,11 +187,14 @@ struct Module {
   CUmodule module = nullptr;
   CUfunction scalar = nullptr;  // cc_ew / cc_sum
   CUfunction vec4 = nullptr;    // cc_ew_v4 / cc_sum_v4 (contiguous inputs)
+  CUfunction vl = nullptr;      // cc_ew_vl (float4 grouped reads; 16-byte aligned inputs)
   int block = 256;              // threads per block the kernels were generated for
   int resident_scalar = 0;      // blocks one SM holds at once, per variant
   int resident_vec4 = 0;
+  int resident_vl = 0;
   int vec_unroll = 1;
   int smem_bytes = 0;           // dynamic shared memory of the scalar kernel (its load ring)
+  int points = 1;               // consecutive points per thread of the scalar elementwise kernel
   std::string source;
   ~Module() {
     if (module && g_drv.ModuleUnload) g_drv.ModuleUnload(module);
@@ -321,6 +324,8 @@ struct Context {
   int batch_run_tiles = 16;       // tiles a persistent block claims at once
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
+  int ew_points = 1;     // generic elementwise kernels: consecutive points per thread
+  int ew_vector_loads = 1;  // generic elementwise kernels: float4 grouped reads when inputs are aligned
   int pdl = 1;           // launch generated kernels with programmatic dependent launch
   int copy_kernel = 0;   // copies between pinned host memory and the device by the SMs
   // The output range of the last generated kernel launched, and its stream: a
@@ -509,9 +514,11 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   bool aligned = (out & 15u) == 0;
   for (uint64_t a : in) aligned = aligned && (a & 15u) == 0;
   const bool vec = m.vec4 && aligned;
-  CUfunction f = vec ? m.vec4 : m.scalar;
+  const bool vl = !vec && m.vl && aligned;
+  CUfunction f = vec ? m.vec4 : vl ? m.vl : m.scalar;
   // float4 kernels: each thread takes vec_unroll positions per batch
-  const int64_t work = vec ? ((n >> 2) + m.vec_unroll - 1) / m.vec_unroll : n;
+  // (scalar elementwise kernels: `points` consecutive points per thread)
+  const int64_t work = vec ? ((n >> 2) + m.vec_unroll - 1) / m.vec_unroll : (n + m.points - 1) / m.points;
   std::vector<void *> args;
   std::vector<uint64_t> ptrs(in);
   for (auto &v : ptrs) args.push_back(&v);
@@ -527,7 +534,7 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
     grid = (unsigned)sum_grid_for(work, block, c.sm_count * c.sum_blocks_per_sm);
   } else {
     if (n == 0) return;
-    int resident = vec ? m.resident_vec4 : m.resident_scalar;
+    int resident = vec ? m.resident_vec4 : vl ? m.resident_vl : m.resident_scalar;
     if (c.ew_blocks_per_sm > 0 && (resident <= 0 || c.ew_blocks_per_sm < resident)) resident = c.ew_blocks_per_sm;
     grid = (unsigned)ew_grid(work, block, c.sm_count, resident);
   }
@@ -549,7 +556,7 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   c.last_write.lo = out;
   c.last_write.hi = out + (uint64_t)(p.gen.out_elems > 0 ? p.gen.out_elems : 1) * sizeof(float);
   c.last_write.valid = c.pdl != 0;
-  const unsigned smem = vec ? 0 : (unsigned)m.smem_bytes;
+  const unsigned smem = vec || vl ? 0 : (unsigned)m.smem_bytes;
   if (c.pdl) {
     // programmatic dependent launch: this grid may be scheduled while the
     // previous kernel in the stream drains; its cc_pdl_begin / cc_pdl_gate keep the order
@@ -816,6 +823,12 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "pdl") {
     if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "pdl must be 0 or 1");
     c.pdl = (int)value;
+  } else if (k == "ew_vector_loads") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "ew_vector_loads must be 0 or 1");
+    c.ew_vector_loads = (int)value;
+  } else if (k == "ew_points") {
+    if (value < 1 || value > 16) fail(CC_ERR_INVALID_VALUE, "ew_points must be in [1, 16]");
+    c.ew_points = (int)value;
   } else if (k == "ew_smem_ring") {
     if (value != 0 && (value < 4 || value > 64)) fail(CC_ERR_INVALID_VALUE, "ew_smem_ring must be 0 or in [4, 64]");
     c.ew_smem_ring = (int)value;
@@ -869,6 +882,8 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "batch_inline") *value = c.batch_inline;
   else if (k == "tuner") *value = c.tuner;
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
+  else if (k == "ew_points") *value = c.ew_points;
+  else if (k == "ew_vector_loads") *value = c.ew_vector_loads;
   else if (k == "pdl") *value = c.pdl;
   else if (k == "tc_group_m") *value = c.tc_group_m;
   else if (k == "copy_kernel") *value = c.copy_kernel;
@@ -1050,10 +1065,12 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     opt.vec_unroll = c.vec_unroll;
     opt.prefetch_min_bytes = c.prefetch_min_bytes;
     opt.smem_ring = c.ew_smem_ring;
+    opt.points_per_thread = c.ew_points;
+    opt.vector_loads = c.ew_vector_loads != 0;
   }
   key += "#lookahead " + std::to_string(opt.load_lookahead) + " asm " + std::to_string((int)opt.asm_loads) +
          " blocks " + std::to_string(-opt.min_blocks) + " block " + std::to_string(opt.block) + " unroll " + std::to_string(opt.vec_unroll) +
-         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " ring " + std::to_string(opt.smem_ring) +
+         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " ring " + std::to_string(opt.smem_ring) + " points " + std::to_string(opt.points_per_thread) + " vl " + std::to_string((int)opt.vector_loads) +
          " sumblock " + std::to_string(c.sum_block) +
          " contraction " + std::to_string(c.contraction) + " tc " + std::to_string(c.tc_variant) + " tuner " +
          std::to_string(c.tuner) + "\n";
@@ -1134,7 +1151,9 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     skey += key.substr(key.rfind('#'));
     opt.min_blocks = 0;
   } else {
-    opt.min_blocks = choose_min_blocks(domain, opt.block, c.sm_count, -opt.min_blocks);
+    // threads, not points: a thread of a multi-point kernel takes several
+    opt.min_blocks = choose_min_blocks(domain / points_for(ir, opt.points_per_thread), opt.block, c.sm_count,
+                                       -opt.min_blocks);
   }
   auto p = std::make_unique<Program>();
   p->kind = ir.kind;
@@ -1156,9 +1175,11 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     const char *vname = ir.kind == ProgramKind::Sum ? "cc_sum_v4" : "cc_ew_v4";
     check_cu(g_drv.ModuleGetFunction(&mod->scalar, mod->module, sname), "cuModuleGetFunction");
     if (p->gen.has_vec4) check_cu(g_drv.ModuleGetFunction(&mod->vec4, mod->module, vname), "cuModuleGetFunction");
+    if (p->gen.has_vl) check_cu(g_drv.ModuleGetFunction(&mod->vl, mod->module, "cc_ew_vl"), "cuModuleGetFunction");
     mod->block = opt.block;
     mod->vec_unroll = p->gen.vec_unroll;
     mod->smem_bytes = p->gen.smem_bytes;
+    mod->points = p->gen.points_per_thread;
     if (mod->smem_bytes > 48 * 1024)
       check_cu(g_drv.FuncSetAttribute(mod->scalar, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, mod->smem_bytes),
                "cuFuncSetAttribute");
@@ -1166,6 +1187,9 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
              "cuOccupancyMaxActiveBlocks");
     if (mod->vec4)
       check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_vec4, mod->vec4, mod->block, 0),
+               "cuOccupancyMaxActiveBlocks");
+    if (mod->vl)
+      check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_vl, mod->vl, mod->block, 0),
                "cuOccupancyMaxActiveBlocks");
     if (!skey.empty()) {
       std::lock_guard<std::recursive_mutex> g(c.mu);
@@ -1200,6 +1224,8 @@ CodegenOptions parse_codegen_options(const char *text) {
     else if (k == "unroll") o.vec_unroll = (int)v;
     else if (k == "min_blocks") o.min_blocks = (int)v;
     else if (k == "asm") o.asm_loads = v != 0;
+    else if (k == "points") o.points_per_thread = (int)v;
+    else if (k == "vl") o.vector_loads = v != 0;
     else fail(CC_ERR_INVALID_VALUE, "unknown code-generation option '" + k + "'");
   }
   return o;

@@ -93,6 +93,12 @@ int cc_synchronize(void);
  *                       before its first memory access, so results and ordering are unchanged
  *   "ew_smem_ring"      generic kernels: per-thread slots of a shared-memory ring through which loads
  *                       with zero padding are staged by cp.async (0 = loads into registers; 4..64)
+ *   "ew_vector_loads"   1 (default) = generic elementwise kernels whose reads of a constant innermost index
+ *                       (a channel split) group into 16-byte loads also get cc_ew_vl, launched when
+ *                       every input and the output are 16-byte aligned (bit-identical); 0 = cc_ew only
+ *   "ew_points"         generic elementwise kernels: consecutive points per thread along the last output
+ *                       dimension (when it divides that extent), with index arithmetic, loads and
+ *                       arithmetic common to the points done once (1 = one point; default 1; 1..16)
  *   "tuner"             0 = generated kernels with the fixed launch shape (default), 1 = exhaustive
  *                       tuner, 2 = learned tuner (see the tuner section)
  *   "batch_max_registers" batch modules: register cap per thread of every compiled part (0 = none;
@@ -156,7 +162,9 @@ int cc_program_cache_stats(uint64_t *hits, uint64_t *misses, uint64_t *entries);
 int cc_codegen(const char *ir, size_t ir_len, char *buf, size_t len, size_t *needed);
 int cc_compile_check(const char *ir, size_t ir_len, int cc_major, int cc_minor, uint32_t flags);
 /* The same with code-generation options as "key=value" words (NULL = defaults):
- * block, lookahead, ring (shared-memory ring slots), unroll, min_blocks, asm. */
+ * block, lookahead, ring (shared-memory ring slots), unroll, min_blocks, asm,
+ * points (consecutive points per thread of a generic elementwise kernel),
+ * vl (1: also the float4 grouped-read kernel cc_ew_vl). */
 int cc_codegen_with(const char *ir, size_t ir_len, const char *options, char *buf, size_t len, size_t *needed);
 int cc_compile_check_with(const char *ir, size_t ir_len, int cc_major, int cc_minor, uint32_t flags,
                           const char *options);

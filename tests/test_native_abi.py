@@ -181,3 +181,51 @@ def test_merged_subexpressions_keep_the_oracle_bits():
     a = interp.evaluate(merged, m_in)
     b_ = interp.evaluate(unmerged, u_in)
     assert np.array_equal(a.view(np.int32), b_.view(np.int32))
+
+
+def test_points_per_thread_codegen():
+    """Two points per thread of the 3x3 convolution: the x reads the two points
+    share and the weight reads are emitted once; a last extent the point count
+    does not divide keeps the one-point kernel."""
+    import bench
+    from compute import Tensors, runtime, trees
+    from compute.tensors import NonInlineTensor
+    d = Tensors(device=0)
+    x, w, b = (NonInlineTensor(d, s, 0.0, None) for s in [(4, 16, 16, 8), (3, 3, 8, 8), (8,)])
+    parts = bench.conv_expr(d.Tensor, x, w, b, parts=True)
+    text = d.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape).text
+    one = runtime.codegen(text)
+    two = runtime.codegen(text, "points=2")
+    assert runtime.codegen(text, "points=1") == one
+    assert runtime.codegen(text, "points=3") == one  # 16 % 3 != 0
+    # 9 offsets x 8 channels of x per point; two points along w share 2 of 3 columns
+    assert one.count("cc_ld(_") == 72 and two.count("cc_ld(_") == 96
+    assert one.count("cc_sp2[") == two.count("cc_sp2[") == 2 + 576  # declaration, copy, reads
+    assert "* 2; lin < n; lin += stride * 2)" in two
+    runtime.compile_check(text, options="points=2")
+
+
+def test_vector_load_codegen():
+    """Reads of the 8 channels of a pixel (NHWC, constant innermost index)
+    become two float4 loads per pixel in cc_ew_vl; cc_ew keeps scalar reads."""
+    import bench
+    from compute import Tensors, runtime, trees
+    from compute.tensors import NonInlineTensor
+    d = Tensors(device=0)
+    x, w, b = (NonInlineTensor(d, s, 0.0, None) for s in [(4, 16, 16, 8), (3, 3, 8, 8), (8,)])
+    parts = bench.conv_expr(d.Tensor, x, w, b, parts=True)
+    text = d.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape).text
+    assert "cc_ew_vl" not in runtime.codegen(text)
+    src = runtime.codegen(text, "vl=1")
+    scalar, vl = src.split("cc_ew_vl(")
+    assert scalar.count("cc_ld(_") == 72 and "cc_ld4(_" not in scalar
+    assert vl.count("cc_ld4(_") == 18 and "cc_ld(_" not in vl  # 9 offsets x 2 groups of 4 channels
+    # the staged weights (filters innermost) and bias as float4 shared reads: 9 x 8 x 2 + 2
+    assert vl.count("reinterpret_cast<const float4 *>(cc_sp") == 146
+    assert "__align__(16) float cc_sp2[576]" in vl and "__align__" not in scalar
+    assert runtime.codegen(text, "vl=1 points=2").split("cc_ew_vl(")[1].count("cc_ld4(_") == 24
+    runtime.compile_check(text, options="vl=1 points=2")
+    # a view whose innermost index varies with the output has nothing to group
+    y = NonInlineTensor(d, (6, 8), 0.0, None)
+    t = y.translate([0, 1]) + y
+    assert "cc_ew_vl" not in runtime.codegen(d.serialize(t.closure, t.shape).text, "vl=1")
