@@ -196,9 +196,10 @@ __device__ __forceinline__ void tile_origin(int tile, int tiles_m, int tiles_n, 
   tn = in / rows;
 }
 
-// The six (A plane, B plane) products, largest first.
-__device__ __constant__ int kProdA[6] = {0, 0, 1, 1, 0, 2};
-__device__ __constant__ int kProdB[6] = {0, 1, 0, 1, 2, 0};
+// The six (A plane, B plane) products, largest first: (0,0) (0,1) (1,0) (1,1)
+// (0,2) (2,0).  Compile-time functions, so the unrolled issue loop folds them.
+__host__ __device__ constexpr int prod_a(int p) { return p == 2 || p == 3 ? 1 : p == 5 ? 2 : 0; }
+__host__ __device__ constexpr int prod_b(int p) { return p == 1 || p == 3 ? 1 : p == 4 ? 2 : 0; }
 
 template <int BN, int STAGES, int ACC_BUFS, int KC>
 __global__ void __launch_bounds__(threads_for(KC), 1)
@@ -321,17 +322,21 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
               break;
             }
             tc_fence_after();
-            const uint32_t sbase = base + stage * kStageBytes;
+            // One descriptor per stage; each operand's is that plus a constant
+            // (16-byte units: shared addresses stay below 256 KiB, so the
+            // 14-bit start-address field never carries).
+            const uint64_t sdesc = smem_desc(base + stage * kStageBytes);
+            const uint32_t fresh = kb == kb0 ? 1u : 0u;
 #pragma unroll
             for (int k16 = 0; k16 < BK / 16; ++k16) {
 #pragma unroll
               for (int prod = 0; prod < 6; ++prod) {
-                const uint64_t adesc = smem_desc(sbase + kProdA[prod] * kAPlaneBytes + k16 * 32);
+                const uint64_t adesc = sdesc + (uint64_t)((prod_a(prod) * kAPlaneBytes + k16 * 32) >> 4);
                 const uint64_t bdesc =
-                    smem_desc(sbase + 3 * kAPlaneBytes + kProdB[prod] * kBPlaneBytes + k16 * 32);
-                const bool fresh = kb == kb0 && k16 == 0;
-                const bool first = prod == 0 ? fresh : (fresh && prod == 1);
-                mma_bf16(prod == 0 ? d_big : d_small, adesc, bdesc, Cfg::kIdesc, first ? 0u : 1u);
+                    sdesc + (uint64_t)((3 * kAPlaneBytes + prod_b(prod) * kBPlaneBytes + k16 * 32) >> 4);
+                // the first product into each accumulator of a chunk overwrites it
+                const uint32_t overwrite = (k16 == 0 && (prod == 0 || prod == 1)) ? fresh : 0u;
+                mma_bf16(prod == 0 ? d_big : d_small, adesc, bdesc, Cfg::kIdesc, overwrite ^ 1u);
               }
             }
             mma_commit(bar_empty + 8 * stage);  // the stage is free once these MMAs have read it
