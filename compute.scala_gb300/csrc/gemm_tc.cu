@@ -23,6 +23,12 @@
 //               32-lane quarter of TMEM), add, store to C, release the pair;
 //               kernels that sum K chunks in registers have a second group,
 //               warps 6..9, and each group takes half of the columns.
+// With one accumulator pair of 256 columns (TMEM holds no second pair) and K
+// chunks, only hi*hi restarts per chunk: the five small products, 2^-8 of it
+// and smaller, accumulate over the whole K (their rounding stays far below
+// the chunked hi*hi's), and at a chunk boundary the MMA thread issues the next
+// k-block's small products before it waits for the epilogue to drain hi*hi, so
+// the drain overlaps tensor work.
 // Every mbarrier wait gives up after kWaitNs of %globaltimer time: it records
 // an error code in *err, raises the CTA's abort flag, and all roles leave their
 // loops, so the CTA still frees its TMEM and returns.
@@ -54,15 +60,19 @@ struct TcCfg {
   static constexpr int kBPlaneBytes = BN * BK * 2;
   static constexpr int kStageBytes = 3 * kAPlaneBytes + 3 * kBPlaneBytes;
   // Shared memory after the stage ring (offsets from the 1 KiB-aligned base):
-  // full[STAGES], empty[STAGES], acc_full[ACC_BUFS], acc_empty[ACC_BUFS], drain.
+  // full[STAGES], empty[STAGES], acc_full[ACC_BUFS], acc_empty[ACC_BUFS], drain,
+  // big_full, big_empty (kernels whose hi*hi chunks drain separately).
   static constexpr int kBarOffset = STAGES * kStageBytes;
-  static constexpr int kNumBars = 2 * STAGES + 2 * ACC_BUFS + 1;
+  static constexpr int kNumBars = 2 * STAGES + 2 * ACC_BUFS + 3;
   static constexpr int kTmemSlotOffset = kBarOffset + kNumBars * 8;
   static constexpr int kAbortOffset = kTmemSlotOffset + 4;
   static constexpr int kSmemBytes = kAbortOffset + 4 + 1024;  // + slack to align the base to 1 KiB
   // Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, M=128, N=BN.
   static constexpr uint32_t kIdesc =
       (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  // The same with N = BN / 2 (a tile split into column halves).
+  static constexpr uint32_t kIdescHalf =
+      (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 4) << 17) | ((uint32_t)(BM >> 4) << 24);
   static_assert(kSmemBytes <= 232448, "shared memory");
 };
 
@@ -196,6 +206,24 @@ __device__ __forceinline__ void tile_origin(int tile, int tiles_m, int tiles_n, 
   tn = in / rows;
 }
 
+// Work item `item` of a persistent grid whose last tiles run as two column
+// halves: items below `full` are whole tiles, then two per remaining tile, so
+// the last round of a grid that does not divide the tiles is half as long.
+// half: -1 for a whole tile, else 0 or 1.
+__device__ __forceinline__ void item_origin(int item, int full, int tiles_m, int tiles_n, int group_m, int bn,
+                                            int &m0, int &n0, int &half) {
+  int tile = item;
+  half = -1;
+  if (item >= full) {
+    tile = full + ((item - full) >> 1);
+    half = (item - full) & 1;
+  }
+  int tm, tn;
+  tile_origin(tile, tiles_m, tiles_n, group_m, tm, tn);
+  m0 = tm * BM;
+  n0 = tn * bn + (half > 0 ? bn / 2 : 0);
+}
+
 // The six (A plane, B plane) products, largest first: (0,0) (0,1) (1,0) (1,1)
 // (0,2) (2,0).  Compile-time functions, so the unrolled issue loop folds them.
 __host__ __device__ constexpr int prod_a(int p) { return p == 2 || p == 3 ? 1 : p == 5 ? 2 : 0; }
@@ -206,8 +234,9 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
     gemm_bf16x6_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
                        const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap tb0,
                        const __grid_constant__ CUtensorMap tb1, const __grid_constant__ CUtensorMap tb2,
-                       float *__restrict__ C, int M, int N, long long ldc, int num_kb, int tiles_n, int num_tiles,
-                       int group_m, int *err) {
+                       const __grid_constant__ CUtensorMap th0, const __grid_constant__ CUtensorMap th1,
+                       const __grid_constant__ CUtensorMap th2, float *__restrict__ C, int M, int N, long long ldc,
+                       int num_kb, int tiles_n, int num_tiles, int full_tiles, int group_m, int *err) {
   using Cfg = TcCfg<BN, STAGES, ACC_BUFS>;
   constexpr int kStages = STAGES;
   constexpr int kStageBytes = Cfg::kStageBytes;
@@ -220,6 +249,13 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
   const uint32_t bar_accfull = bar_empty + 8 * kStages;        // + 8*a
   const uint32_t bar_accempty = bar_accfull + 8 * ACC_BUFS;    // + 8*a
   const uint32_t bar_drain = bar_accempty + 8 * ACC_BUFS;
+  const uint32_t bar_bigfull = bar_drain + 8;   // (late-small kernels) a hi*hi chunk is complete
+  const uint32_t bar_bigempty = bar_drain + 16; // (late-small kernels) the epilogue has read it
+  // One 256-column pair and K chunks: hi*hi drains per chunk, the rest per tile.
+  constexpr bool kLate = ACC_BUFS == 1 && KC > 0;
+  // items: whole tiles, then column halves of the rest (only kLate kernels are given full_tiles < num_tiles)
+  const int num_items = full_tiles + 2 * (num_tiles - full_tiles);
+  const int tiles_m = num_tiles / tiles_n;
   volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(smem + Cfg::kTmemSlotOffset);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + Cfg::kAbortOffset);
 
@@ -235,6 +271,8 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
       mbar_init(bar_accempty + 8 * a, 128 * epilogue_groups(KC));
     }
     mbar_init(bar_drain, 1);
+    mbar_init(bar_bigfull, 1);
+    mbar_init(bar_bigempty, 128 * epilogue_groups(KC));
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -254,6 +292,7 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
     if (lane == 0) {
       const CUtensorMap *ta[3] = {&ta0, &ta1, &ta2};
       const CUtensorMap *tb[3] = {&tb0, &tb1, &tb2};
+      const CUtensorMap *th[3] = {&th0, &th1, &th2};  // B planes, half-width boxes
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
@@ -261,10 +300,12 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
       bool filled[kStages];
 #pragma unroll
       for (int s = 0; s < kStages; ++s) filled[s] = false;
-      for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
-        int tm, tn;
-        tile_origin(tile, num_tiles / tiles_n, tiles_n, group_m, tm, tn);
-        const int m0 = tm * BM, n0 = tn * BN;
+      for (int item = blockIdx.x; item < num_items && ok; item += gridDim.x) {
+        int m0, n0, half;
+        item_origin(item, full_tiles, tiles_m, tiles_n, group_m, BN, m0, n0, half);
+        const CUtensorMap *const *tbs = half < 0 ? tb : th;
+        // a half tile fills the first half of each B plane slot
+        const uint32_t bytes = half < 0 ? (uint32_t)kStageBytes : (uint32_t)(3 * kAPlaneBytes + 3 * (kBPlaneBytes / 2));
         for (int kb = 0; kb < num_kb; ++kb) {
           if (!mbar_wait(bar_empty + 8 * stage, phase ^ 1u, abort_flag, err, 1)) {
             ok = false;
@@ -273,12 +314,12 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
           const uint32_t sbase = base + stage * kStageBytes;
           filled[stage] = true;
           fill_parity[stage] = phase;
-          mbar_arrive_expect_tx(bar_full + 8 * stage, kStageBytes);
+          mbar_arrive_expect_tx(bar_full + 8 * stage, bytes);
 #pragma unroll
           for (int p = 0; p < 3; ++p) tma_load_2d(sbase + p * kAPlaneBytes, ta[p], kb * BK, m0, bar_full + 8 * stage);
 #pragma unroll
           for (int p = 0; p < 3; ++p)
-            tma_load_2d(sbase + 3 * kAPlaneBytes + p * kBPlaneBytes, tb[p], kb * BK, n0, bar_full + 8 * stage);
+            tma_load_2d(sbase + 3 * kAPlaneBytes + p * kBPlaneBytes, tbs[p], kb * BK, n0, bar_full + 8 * stage);
           if (++stage == kStages) {
             stage = 0;
             phase ^= 1u;
@@ -299,7 +340,68 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
     }
     __syncwarp();
   } else if (warp == 1) {
-    if (lane == 0) {
+    if (lane == 0 && kLate) {
+      int stage = 0;
+      uint32_t phase = 0, small_phase = 0, big_phase = 0;
+      bool ok = true;
+      const uint32_t d_big = tmem_base, d_small = tmem_base + BN;
+      for (int item = blockIdx.x; item < num_items && ok; item += gridDim.x) {
+        int m0, n0, half;
+        item_origin(item, full_tiles, tiles_m, tiles_n, group_m, BN, m0, n0, half);
+        const uint32_t idesc = half < 0 ? Cfg::kIdesc : Cfg::kIdescHalf;
+        for (int kb = 0; kb < num_kb; ++kb) {
+          if (!mbar_wait(bar_full + 8 * stage, phase, abort_flag, err, 3)) {
+            ok = false;
+            break;
+          }
+          if (kb == 0 && !mbar_wait(bar_accempty, small_phase ^ 1u, abort_flag, err, 2)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint64_t sdesc = smem_desc(base + stage * kStageBytes);
+#pragma unroll
+          for (int k16 = 0; k16 < BK / 16; ++k16) {
+#pragma unroll
+            for (int prod = 1; prod < 6; ++prod) {
+              const uint64_t adesc = sdesc + (uint64_t)((prod_a(prod) * kAPlaneBytes + k16 * 32) >> 4);
+              const uint64_t bdesc =
+                  sdesc + (uint64_t)((3 * kAPlaneBytes + prod_b(prod) * kBPlaneBytes + k16 * 32) >> 4);
+              mma_bf16(d_small, adesc, bdesc, idesc, (kb == 0 && k16 == 0 && prod == 1) ? 0u : 1u);
+            }
+          }
+          const bool chunk_start = kb % KC == 0;
+          if (chunk_start) {
+            if (!mbar_wait(bar_bigempty, big_phase ^ 1u, abort_flag, err, 2)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+          }
+#pragma unroll
+          for (int k16 = 0; k16 < BK / 16; ++k16) {
+            const uint64_t adesc = sdesc + (uint64_t)((k16 * 32) >> 4);
+            const uint64_t bdesc = sdesc + (uint64_t)((3 * kAPlaneBytes + k16 * 32) >> 4);
+            mma_bf16(d_big, adesc, bdesc, idesc, (chunk_start && k16 == 0) ? 0u : 1u);
+          }
+          mma_commit(bar_empty + 8 * stage);
+          if (++stage == kStages) {
+            stage = 0;
+            phase ^= 1u;
+          }
+          if ((kb + 1) % KC == 0 || kb + 1 == num_kb) {
+            mma_commit(bar_bigfull);  // this hi*hi chunk is complete
+            big_phase ^= 1u;
+          }
+        }
+        if (!ok) break;
+        mma_commit(bar_accfull);  // the small products of the tile are complete
+        small_phase ^= 1u;
+      }
+      mma_commit(bar_drain);
+      const unsigned long long t0 = globaltimer();
+      while (!mbar_try_wait(bar_drain, 0) && globaltimer() - t0 < kWaitNs) __nanosleep(64);
+    } else if (lane == 0) {
       int stage = 0, acc = 0;
       uint32_t phase = 0, acc_phase = 0;
       bool ok = true;
@@ -366,7 +468,59 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
     int acc = 0;
     uint32_t acc_phase = 0;
     const uint32_t lane_tmem = tmem_base + ((uint32_t)(quarter * 32) << 16);
-    if constexpr (KC == 0) {
+    if constexpr (kLate) {
+      // hi*hi per chunk into a running sum of the row; the small products once
+      // per tile, added last.
+      const int nchunks = (num_kb + KC - 1) / KC;
+      constexpr int kCols = BN / epilogue_groups(KC);  // columns of a group in a whole tile
+      const int group = (warp - 2) >> 2;
+      uint32_t big_phase = 0, small_phase = 0;
+      bool ok = true;
+      for (int item = blockIdx.x; item < num_items && ok; item += gridDim.x) {
+        int m0, n0, half;
+        item_origin(item, full_tiles, tiles_m, tiles_n, group_m, BN, m0, n0, half);
+        const int cols = half < 0 ? kCols : kCols / 2;  // this group's columns of the item
+        const int col0 = group * cols;
+        float sum[kCols];
+#pragma unroll
+        for (int j = 0; j < kCols; ++j) sum[j] = 0.0f;
+        for (int ch = 0; ch < nchunks; ++ch) {
+          if (!mbar_wait(bar_bigfull, big_phase, abort_flag, err, 4)) {
+            ok = false;
+            break;
+          }
+          big_phase ^= 1u;
+          tc_fence_after();
+#pragma unroll
+          for (int c32 = 0; c32 < kCols / 32; ++c32) {
+            if (c32 * 32 >= cols) break;
+            float v[32];
+            tmem_ld32(lane_tmem + (uint32_t)(col0 + c32 * 32), v);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) sum[c32 * 32 + j] = __fadd_rn(sum[c32 * 32 + j], v[j]);
+          }
+          tc_fence_before();
+          mbar_arrive(bar_bigempty);
+        }
+        if (!ok) break;
+        if (!mbar_wait(bar_accfull, small_phase, abort_flag, err, 4)) break;
+        small_phase ^= 1u;
+        tc_fence_after();
+        const int row = m0 + row_in_tile;
+        float *crow = C + (long long)row * ldc;
+#pragma unroll
+        for (int c32 = 0; c32 < kCols / 32; ++c32) {
+          if (c32 * 32 >= cols) break;
+          float w[32];
+          tmem_ld32(lane_tmem + (uint32_t)(BN + col0 + c32 * 32), w);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) w[j] = __fadd_rn(sum[c32 * 32 + j], w[j]);
+          store_row_chunk(crow, row, M, N, ldc, n0 + col0 + c32 * 32, w);
+        }
+        tc_fence_before();
+        mbar_arrive(bar_accempty);
+      }
+    } else if constexpr (KC == 0) {
       // One accumulator pair per tile: add the pair and store, 32 columns at a time.
       for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x) {
         if (!mbar_wait(bar_accfull + 8 * acc, acc_phase, abort_flag, err, 4)) break;
@@ -463,15 +617,20 @@ cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int 
   const int num_tiles = tiles_m * tiles_n;
   const int num_kb = K_padded / BK;
   const int grid = num_tiles < sm_count ? num_tiles : sm_count;
+  // Kernels with one 256-column accumulator pair and K chunks split the tiles
+  // of a last, partial round into column halves when those fit one round.
+  int full = num_tiles;
+  const int rem = num_tiles % grid;
+  if (ACC_BUFS == 1 && KC > 0 && num_tiles > grid && rem > 0 && 2 * rem <= grid) full = num_tiles - rem;
   gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS, KC><<<grid, threads_for(KC), Cfg::kSmemBytes, stream>>>(
-      maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], C, M, N, ldc, num_kb, tiles_n, num_tiles,
-      group_m < 1 ? 1 : group_m, err);
+      maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], maps[6], maps[7], maps[8], C, M, N, ldc, num_kb,
+      tiles_n, num_tiles, full, group_m < 1 ? 1 : group_m, err);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-int gemm_tc_box_n(int variant) { return variant == 1 ? 256 : 128; }
+int gemm_tc_box_n(int variant) { return variant == 1 || variant == 5 ? 256 : 128; }
 
 cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
                                int sm_count, int *err, int variant, int group_m, cudaStream_t stream) {
@@ -480,6 +639,8 @@ cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, 
   // kernel computes the same without the running sum's registers.
   const int num_kb = K_padded / BK;
   if ((variant == 0 && num_kb <= 4) || (variant == 3 && num_kb <= 8) || (variant == 4 && num_kb <= 16)) variant = 2;
+  if (variant == 5 && num_kb <= 8) variant = 1;
+  if (variant == 5) return launch_variant<256, 3, 1, 8>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   if (variant == 1) return launch_variant<256, 3, 1, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   if (variant == 2) return launch_variant<128, 4, 2, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   if (variant == 3) return launch_variant<128, 4, 2, 8>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);

@@ -317,7 +317,7 @@ struct Context {
   int vec_unroll = 4;
   int64_t prefetch_min_bytes = -1;
   int sum_block = 256;
-  int tc_variant = 3;  // 128x128 tiles, accumulators restarted every 256 of K
+  int tc_variant = 5;  // 128x256 tiles, hi*hi restarted every 256 of K
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
   int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel
@@ -471,12 +471,14 @@ void run_gemm(Context &c, const float *A, const float *B, float *C, int m, int n
   cudaError_t e = launch_split_a(A, lda, m, k, static_cast<__nv_bfloat16 *>(pa), Mp, Kp, c.sm_count, s);
   if (e == cudaSuccess) e = launch_split_bt(B, ldb, k, n, static_cast<__nv_bfloat16 *>(pb), Np, Kp, s);
   if (e == cudaSuccess) {
-    CUtensorMap maps[6];
+    CUtensorMap maps[9];
     const size_t plane_a = (size_t)Mp * Kp * 2, plane_b = (size_t)Np * Kp * 2;
     try {
       for (int p = 0; p < 3; ++p) {
         encode_plane_map(&maps[p], static_cast<char *>(pa) + p * plane_a, Mp, Kp, kTcBM);
         encode_plane_map(&maps[3 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp, gemm_tc_box_n(c.tc_variant));
+        encode_plane_map(&maps[6 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp,
+                         gemm_tc_box_n(c.tc_variant) / 2);
       }
     } catch (...) {
       c.pool.release(pa, cls_a);
@@ -848,7 +850,7 @@ int cc_config_set(const char *key, int64_t value) {
     if (value < 0 || value > 3) fail(CC_ERR_INVALID_VALUE, "contraction must be in [0, 3]");
     c.contraction = (int)value;
   } else if (k == "tc_variant") {
-    if (value < 0 || value > 4) fail(CC_ERR_INVALID_VALUE, "tc_variant must be in [0, 4]");
+    if (value < 0 || value > 5) fail(CC_ERR_INVALID_VALUE, "tc_variant must be in [0, 5]");
     c.tc_variant = (int)value;
   } else if (k == "vec_unroll") {
     if (value < 1 || value > 8) fail(CC_ERR_INVALID_VALUE, "vec_unroll must be in [1, 8]");

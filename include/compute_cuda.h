@@ -111,7 +111,9 @@ int cc_synchronize(void);
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
  *                       registers (error ~1.6e-7 at any K), 1 = 128x256 tiles, one accumulator
  *                       per tile (error grows with K), 2 = 128x128, one per tile, 3 = as 0 with
- *                       chunks of 256 (default: ~2.4e-7), 4 = chunks of 512 (~4.7e-7)
+ *                       chunks of 256 (~2.4e-7), 4 = chunks of 512 (~4.7e-7), 5 (default) =
+ *                       128x256 tiles, hi*hi in chunks of 256, the five small products over
+ *                       the whole K (~2.5e-7)
  *   "vec_unroll"        float4 positions a thread of a contiguous kernel loads before computing (1..8; default 4)
  * Unknown keys or values out of range return CC_ERR_INVALID_VALUE. */
 int cc_config_set(const char *key, int64_t value);

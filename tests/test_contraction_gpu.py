@@ -85,6 +85,31 @@ def test_split_bf16_tensor_core_mode(cuda_device, shape):
     b.close()
 
 
+@pytest.mark.parametrize("variant", [3, 4, 5])
+@pytest.mark.parametrize("shape", [(300, 100, 700), (1024, 1024, 1024), (512, 4096, 768), (200, 1000, 520),
+                                   (2560, 512, 2048), (2500, 600, 2000)])
+def test_tensor_core_kernel_variants(cuda_device, variant, shape):
+    """Every K-chunked kernel (128-column tiles restarting every 256 / 512 of K;
+    256-column tiles restarting hi*hi every 256 of K) within the error bar, on
+    ragged shapes and on K long enough for many chunks.  The last two shapes
+    have 160 256-column tiles, more than one round of 152 SMs, so variant 5
+    runs its last 8 tiles as column halves (ragged ones in the second)."""
+    rt = cuda_device.runtime
+    m, k, n = shape
+    a, b = _operands(cuda_device, m, k, n)
+    saved = rt.config_get("tc_variant")
+    try:
+        rt.config_set("tc_variant", variant)
+        c = _run(cuda_device, a, b, m, k, n, 2)
+    finally:
+        rt.config_set("tc_variant", saved)
+    ref = a.flatArray().reshape(m, k).astype(np.float64) @ b.flatArray().reshape(k, n).astype(np.float64)
+    err = rel_fro(c, ref)
+    assert err <= 1e-6, err
+    a.close()
+    b.close()
+
+
 def _api_matmul(device, m1, m2):
     """TensorsSpec.scala:472-478, through the Tensor API."""
     i, j = m1.shape
