@@ -146,6 +146,7 @@ _SIGNATURES = {
     "cc_gemm_f32": [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                     ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64],
     "cc_device_errors": [ctypes.POINTER(ctypes.c_int)],
+    "cc_probe_bounded_wait": [ctypes.c_uint64, ctypes.c_int],
     "cc_batch_create": [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(c_size), ctypes.c_int, ctypes.POINTER(c_handle)],
     "cc_codegen_with": [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t,
                         ctypes.POINTER(ctypes.c_size_t)],

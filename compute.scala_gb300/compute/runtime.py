@@ -172,6 +172,12 @@ class NativeRuntime:
         call("cc_device_errors", ctypes.byref(v))
         return v.value
 
+    PROBE_TIMEOUT = 90  # CC_DEVICE_ERR_PROBE_TIMEOUT
+
+    def probe_bounded_wait(self, limit_ns: int, flag_value: int):
+        """Enqueues a device wait on a word that is set (flag_value != 0) or never set."""
+        call("cc_probe_bounded_wait", ctypes.c_uint64(int(limit_ns)), int(flag_value))
+
     # -- batches (many independent contiguous elementwise programs)
     BATCH_PERSISTENT, BATCH_PER_PROGRAM, BATCH_GRAPH = 0, 1, 2
 

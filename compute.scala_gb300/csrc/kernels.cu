@@ -110,7 +110,29 @@ __global__ void __launch_bounds__(256) copy16_kernel(const uint4 *__restrict__ s
   for (; i < n16; i += stride) dst[i] = src[i];
 }
 
+// One thread waits until *flag is nonzero, for at most limit_ns of
+// %globaltimer time; when the limit passes it records `code` in *err (the first
+// error stays) and returns.  The pattern of every spinning wait in this library.
+__global__ void flag_wait_kernel(const volatile int *flag, unsigned long long limit_ns, int *err, int code) {
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    if (*flag != 0) return;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > limit_ns) {
+      atomicCAS(err, 0, code);
+      return;
+    }
+    __nanosleep(1000);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_flag_wait(const int *flag, unsigned long long limit_ns, int *err, int code, cudaStream_t stream) {
+  flag_wait_kernel<<<1, 1, 0, stream>>>(flag, limit_ns, err, code);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_copy16(void *dst, const void *src, size_t bytes, int sm_count, cudaStream_t stream) {
   const long long n16 = (long long)(bytes / 16);

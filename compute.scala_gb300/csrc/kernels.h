@@ -15,6 +15,9 @@ int sum_grid(long long work, int sm_count);
 // Copies bytes / 16 sixteen-byte words with a kernel (both pointers 16-byte aligned,
 // device-accessible: device memory or pinned host memory); the remainder is the caller's.
 cudaError_t launch_copy16(void *dst, const void *src, size_t bytes, int sm_count, cudaStream_t stream);
+// One thread waits until *flag is nonzero, at most limit_ns; on expiry *err = code
+// (if it was 0).
+cudaError_t launch_flag_wait(const int *flag, unsigned long long limit_ns, int *err, int code, cudaStream_t stream);
 // Blocks of a grid sum: one element (or float4) per thread, capped at max_blocks.
 int sum_grid_for(long long work, int block, int max_blocks);
 cudaError_t launch_sum(const float *in, long long n, float2 *partials, unsigned int *counter, float *out,

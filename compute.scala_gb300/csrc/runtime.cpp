@@ -352,6 +352,10 @@ struct Context {
   int *error_flag() {
     return reinterpret_cast<int *>(static_cast<char *>(sum_scratch) + sizeof(float2) * kMaxSumBlocks + 128);
   }
+  // The word cc_probe_bounded_wait waits on (same block).
+  int *probe_flag() {
+    return reinterpret_cast<int *>(static_cast<char *>(sum_scratch) + sizeof(float2) * kMaxSumBlocks + 192);
+  }
 };
 
 std::mutex g_init_mu;
@@ -1377,6 +1381,18 @@ int cc_gemm_f32(uint64_t a_ptr, uint64_t b_ptr, uint64_t c_ptr, int m, int n, in
   cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   run_gemm(c, reinterpret_cast<const float *>(a_ptr), reinterpret_cast<const float *>(b_ptr),
            reinterpret_cast<float *>(c_ptr), m, n, k, lda, ldb, ldc, mode, s);
+  CC_API_END
+}
+
+int cc_probe_bounded_wait(uint64_t limit_ns, int flag_value) {
+  CC_API_BEGIN
+  if (limit_ns > 10000000000ull) fail(CC_ERR_INVALID_VALUE, "limit_ns above 10 s");
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  c.last_write.valid = false;
+  check_cuda(cudaMemsetAsync(c.probe_flag(), flag_value ? 1 : 0, sizeof(int), c.stream), "set probe flag");
+  check_cuda(launch_flag_wait(c.probe_flag(), limit_ns, c.error_flag(), CC_DEVICE_ERR_PROBE_TIMEOUT, c.stream),
+             "probe launch");
   CC_API_END
 }
 

@@ -225,6 +225,14 @@ int cc_gemm_f32(uint64_t a_ptr, uint64_t b_ptr, uint64_t c_ptr, int m, int n, in
 /* Reads and clears the device error flag that kernels with bounded waits set
  * when a wait expires (0 = none); blocking. */
 int cc_device_errors(int *code);
+/* Diagnostic of the bounded waits themselves: enqueues on the context stream
+ * one thread that waits for a device word, which is set beforehand when
+ * flag_value != 0 (the wait ends at once) and never otherwise, so the wait
+ * gives up after limit_ns (at most 10 s) and the device error flag reads
+ * CC_DEVICE_ERR_PROBE_TIMEOUT.  Asynchronous: an event recorded after it
+ * completes once the wait has ended; the context stays usable. */
+#define CC_DEVICE_ERR_PROBE_TIMEOUT 90
+int cc_probe_bounded_wait(uint64_t limit_ns, int flag_value);
 
 /* ---- batches: many independent elementwise programs of uneven lengths evaluated
  *      together (no reference counterpart: the reference launches one kernel per
