@@ -87,11 +87,12 @@ def test_split_bf16_tensor_core_mode(cuda_device, shape):
 
 @pytest.mark.parametrize("variant", [3, 4, 5])
 @pytest.mark.parametrize("shape", [(300, 100, 700), (1024, 1024, 1024), (512, 4096, 768), (200, 1000, 520),
-                                   (2560, 512, 2048), (2500, 600, 2000)])
+                                   (256, 300, 512), (2560, 512, 2048), (2500, 600, 2000)])
 def test_tensor_core_kernel_variants(cuda_device, variant, shape):
     """Every K-chunked kernel (128-column tiles restarting every 256 / 512 of K;
     256-column tiles restarting hi*hi every 256 of K) within the error bar, on
-    ragged shapes and on K long enough for many chunks.  The last two shapes
+    ragged shapes, on K long enough for many chunks and on a last partial chunk
+    (K = 300: ten k-blocks of 32, chunks of 8 then 2).  The last two shapes
     have 160 256-column tiles, more than one round of 152 SMs, so variant 5
     runs its last 8 tiles as column halves (ragged ones in the second)."""
     rt = cuda_device.runtime
