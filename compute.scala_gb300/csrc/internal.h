@@ -90,7 +90,7 @@ struct CodegenOptions {
   int64_t prefetch_min_bytes = -1;  // L2-prefetch loads from inputs at least this large (-1: never)
   int smem_ring = 0;        // generic kernels: shared-memory ring slots per thread for staged loads (0: none)
   int points_per_thread = 1;  // generic elementwise kernels: consecutive points a thread computes together
-  bool vector_loads = false;  // generic elementwise kernels: also cc_ew_vl, with float4 grouped reads
+  bool vector_loads = true;   // generic elementwise kernels: also cc_ew_vl, with float4 grouped reads
 };
 
 // Minimum resident blocks per SM to request for a generic kernel over `domain`

@@ -166,7 +166,7 @@ int cc_compile_check(const char *ir, size_t ir_len, int cc_major, int cc_minor, 
 /* The same with code-generation options as "key=value" words (NULL = defaults):
  * block, lookahead, ring (shared-memory ring slots), unroll, min_blocks, asm,
  * points (consecutive points per thread of a generic elementwise kernel),
- * vl (1: also the float4 grouped-read kernel cc_ew_vl). */
+ * vl (1, the default as in the runtime: also the float4 grouped-read kernel cc_ew_vl). */
 int cc_codegen_with(const char *ir, size_t ir_len, const char *options, char *buf, size_t len, size_t *needed);
 int cc_compile_check_with(const char *ir, size_t ir_len, int cc_major, int cc_minor, uint32_t flags,
                           const char *options);

@@ -194,15 +194,15 @@ def test_points_per_thread_codegen():
     x, w, b = (NonInlineTensor(d, s, 0.0, None) for s in [(4, 16, 16, 8), (3, 3, 8, 8), (8,)])
     parts = bench.conv_expr(d.Tensor, x, w, b, parts=True)
     text = d.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape).text
-    one = runtime.codegen(text)
-    two = runtime.codegen(text, "points=2")
-    assert runtime.codegen(text, "points=1") == one
-    assert runtime.codegen(text, "points=3") == one  # 16 % 3 != 0
+    one = runtime.codegen(text, "vl=0")
+    two = runtime.codegen(text, "points=2 vl=0")
+    assert runtime.codegen(text, "points=1 vl=0") == one
+    assert runtime.codegen(text, "points=3 vl=0") == one  # 16 % 3 != 0
     # 9 offsets x 8 channels of x per point; two points along w share 2 of 3 columns
     assert one.count("cc_ld(_") == 72 and two.count("cc_ld(_") == 96
     assert one.count("cc_sp2[") == two.count("cc_sp2[") == 2 + 576  # declaration, copy, reads
     assert "* 2; lin < n; lin += stride * 2)" in two
-    runtime.compile_check(text, options="points=2")
+    runtime.compile_check(text, options="points=2 vl=0")
 
 
 def test_vector_load_codegen():
@@ -215,8 +215,8 @@ def test_vector_load_codegen():
     x, w, b = (NonInlineTensor(d, s, 0.0, None) for s in [(4, 16, 16, 8), (3, 3, 8, 8), (8,)])
     parts = bench.conv_expr(d.Tensor, x, w, b, parts=True)
     text = d.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape).text
-    assert "cc_ew_vl" not in runtime.codegen(text)
-    src = runtime.codegen(text, "vl=1")
+    assert "cc_ew_vl" not in runtime.codegen(text, "vl=0")
+    src = runtime.codegen(text)  # vl=1 by default
     scalar, vl = src.split("cc_ew_vl(")
     assert scalar.count("cc_ld(_") == 72 and "cc_ld4(_" not in scalar
     assert vl.count("cc_ld4(_") == 18 and "cc_ld(_" not in vl  # 9 offsets x 2 groups of 4 channels
