@@ -279,3 +279,35 @@ def test_convolution_idiom_bit_exact(cuda_device, shape):
     unmerged = plain.serialize(trees.Concatenate([t.closure for t in parts]), parts[0].shape)
     assert unmerged.text.count("\nx ") > ser.text.count("\nx ")
     assert np.array_equal(bits(bench.conv_expr(plain.Tensor, x, wt, b).flatArray()), bits(got))
+
+
+def test_wide_indices_past_2_31(cuda_device):
+    """A view program over 5 x 2^29 = 2.7e9 points (10.7 GB per tensor): the
+    coordinate decode and the view offsets run in 64-bit arithmetic past 2^31.
+    Checked bit-exactly at chunks around the 2^31 and 2^32-byte boundaries and
+    at the end, from the reference RNG's values at the mapped indices."""
+    rt = cuda_device.runtime
+    T = cuda_device.Tensor
+    rows, cols = 5, 1 << 29
+    seed = 0x40000007
+    x = T.random([rows, cols], seed=seed).doCache()
+    e = x.translate([1, -3]) + x
+    ser = cuda_device.serialize(e.closure, e.shape)
+    assert [id(p) for p in ser.params] == [id(x)]
+    out = rt.alloc(rows * cols * 4)
+    try:
+        rt.launch(rt.program(ser.text), [x._cached], out)
+        starts = [0, (1 << 29) - 8, (1 << 31) - 8, (1 << 31) + 1000, 3 * (1 << 29) + 7, rows * cols - 4096]
+        for s0 in starts:
+            got = rt.download(out, 4096, offset=4 * s0)
+            lin = np.arange(s0, s0 + 4096, dtype=np.int64)
+            i0, i1 = lin // cols, lin % cols
+            src0, src1 = i0 - 1, i1 + 3  # translate negates its offsets: source = target - offset
+            inside = (src0 >= 0) & (src1 < cols)
+            xv = lambda j: rng._unit(rng.wang_hash(j.astype(np.uint32) ^ np.uint32(seed)))
+            shifted = np.where(inside, xv(np.where(inside, src0 * cols + src1, 0)), np.float32(0.0))
+            want = (shifted + xv(lin)).astype(np.float32)
+            assert np.array_equal(got.view(np.int32), want.view(np.int32)), s0
+    finally:
+        out.release()
+        x.close()
