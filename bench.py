@@ -377,7 +377,8 @@ def keep_busy(rt, st, seconds):
 
 
 def time_e2e(d, st, steps):
-    """Host buffers in, result out, through the C ABI: upload inputs, launch, download."""
+    """Host buffers in, result out, through the C ABI: upload inputs (non-blocking
+    writes ordered on the runtime's stream), launch, download (blocking)."""
     import ctypes
     import numpy as np
     from compute._native import call
@@ -400,7 +401,7 @@ def time_e2e(d, st, steps):
 
     def step():
         for (ptr, arr), b in zip(hosts, inputs):
-            call("cc_buf_upload", ctypes.c_uint64(b.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(b.nbytes))
+            call("cc_buf_upload_async", ctypes.c_uint64(b.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(b.nbytes))
         rt.launch(st["prog"], inputs, out)
         call("cc_buf_download", ctypes.c_uint64(out.handle), ctypes.c_size_t(0), res, ctypes.c_size_t(d2h))
 
