@@ -254,6 +254,10 @@ struct Frame {
   std::vector<std::string> gid;   // index variable names
   std::vector<int64_t> shape;
   std::vector<int64_t> goff = {};  // constant added to each index variable (empty: none)
+  // Index variables whose value is a compile-time integer (a view row with no
+  // coordinate term): gknown[x] != 0 means gid[x] == gval[x] (empty: none).
+  std::vector<uint8_t> gknown = {};
+  std::vector<int64_t> gval = {};
 };
 
 // One generated statement.  Index statements are integer view arithmetic (they
@@ -339,7 +343,8 @@ class Generator {
           break;
         }
         std::vector<std::string> idx, row_ok;
-        std::string ok = index_rows(node, p.dims, f, idx, &row_ok);
+        std::vector<std::pair<bool, int64_t>> rc;
+        std::string ok = index_rows(node, p.dims, f, idx, &row_ok, &rc);
         std::string off = offset_expr(p.dims, idx);
         std::string ptr = "in" + std::to_string(p.param_index) + (p.dims.empty() ? "" : " + " + off);
         // A load whose address depends on no output coordinate reads the same
@@ -350,8 +355,8 @@ class Generator {
           if (!uniform_.count(i)) uniform = false;
         const Cat load_cat = uniform ? Cat::Compute : Cat::Load;
         if (!uniform) varying_params_.insert(p.param_index);
-        if (vec_loads_ && asm_loads_ && merge_ && (!uniform || staged_.count(p.param_index)) &&
-            vector_load(node, p, idx, row_ok, !uniform, v))
+        if (vec_loads_ && asm_loads_ && merge_ &&
+            vector_load(p, idx, row_ok, rc, !uniform || !staged_.count(p.param_index), !uniform, v))
           break;
         if (reuse("L " + ptr + " " + ok + " " + lit_code(p.bits), v)) break;
         if (ring_ > 0 && !uniform && asm_loads_ && (ok.empty() || p.bits == 0)) {
@@ -401,8 +406,13 @@ class Generator {
           fail(CC_ERR_INVALID_PROGRAM, "IR: view matrix columns do not match the frame rank");
         v = fresh();
         std::vector<std::string> idx;
-        std::string ok = index_rows(node, node.dims, f, idx);
+        std::vector<std::pair<bool, int64_t>> rc;
+        std::string ok = index_rows(node, node.dims, f, idx, nullptr, &rc);
         Frame inner{next_frame_++, idx, node.dims};
+        for (auto &k : rc) {
+          inner.gknown.push_back(k.first ? 1 : 0);
+          inner.gval.push_back(k.second);
+        }
         std::string sub = gen(node.a, inner);
         if (reuse("V " + ok + " " + sub + " " + lit_code(node.bits), v)) break;
         if (!ok.empty())
@@ -583,16 +593,15 @@ class Generator {
   // into separate reads.  Needs 16-byte aligned inputs (cc_ew_vl).
   // A thread-independent read of a staged parameter groups the same way into
   // a float4 read of its (16-byte aligned) shared-memory copy.
-  bool vector_load(const IrNode &node, const IrNode &p, const std::vector<std::string> &idx,
-                   const std::vector<std::string> &row_ok, bool global, std::string &v) {
+  // A thread-independent read of an unstaged parameter stays a global load,
+  // emitted where it is used like the scalar one (`windowed` false).
+  bool vector_load(const IrNode &p, const std::vector<std::string> &idx, const std::vector<std::string> &row_ok,
+                   const std::vector<std::pair<bool, int64_t>> &row_const, bool global, bool windowed,
+                   std::string &v) {
     const int r = (int)p.dims.size();
-    const int cols = node.cols;
-    if (r == 0 || p.dims[r - 1] % 4 != 0) return false;
-    for (int x = 0; x < cols - 1; ++x)
-      if (node.m[(size_t)(r - 1) * cols + x] != 0.0) return false;
-    const double c = node.m[(size_t)(r - 1) * cols + cols - 1];
-    if (c < 0.0 || c >= (double)p.dims[r - 1] || c != (double)(int64_t)c) return false;
-    const int64_t ci = (int64_t)c;
+    if (r == 0 || p.dims[r - 1] % 4 != 0 || !row_const[r - 1].first) return false;
+    const int64_t ci = row_const[r - 1].second;
+    if (ci < 0 || ci >= p.dims[r - 1]) return false;
     int64_t total = 1;
     for (int64_t d : p.dims) total *= d;
     const bool wide = total >= (int64_t(1) << 31);
@@ -613,8 +622,8 @@ class Generator {
       const std::string pad = lit_code(p.bits);
       const std::string pad4 = "make_float4(" + pad + ", " + pad + ", " + pad + ", " + pad + ")";
       if (global)
-        add(Cat::Load, "float4 " + q + " = " + pad4 + "; cc_ld4(" + q + ", " + ptr + ", " +
-                           (ok.empty() ? std::string("1") : "(" + ok + ")") + ");");
+        add(windowed ? Cat::Load : Cat::Compute, "float4 " + q + " = " + pad4 + "; cc_ld4(" + q + ", " + ptr + ", " +
+                                                     (ok.empty() ? std::string("1") : "(" + ok + ")") + ");");
       else
         add(Cat::Compute, "const float4 " + q + " = " + (ok.empty() ? ptr : "(" + ok + ") ? " + ptr + " : " + pad4) +
                               ";");
@@ -629,8 +638,11 @@ class Generator {
   // One index variable per source dimension, the way ArrayView.extract
   // computes it (OpenCLKernelBuilder.scala:348-411); returns the bounds
   // condition ("" when every row is constant-zero and no check applies).
+  // row_const: per row, whether the index is a known integer and its value
+  // (integral coefficients on known index variables only).
   std::string index_rows(const IrNode &node, const std::vector<int64_t> &dims, const Frame &f,
-                         std::vector<std::string> &idx, std::vector<std::string> *row_ok = nullptr) {
+                         std::vector<std::string> &idx, std::vector<std::string> *row_ok = nullptr,
+                         std::vector<std::pair<bool, int64_t>> *row_const = nullptr) {
     const int rows = (int)dims.size();
     const int cols = node.cols;
     std::string ok;
@@ -668,6 +680,20 @@ class Generator {
       }
       if (!cond.empty()) ok += std::string(ok.empty() ? "" : " && ") + cond;
       if (row_ok) row_ok->push_back(cond);
+      if (row_const) {
+        bool known = c == (double)(int64_t)c;
+        double kv = c;
+        for (int x = 0; x < cols - 1 && known; ++x) {
+          const double s = node.m[(size_t)y * cols + x];
+          if (s == 0.0) continue;
+          if (s != (double)(int64_t)s || x >= (int)f.gknown.size() || !f.gknown[x]) {
+            known = false;
+          } else {
+            kv += s * (double)f.gval[x];
+          }
+        }
+        row_const->emplace_back(known, known ? (int64_t)kv : 0);
+      }
       idx.push_back(name);
     }
     return ok;
