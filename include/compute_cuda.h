@@ -93,9 +93,10 @@ int cc_synchronize(void);
  *                       before its first memory access, so results and ordering are unchanged
  *   "ew_smem_ring"      generic kernels: per-thread slots of a shared-memory ring through which loads
  *                       with zero padding are staged by cp.async (0 = loads into registers; 4..64)
- *   "ew_vector_loads"   1 (default) = generic elementwise kernels whose reads of a constant innermost index
- *                       (a channel split) group into 16-byte loads also get cc_ew_vl, launched when
- *                       every input and the output are 16-byte aligned (bit-identical); 0 = cc_ew only
+ *   "ew_vector_loads"   1 (default) = generic elementwise kernels whose reads at a constant innermost index
+ *                       (a channel split, also through views) group into 16-byte loads also get
+ *                       cc_ew_vl, launched when every input and the output are 16-byte aligned
+ *                       (bit-identical); 0 = cc_ew only
  *   "ew_points"         generic elementwise kernels: consecutive points per thread along the last output
  *                       dimension (when it divides that extent), with index arithmetic, loads and
  *                       arithmetic common to the points done once (1 = one point; default 1; 1..16)
