@@ -1069,11 +1069,10 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
   std::vector<std::vector<std::string>> mres;
   if (P > 1) merged_body(false, multi, mres);
   // The same with reads of a short innermost axis grouped into float4 loads
-  // (cc_ew_vl, launched when every input is 16-byte aligned).
+  // (cc_ew_vl / cc_sum_vl, launched when every input is 16-byte aligned).
   std::ostringstream vl_body;
   std::vector<std::vector<std::string>> vl_res;
-  if (opt.vector_loads && !contiguous && ir.kind == ProgramKind::Elementwise)
-    g.has_vl = merged_body(true, vl_body, vl_res) > 0;
+  if (opt.vector_loads && !contiguous) g.has_vl = merged_body(true, vl_body, vl_res) > 0;
   // (cc_ew_vl reads the copies as float4: 16-byte aligned there)
   auto staging = [&](bool align16) {
     std::string code;
@@ -1229,6 +1228,16 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << generic.str() << "    cc_acc(s_, c_, " << results[0] << ");\n  }\n"
         << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+    if (g.has_vl) {
+      // the same points in the same order: only the reads differ, so the sum's bits do not
+      src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_sum_vl(" << params
+          << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
+          << staging(true) << "  float s_ = 0.0f, c_ = 0.0f;\n"
+          << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
+          << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
+          << vl_body.str() << "    cc_acc(s_, c_, " << vl_res[0][0] << ");\n  }\n"
+          << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+    }
     if (contiguous) {
       src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum_v4(" << params
           << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"

@@ -90,7 +90,7 @@ struct CodegenOptions {
   int64_t prefetch_min_bytes = -1;  // L2-prefetch loads from inputs at least this large (-1: never)
   int smem_ring = 0;        // generic kernels: shared-memory ring slots per thread for staged loads (0: none)
   int points_per_thread = 1;  // generic elementwise kernels: consecutive points a thread computes together
-  bool vector_loads = true;   // generic elementwise kernels: also cc_ew_vl, with float4 grouped reads
+  bool vector_loads = true;   // generic kernels: also cc_ew_vl / cc_sum_vl, with float4 grouped reads
 };
 
 // Minimum resident blocks per SM to request for a generic kernel over `domain`
@@ -115,7 +115,7 @@ struct Generated {
   int smem_bytes = 0;      // dynamic shared memory of the generic kernel (its load ring)
   std::vector<int64_t> param_bytes;  // bytes of each input buffer the kernel may read
   int points_per_thread = 1;         // of the generic elementwise kernel
-  bool has_vl = false;               // cc_ew_vl exists (float4 grouped reads; 16-byte aligned inputs)
+  bool has_vl = false;               // cc_ew_vl / cc_sum_vl exists (float4 grouped reads; aligned inputs)
 };
 
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);

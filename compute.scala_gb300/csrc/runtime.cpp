@@ -187,7 +187,7 @@ struct Module {
   CUmodule module = nullptr;
   CUfunction scalar = nullptr;  // cc_ew / cc_sum
   CUfunction vec4 = nullptr;    // cc_ew_v4 / cc_sum_v4 (contiguous inputs)
-  CUfunction vl = nullptr;      // cc_ew_vl (float4 grouped reads; 16-byte aligned inputs)
+  CUfunction vl = nullptr;      // cc_ew_vl / cc_sum_vl (float4 grouped reads; 16-byte aligned inputs)
   int block = 256;              // threads per block the kernels were generated for
   int resident_scalar = 0;      // blocks one SM holds at once, per variant
   int resident_vec4 = 0;
@@ -1181,7 +1181,9 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     const char *vname = ir.kind == ProgramKind::Sum ? "cc_sum_v4" : "cc_ew_v4";
     check_cu(g_drv.ModuleGetFunction(&mod->scalar, mod->module, sname), "cuModuleGetFunction");
     if (p->gen.has_vec4) check_cu(g_drv.ModuleGetFunction(&mod->vec4, mod->module, vname), "cuModuleGetFunction");
-    if (p->gen.has_vl) check_cu(g_drv.ModuleGetFunction(&mod->vl, mod->module, "cc_ew_vl"), "cuModuleGetFunction");
+    if (p->gen.has_vl)
+      check_cu(g_drv.ModuleGetFunction(&mod->vl, mod->module, ir.kind == ProgramKind::Sum ? "cc_sum_vl" : "cc_ew_vl"),
+               "cuModuleGetFunction");
     mod->block = opt.block;
     mod->vec_unroll = p->gen.vec_unroll;
     mod->smem_bytes = p->gen.smem_bytes;

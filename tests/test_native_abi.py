@@ -229,3 +229,21 @@ def test_vector_load_codegen():
     y = NonInlineTensor(d, (6, 8), 0.0, None)
     t = y.translate([0, 1]) + y
     assert "cc_ew_vl" not in runtime.codegen(d.serialize(t.closure, t.shape).text, "vl=1")
+
+
+def test_vector_load_sum_codegen():
+    """A sum over the view-heavy op gets cc_sum_vl (the bias read as float4
+    groups), compiled for sm_103a."""
+    import bench
+    from compute import Tensors, runtime
+    from compute.tensors import NonInlineTensor
+    d = Tensors(device=0)
+    n, c, h, w = 2, 16, 5, 7
+    x = NonInlineTensor(d, (n, c, h, w), 0.0, None)
+    bias = NonInlineTensor(d, (1, 1, 1, c), 0.0, None)
+    s = bench.build_c2(d.Tensor, x, bias, n, c, h, w)
+    text = d.serialize(s.closure, s.shape, "sum").text
+    src = runtime.codegen(text)
+    assert "cc_sum_vl(" in src and src.split("cc_sum_vl(")[1].count("cc_ld4(_") == 4
+    assert "cc_sum_vl(" not in runtime.codegen(text, "vl=0")
+    runtime.compile_check(text)

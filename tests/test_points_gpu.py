@@ -145,3 +145,34 @@ def test_channel_split_programs(cuda_device, c):
     finally:
         rt.config_set("ew_points", 1)
         rt.config_set("ew_vector_loads", before)
+
+
+def test_vector_load_sum_keeps_the_bits(cuda_device):
+    """cc_sum_vl folds the same point values in the same order as cc_sum: the
+    sum of the view-heavy op has the same bits with and without float4 reads,
+    and is within the sum bound of the exact sum of the oracle's values."""
+    import bench
+    from compute.tensors import NonInlineTensor
+    rt = cuda_device.runtime
+    d = cuda_device
+    n, c, h, w = 4, 128, 28, 28
+    x = NonInlineTensor(d, (n, c, h, w), 0.0, None)
+    bias = NonInlineTensor(d, (1, 1, 1, c), 0.0, None)
+    s = bench.build_c2(d.Tensor, x, bias, n, c, h, w)
+    text = d.serialize(s.closure, s.shape, "sum").text
+    r = np.random.RandomState(9)
+    arrays = [r.normal(size=n * c * h * w).astype(np.float32), r.normal(size=c).astype(np.float32)]
+    before = rt.config_get("ew_vector_loads")
+    try:
+        rt.config_set("ew_vector_loads", 1)
+        assert "cc_sum_vl" in rt.program(text).source()
+        got = _run(rt, text, arrays, 1)
+        rt.config_set("ew_vector_loads", 0)
+        want = _run(rt, text, arrays, 1)
+    finally:
+        rt.config_set("ew_vector_loads", before)
+    assert got.view(np.int32)[0] == want.view(np.int32)[0]
+    ew = text.replace("ccir 1 sum", "ccir 1 ew", 1)
+    vals = np.asarray(interp.evaluate(ew, arrays), np.float64)
+    exact = float(np.sum(vals))
+    assert abs(float(got[0]) - exact) <= np.sqrt(vals.size) * 2.0 ** -24 * float(np.sum(np.abs(vals))) + 1e-30
