@@ -421,7 +421,8 @@ def time_e2e(d, st, steps):
 
 def time_e2e_batch(d, b, progs, nbytes, steps):
     """The batch through the C ABI with host buffers: every input uploaded from
-    pinned memory, one persistent launch, every output downloaded, per step."""
+    pinned memory, one persistent launch, every output downloaded (non-blocking
+    reads, then one synchronisation), per step."""
     import ctypes
     import numpy as np
     from compute._native import call
@@ -452,7 +453,9 @@ def time_e2e_batch(d, b, progs, nbytes, steps):
                  ctypes.c_size_t(buf.nbytes))
         b.run(0)
         for ptr, out in zip(outs, b.outputs):
-            call("cc_buf_download", ctypes.c_uint64(out.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(out.nbytes))
+            call("cc_buf_download_async", ctypes.c_uint64(out.handle), ctypes.c_size_t(0), ptr,
+                 ctypes.c_size_t(out.nbytes))
+        call("cc_synchronize")
 
     try:
         step()

@@ -124,6 +124,7 @@ _SIGNATURES = {
     "cc_buf_upload": [c_handle, c_size, ctypes.c_void_p, c_size],
     "cc_buf_upload_async": [c_handle, c_size, ctypes.c_void_p, c_size],
     "cc_buf_download": [c_handle, c_size, ctypes.c_void_p, c_size],
+    "cc_buf_download_async": [c_handle, c_size, ctypes.c_void_p, c_size],
     "cc_host_alloc": [c_size, ctypes.POINTER(ctypes.c_void_p)],
     "cc_host_free": [ctypes.c_void_p],
     "cc_pool_stats": [ctypes.POINTER(c_size), ctypes.POINTER(c_size), ctypes.POINTER(ctypes.c_uint64),

@@ -1011,6 +1011,23 @@ int cc_buf_download(cc_handle h, size_t offset, void *host, size_t bytes) {
   CC_API_END
 }
 
+int cc_buf_download_async(cc_handle h, size_t offset, void *host, size_t bytes) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  void *src;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    Buffer &b = buffer_of(c, h);
+    if (offset > b.bytes || bytes > b.bytes - offset) fail(CC_ERR_INVALID_VALUE, "download range exceeds the buffer");
+    src = static_cast<char *>(b.ptr) + offset;
+  }
+  if (bytes == 0) return CC_OK;
+  if (!host) fail(CC_ERR_INVALID_VALUE, "null host pointer");
+  if (!sm_copy(c, host, src, bytes, false))
+    check_cuda(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, c.stream), "cudaMemcpyAsync D2H");
+  CC_API_END
+}
+
 int cc_host_alloc(size_t bytes, void **host) {
   CC_API_BEGIN
   if (!host) fail(CC_ERR_INVALID_VALUE, "null pointer");

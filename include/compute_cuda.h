@@ -137,6 +137,11 @@ int cc_buf_upload(cc_handle buf, size_t offset, const void *host, size_t bytes);
 int cc_buf_upload_async(cc_handle buffer, size_t offset, const void *host, size_t bytes);
 /* Device -> host copy of [offset, offset+bytes) after all work queued so far; blocking. */
 int cc_buf_download(cc_handle buf, size_t offset, void *host, size_t bytes);
+/* The same, ordered on the context stream without waiting (OpenCL's non-blocking
+ * enqueueReadBuffer): the host memory holds the data once the copy is complete
+ * (cc_synchronize, or an event recorded after it); pinned host memory
+ * (cc_host_alloc) makes the copy asynchronous to the host. */
+int cc_buf_download_async(cc_handle buf, size_t offset, void *host, size_t bytes);
 /* Page-locked host memory for fast transfers (the staging of Tensor.apply / flatArray). */
 int cc_host_alloc(size_t bytes, void **host);
 int cc_host_free(void *host);

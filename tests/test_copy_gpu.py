@@ -42,7 +42,8 @@ def test_copy_kernel_round_trips(cuda_device):
 
 def test_async_uploads_are_ordered_before_launches(cuda_device):
     """cc_buf_upload_async copies many buffers without waiting; a launch and a
-    download queued after them see the uploaded bytes."""
+    download queued after them see the uploaded bytes; cc_buf_download_async
+    reads them back without waiting, complete at the next synchronisation."""
     rt = cuda_device.runtime
     d = cuda_device
     from compute.tensors import NonInlineTensor
@@ -65,6 +66,13 @@ def test_async_uploads_are_ordered_before_launches(cuda_device):
             rt.launch(prog, [b], o)
         for k, o in enumerate(outs):
             assert np.array_equal(rt.download(o, n), 2 * (np.arange(n, dtype=np.float32) + k))
+        # non-blocking reads into the same pinned buffers, complete after one synchronisation
+        for (h, arr), o in zip(hosts, outs):
+            arr[:] = -1.0
+            call("cc_buf_download_async", ctypes.c_uint64(o.handle), ctypes.c_size_t(0), h, ctypes.c_size_t(4 * n))
+        rt.synchronize()
+        for k, (_, arr) in enumerate(hosts):
+            assert np.array_equal(arr, 2 * (np.arange(n, dtype=np.float32) + k))
     finally:
         for h, _ in hosts:
             call("cc_host_free", h)
