@@ -279,6 +279,9 @@ struct Stmt {
   // Emission order of loads and arithmetic (stable; creation order unless
   // statements are merged across points, see Generator::set_point).
   int64_t key = 0;
+  // A scalar predicated load (var, ptr, ok, padding ubits) that emit() may put
+  // in one inline-PTX block with its neighbours of the same condition.
+  bool batchable = false;
 };
 
 class Generator {
@@ -381,6 +384,14 @@ class Generator {
           // keeps these in the order emit() places them, so the lookahead holds.
           add(load_cat, "float " + v + " = " + lit_code(p.bits) + "; cc_ld(" + v + ", " + ptr + ", " +
                             (ok.empty() ? std::string("1") : "(" + ok + ")") + ");");
+          if (!uniform && batch_loads_) {
+            Stmt &st = stmts_.back();
+            st.batchable = true;
+            st.var = v;
+            st.ptr = ptr;
+            st.ok = ok;
+            st.ubits = p.bits;
+          }
         } else if (ok.empty()) {
           add(load_cat, "const float " + v + " = __ldg(" + ptr + ");");
         } else {
@@ -456,8 +467,31 @@ class Generator {
     auto slot = [&](int r) { return "cc_ring[" + std::to_string(r % ring_) + " * blockDim.x + threadIdx.x]"; };
     auto emit_loads_to = [&](size_t n) {
       if (n > loads.size()) n = loads.size();
+      // batched loads: top up in whole groups so neighbours share a block
+      if (batch_loads_ && n > emitted) n = std::min(loads.size(), emitted + (n - emitted + kLoadBatch - 1) / kLoadBatch * kLoadBatch);
       while (emitted < n) {
         const Stmt &l = stmts_[loads[emitted++]];
+        if (l.batchable) {
+          // up to kLoadBatch consecutive loads under the same condition: one
+          // predicate for all of them
+          std::vector<const Stmt *> run{&l};
+          while (emitted < n && run.size() < (size_t)kLoadBatch) {
+            const Stmt &m = stmts_[loads[emitted]];
+            if (!m.batchable || m.ok != l.ok) break;
+            run.push_back(&m);
+            ++emitted;
+          }
+          const int k = (int)run.size();
+          for (const Stmt *m : run) os << pad << "float " << m->var << " = " << lit_code(m->ubits) << ";\n";
+          os << pad << "asm volatile(\"{\\n .reg .pred q;\\n setp.ne.b32 q, %" << 2 * k << ", 0;\\n";
+          for (int j = 0; j < k; ++j) os << " @q ld.global.nc.f32 %" << j << ", [%" << k + j << "];\\n";
+          os << "}\\n\"\n" << pad << "    : ";
+          for (int j = 0; j < k; ++j) os << (j ? ", " : "") << "\"+f\"(" << run[j]->var << ")";
+          os << "\n" << pad << "    : ";
+          for (int j = 0; j < k; ++j) os << "\"l\"(" << run[j]->ptr << "), ";
+          os << "\"r\"((int)(" << (l.ok.empty() ? std::string("1") : l.ok) << ")));\n";
+          continue;
+        }
         if (l.ring < 0) {
           os << pad << l.text << "\n";
           continue;
@@ -534,6 +568,9 @@ class Generator {
   // Merge statements with identical right-hand sides (the frames of several
   // points per thread share index arithmetic, loads and arithmetic).
   void set_merge(bool on) { merge_ = on; }
+  // Emit scalar predicated loads of one condition in groups of kLoadBatch,
+  // one predicate per group.
+  void set_batch_loads(bool on) { batch_loads_ = on; }
   // Group reads of the same 16 bytes into float4 loads (needs merging on).
   void set_vector_loads(bool on) { vec_loads_ = on; }
   // Parameters with shared-memory copies (cc_sp<k>, 16-byte aligned).
@@ -672,28 +709,30 @@ class Generator {
         if (row_uniform) uniform_.insert(name);
         add(Cat::Index, "const int " + name + " = " + rhs + ";");
       }
+      // the index as a compile-time integer, when the row has one
+      bool known = c == (double)(int64_t)c;
+      double kv = c;
+      for (int x = 0; x < cols - 1 && known; ++x) {
+        const double s = node.m[(size_t)y * cols + x];
+        if (s == 0.0) continue;
+        if (s != (double)(int64_t)s || x >= (int)f.gknown.size() || !f.gknown[x]) {
+          known = false;
+        } else {
+          kv += s * (double)f.gval[x];
+        }
+      }
       std::string cond;
       if (!any) {
         if (dims[y] == 0) cond = "false";
+      } else if (known && f.gknown.size() > 0) {
+        // a known index through a view: its bounds test is decided here
+        if (kv < 0.0 || kv >= (double)dims[y]) cond = "false";
       } else {
         cond = "(" + name + " >= 0) && (" + name + " < " + std::to_string(dims[y]) + ")";
       }
       if (!cond.empty()) ok += std::string(ok.empty() ? "" : " && ") + cond;
       if (row_ok) row_ok->push_back(cond);
-      if (row_const) {
-        bool known = c == (double)(int64_t)c;
-        double kv = c;
-        for (int x = 0; x < cols - 1 && known; ++x) {
-          const double s = node.m[(size_t)y * cols + x];
-          if (s == 0.0) continue;
-          if (s != (double)(int64_t)s || x >= (int)f.gknown.size() || !f.gknown[x]) {
-            known = false;
-          } else {
-            kv += s * (double)f.gval[x];
-          }
-        }
-        row_const->emplace_back(known, known ? (int64_t)kv : 0);
-      }
+      if (row_const) row_const->emplace_back(known, known ? (int64_t)kv : 0);
       idx.push_back(name);
     }
     return ok;
@@ -727,6 +766,8 @@ class Generator {
   int next_var_ = 0;
   int next_frame_ = 1;
   bool merge_ = false;
+  bool batch_loads_ = false;
+  static constexpr int kLoadBatch = 8;
   bool vec_loads_ = false;
   std::set<int> staged_;
   int vector_loads_ = 0;
@@ -1047,6 +1088,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
     Generator mg(ir, false, opt.asm_loads, opt.prefetch_min_bytes);
     mg.set_merge(true);
     mg.set_vector_loads(vec);
+    mg.set_batch_loads(vec && opt.batch_loads);
     if (vec) mg.set_staged(staged);
     decode(os, 4);
     res.assign(P, {});

@@ -91,6 +91,7 @@ struct CodegenOptions {
   int smem_ring = 0;        // generic kernels: shared-memory ring slots per thread for staged loads (0: none)
   int points_per_thread = 1;  // generic elementwise kernels: consecutive points a thread computes together
   bool vector_loads = true;   // generic kernels: also cc_ew_vl / cc_sum_vl, with float4 grouped reads
+  bool batch_loads = false;   // those kernels: scalar loads of one condition share one predicate, 8 at a time
 };
 
 // Minimum resident blocks per SM to request for a generic kernel over `domain`

@@ -326,6 +326,7 @@ struct Context {
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int ew_points = 1;     // generic elementwise kernels: consecutive points per thread
   int ew_vector_loads = 1;  // generic elementwise kernels: float4 grouped reads when inputs are aligned
+  int ew_batch_loads = 0;   // those kernels: one predicate per group of 8 scalar loads
   int pdl = 1;           // launch generated kernels with programmatic dependent launch
   int copy_kernel = 0;   // copies between pinned host memory and the device by the SMs
   // The output range of the last generated kernel launched, and its stream: a
@@ -829,6 +830,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "pdl") {
     if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "pdl must be 0 or 1");
     c.pdl = (int)value;
+  } else if (k == "ew_batch_loads") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "ew_batch_loads must be 0 or 1");
+    c.ew_batch_loads = (int)value;
   } else if (k == "ew_vector_loads") {
     if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "ew_vector_loads must be 0 or 1");
     c.ew_vector_loads = (int)value;
@@ -890,6 +894,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
   else if (k == "ew_points") *value = c.ew_points;
   else if (k == "ew_vector_loads") *value = c.ew_vector_loads;
+  else if (k == "ew_batch_loads") *value = c.ew_batch_loads;
   else if (k == "pdl") *value = c.pdl;
   else if (k == "tc_group_m") *value = c.tc_group_m;
   else if (k == "copy_kernel") *value = c.copy_kernel;
@@ -1090,10 +1095,11 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     opt.smem_ring = c.ew_smem_ring;
     opt.points_per_thread = c.ew_points;
     opt.vector_loads = c.ew_vector_loads != 0;
+    opt.batch_loads = c.ew_batch_loads != 0;
   }
   key += "#lookahead " + std::to_string(opt.load_lookahead) + " asm " + std::to_string((int)opt.asm_loads) +
          " blocks " + std::to_string(-opt.min_blocks) + " block " + std::to_string(opt.block) + " unroll " + std::to_string(opt.vec_unroll) +
-         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " ring " + std::to_string(opt.smem_ring) + " points " + std::to_string(opt.points_per_thread) + " vl " + std::to_string((int)opt.vector_loads) +
+         " prefetch " + std::to_string(opt.prefetch_min_bytes) + " ring " + std::to_string(opt.smem_ring) + " points " + std::to_string(opt.points_per_thread) + " vl " + std::to_string((int)opt.vector_loads) + " bl " + std::to_string((int)opt.batch_loads) +
          " sumblock " + std::to_string(c.sum_block) +
          " contraction " + std::to_string(c.contraction) + " tc " + std::to_string(c.tc_variant) + " tuner " +
          std::to_string(c.tuner) + "\n";
@@ -1251,6 +1257,7 @@ CodegenOptions parse_codegen_options(const char *text) {
     else if (k == "asm") o.asm_loads = v != 0;
     else if (k == "points") o.points_per_thread = (int)v;
     else if (k == "vl") o.vector_loads = v != 0;
+    else if (k == "batch") o.batch_loads = v != 0;
     else fail(CC_ERR_INVALID_VALUE, "unknown code-generation option '" + k + "'");
   }
   return o;

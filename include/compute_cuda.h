@@ -97,6 +97,9 @@ int cc_synchronize(void);
  *                       (a channel split, also through views) group into 16-byte loads also get
  *                       cc_ew_vl, launched when every input and the output are 16-byte aligned
  *                       (bit-identical); 0 = cc_ew only
+ *   "ew_batch_loads"    1 = in cc_ew_vl / cc_sum_vl, scalar loads under one bounds condition share one
+ *                       predicate, 8 per inline-PTX block, issued 8 at a time (faster from L2, slower
+ *                       from DRAM: default 0)
  *   "ew_points"         generic elementwise kernels: consecutive points per thread along the last output
  *                       dimension (when it divides that extent), with index arithmetic, loads and
  *                       arithmetic common to the points done once (1 = one point; default 1; 1..16)
@@ -172,7 +175,8 @@ int cc_compile_check(const char *ir, size_t ir_len, int cc_major, int cc_minor, 
 /* The same with code-generation options as "key=value" words (NULL = defaults):
  * block, lookahead, ring (shared-memory ring slots), unroll, min_blocks, asm,
  * points (consecutive points per thread of a generic elementwise kernel),
- * vl (1, the default as in the runtime: also the float4 grouped-read kernel cc_ew_vl). */
+ * vl (1, the default as in the runtime: also the float4 grouped-read kernel cc_ew_vl),
+ * batch (1: its scalar loads in predicate-sharing blocks of 8). */
 int cc_codegen_with(const char *ir, size_t ir_len, const char *options, char *buf, size_t len, size_t *needed);
 int cc_compile_check_with(const char *ir, size_t ir_len, int cc_major, int cc_minor, uint32_t flags,
                           const char *options);

@@ -176,3 +176,31 @@ def test_vector_load_sum_keeps_the_bits(cuda_device):
     vals = np.asarray(interp.evaluate(ew, arrays), np.float64)
     exact = float(np.sum(vals))
     assert abs(float(got[0]) - exact) <= np.sqrt(vals.size) * 2.0 ** -24 * float(np.sum(np.abs(vals))) + 1e-30
+
+
+def test_batched_loads_keep_the_bits(cuda_device):
+    """`ew_batch_loads`: scalar loads of one condition share a predicate in
+    blocks of 8 (the view-heavy op's 128 channel reads); same bits."""
+    import bench
+    from compute.tensors import NonInlineTensor
+    rt = cuda_device.runtime
+    d = cuda_device
+    r = np.random.RandomState(6)
+    n, c, h, w = 4, 128, 28, 28
+    x = NonInlineTensor(d, (n, c, h, w), 0.0, None)
+    bias = NonInlineTensor(d, (1, 1, 1, c), 0.0, None)
+    s = bench.build_c2(d.Tensor, x, bias, n, c, h, w)
+    arrays = [r.normal(size=n * c * h * w).astype(np.float32), r.normal(size=c).astype(np.float32)]
+    try:
+        for kind in ("ew", "sum"):
+            text = d.serialize(s.closure, s.shape, kind).text
+            n_out = n * h * w if kind == "ew" else 1
+            rt.config_set("ew_batch_loads", 0)
+            want = _run(rt, text, arrays, n_out)
+            rt.config_set("ew_batch_loads", 1)
+            assert "@q ld.global.nc.f32 %7" in rt.program(text).source()
+            _same_bits(want, _run(rt, text, arrays, n_out))
+        ref = interp.evaluate(d.serialize(s.closure, s.shape).text, arrays)
+        _same_bits(np.asarray(ref, np.float32), _run(rt, d.serialize(s.closure, s.shape).text, arrays, n * h * w))
+    finally:
+        rt.config_set("ew_batch_loads", 0)
