@@ -247,3 +247,31 @@ def test_vector_load_sum_codegen():
     assert "cc_sum_vl(" in src and src.split("cc_sum_vl(")[1].count("cc_ld4(_") == 4
     assert "cc_sum_vl(" not in runtime.codegen(text, "vl=0")
     runtime.compile_check(text)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_channel_view_programs_compile_in_every_form(seed):
+    """Random channel splits of translated/permuted NHWC tensors (reads at known
+    view indices, float4 groups, staged weights), as elementwise programs and
+    sums, compile for sm_103a with every read form: scalar, float4 groups,
+    batched predicates, two points per thread."""
+    import numpy as np
+    from compute import Tensors, runtime
+    from compute.tensors import NonInlineTensor
+    r = np.random.RandomState(seed)
+    d = Tensors(device=0)
+    n, h, w = 2, int(r.randint(3, 9)), 2 * int(r.randint(2, 6))
+    c = int(r.choice([4, 8, 12]))
+    x = NonInlineTensor(d, (n, h, w, c), 0.0, None)
+    wt = NonInlineTensor(d, (c,), 0.0, None)
+    chans = x.split(3)
+    ws = wt.split(0)
+    acc = None
+    for k in range(c):
+        t = chans[k].translate([0, int(r.randint(-1, 2)), int(r.randint(-1, 2))]) * ws[k].broadcast([n, h, w])
+        acc = t if acc is None else acc + t
+    for kind in ("ew", "sum"):
+        text = d.serialize(acc.closure, acc.shape, kind).text
+        for opts in ("vl=0", "vl=1", "vl=1 batch=1", "vl=1 points=2"):
+            runtime.compile_check(text, options=opts)
+        assert ("cc_ew_vl(" if kind == "ew" else "cc_sum_vl(") in runtime.codegen(text)
