@@ -204,3 +204,42 @@ def test_batched_loads_keep_the_bits(cuda_device):
         _same_bits(np.asarray(ref, np.float32), _run(rt, d.serialize(s.closure, s.shape).text, arrays, n * h * w))
     finally:
         rt.config_set("ew_batch_loads", 0)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_channel_view_programs_in_every_form(cuda_device, seed):
+    """Random channel splits of translated NHWC tensors weighted by a staged
+    vector: the oracle's bits with scalar reads, float4 groups, batched
+    predicates and two points per thread; sums bit-identical across forms."""
+    from compute.tensors import NonInlineTensor
+    rt = cuda_device.runtime
+    d = cuda_device
+    r = np.random.RandomState(seed)
+    n, h, w = 2, int(r.randint(3, 9)), 2 * int(r.randint(2, 6))
+    c = int(r.choice([4, 8, 12]))
+    x = NonInlineTensor(d, (n, h, w, c), 0.0, None)
+    wt = NonInlineTensor(d, (c,), 0.0, None)
+    chans, ws = x.split(3), wt.split(0)
+    acc = None
+    for k in range(c):
+        t = chans[k].translate([0, int(r.randint(-1, 2)), int(r.randint(-1, 2))]) * ws[k].broadcast([n, h, w])
+        acc = t if acc is None else acc + t
+    ser = d.serialize(acc.closure, acc.shape)
+    by_id = {id(x): r.normal(size=n * h * w * c).astype(np.float32), id(wt): r.normal(size=c).astype(np.float32)}
+    arrays = [by_id[id(p)] for p in ser.params]
+    want = np.asarray(interp.evaluate(ser.text, arrays), np.float32)
+    sum_text = d.serialize(acc.closure, acc.shape, "sum").text
+    knobs = ("ew_vector_loads", "ew_batch_loads", "ew_points")
+    saved = [rt.config_get(k) for k in knobs]
+    sums = []
+    try:
+        for vl, bl, pts in ((0, 0, 1), (1, 0, 1), (1, 1, 1), (1, 0, 2)):
+            for k, v in zip(knobs, (vl, bl, pts)):
+                rt.config_set(k, v)
+            _same_bits(want, _run(rt, ser.text, arrays, n * h * w))
+            sums.append(_run(rt, sum_text, arrays, 1))
+    finally:
+        for k, v in zip(knobs, saved):
+            rt.config_set(k, v)
+    for s in sums[1:]:
+        _same_bits(sums[0], s)
