@@ -224,8 +224,7 @@ def setup(workload, d):
         out = rt.alloc(n * h * w * 4)
         return dict(prog=prog, sets=sets, out=out, bytes=c2_bytes(n, c, h, w), copies=copies,
                     keep=[x, bias], ser=ser, shape=(n, c, h, w),
-                    config={"workload": ("view-heavy fused op: x[%d,128,56,56] permute->+bias[128]->max0"
-                                         "->translate W+1->channel sum [%d,56,56]") % (n, n),
+                    config={"workload": arm_workload("c2"),
                             "x": [n, c, h, w], "bias": [c], "out": [n, h, w],
                             "l2": "inputs rotate over %d copies of x (%.0f MB > 4x L2)" % (copies, copies * xbytes / 1e6)})
     if workload == "c1":
@@ -247,7 +246,7 @@ def setup(workload, d):
         out = rt.alloc(4)
         return dict(prog=prog, sets=sets, out=out, bytes=c1_bytes(n, m), copies=copies, keep=abc, ser=ser,
                     shape=(n, m),
-                    config={"workload": "fused elementwise+sum: ((a*b+c).tanh).sum, a,b,c [%d,%d] U[-1,1]" % (n, m),
+                    config={"workload": arm_workload("c1"),
                             "l2": "inputs rotate over %d copies of (a,b,c) (%.0f MB > 4x L2)"
                                   % (copies, copies * 3 * n * m * 4 / 1e6)})
     if workload == "c6":
@@ -272,8 +271,7 @@ def setup(workload, d):
         nbytes = 2 * xbytes + k * k * c * c * 4 + c * 4
         return dict(prog=prog, sets=sets, out=out, bytes=nbytes, copies=copies, keep=(x, weight, bias), ser=ser,
                     shape=(n, h, w, c),
-                    config={"workload": "3x3 convolution via translate/split/join: x[128,32,32,8] NHWC ~N(0,1), "
-                                        "weight[3,3,8,8], bias[8] -> [128,32,32,8]",
+                    config={"workload": arm_workload("c6"),
                             "flops_per_step": 2 * n * h * w * c * k * k * c,
                             "l2": "inputs rotate over %d copies of x (%.0f MB > 4x L2)"
                                   % (copies, copies * xbytes / 1e6)})
@@ -290,9 +288,8 @@ def setup(workload, d):
         out = rt.alloc(m * n * 4)
         return dict(prog=prog, sets=[[a._cached, b._cached]], out=out, flops=2.0 * m * n * k, bytes=4 * (m * k + k * n + m * n),
                     keep=[a, b], ser=ser, shape=(m, k, n), copies=1,
-                    config={"workload": "contraction via broadcast+split(1).reduce: A[%d,%d] x B[%d,%d] ~ N(0,1), "
-                                        "split-BF16 (3 planes, 6 products) on tcgen05 tensor cores, FP32 accumulate"
-                                        % (m, k, k, n),
+                    config={"workload": arm_workload(workload),
+                            "method": "split-BF16 (3 planes, 6 products) on tcgen05 tensor cores, FP32 accumulate",
                             "seeds": [C3_SEED, C3_SEED + 1],
                             "l2": "operands %.0f MB; no rotation (compute-bound)" % (4 * (m * k + k * n) / 1e6)})
     raise SystemExit("unknown workload " + workload)
@@ -480,6 +477,23 @@ def emit(line):
     print(json.dumps(line), flush=True)
 
 
+def arm_workload(workload):
+    """The `config.workload` string of a workload, shared by both arms."""
+    if workload == "c2":
+        n = C2["n"]
+        return ("view-heavy fused op: x[%d,128,56,56] permute->+bias[128]->max0"
+                "->translate W+1->channel sum [%d,56,56]") % (n, n)
+    if workload == "c1":
+        return "fused elementwise+sum: ((a*b+c).tanh).sum, a,b,c [%d,%d] U[-1,1]" % (C1["n"], C1["m"])
+    if workload == "c6":
+        return ("3x3 convolution via translate/split/join: x[128,32,32,8] NHWC ~N(0,1), "
+                "weight[3,3,8,8], bias[8] -> [128,32,32,8]")
+    if workload in C3:
+        m, k, n = C3[workload]
+        return "contraction via broadcast+split(1).reduce: A[%d,%d] x B[%d,%d] ~ N(0,1)" % (m, k, k, n)
+    raise SystemExit("unknown workload " + workload)
+
+
 def apply_knobs(rt, knobs):
     _KNOBS[:] = list(knobs)
     for kv in knobs:
@@ -561,10 +575,11 @@ def main():
         if rank != 0:
             return
         r = cpu_reference(args.workload)
+        config = dict(r["config"], workload=arm_workload(args.workload), path=r["config"]["workload"])
         line = {"impl": "reference", "metric": metric, "value": r["gbs"], "unit": "GB/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
-                "config": r["config"],
+                "config": config,
                 "cpu_baseline": {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port",
                                  "sample": r["sample"]},
                 "e2e": {"value": r["gbs"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -822,10 +837,11 @@ def main_contraction(args, warmup, rank, world, local_rank):
             return
         from oracle import cref
         r = cref.time_contraction(C3[args.workload])
+        config = dict(r["config"], workload=arm_workload(args.workload), path=r["config"]["workload"])
         line = {"impl": "reference", "metric": metric, "value": r["tflops"], "unit": "TFLOP/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
-                "config": r["config"],
+                "config": config,
                 "cpu_baseline": {"value": r["tflops"], "unit": "TFLOP/s", "cores": r["threads"], "kind": "port",
                                  "sample": r["sample"]},
                 "e2e": {"value": r["tflops"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
