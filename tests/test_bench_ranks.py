@@ -43,3 +43,23 @@ def test_two_ranks_take_the_slowest_time():
         assert p.exitcode == 0
     got = dict(q.get(timeout=10) for _ in range(2))
     assert got == {0: 15.0, 1: 15.0}
+
+
+def test_both_arms_name_the_same_workload(capsys):
+    """`bench.py --impl reference` prints the workload string of the GPU arm
+    (the driver pairs the two lines by it); the CPU path is described beside."""
+    import json
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    assert bench.arm_workload("c2").startswith("view-heavy fused op: x[64,128,56,56]")
+    assert "split-BF16" not in bench.arm_workload("c3")
+    sys_argv = sys.argv
+    try:
+        sys.argv = ["bench.py", "--workload", "c3s", "--impl", "reference", "--steps", "1", "--warmup", "3"]
+        bench.main()
+    finally:
+        sys.argv = sys_argv
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["config"]["workload"] == bench.arm_workload("c3s")
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
