@@ -71,7 +71,7 @@ def _c2(T, n, c, h, w):
     return x, bias, y, t, s
 
 
-@pytest.mark.parametrize("shape", [(1, 1, 1, 1), (2, 3, 4, 5), (2, 16, 7, 9), (4, 128, 56, 56)])
+@pytest.mark.parametrize("shape", [(1, 1, 1, 1), (2, 3, 4, 5), (2, 16, 7, 9), (4, 128, 56, 56), (64, 128, 56, 56)])
 def test_view_heavy_fused_op_bit_exact(cuda_device, shape):
     T = cuda_device.Tensor
     x, bias, y, t, s = _c2(T, *shape)
