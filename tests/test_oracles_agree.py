@@ -64,3 +64,23 @@ def test_convolution_agrees():
         b = T.randomNormal([2], seed=0x40000005)
         outs.append(np.asarray(bench.conv_expr(T, x, w, b).flatArray(), np.float32))
     assert np.array_equal(outs[0].view(np.int32), outs[1].view(np.int32))
+
+
+def test_scaled_joined_and_reshaped_views_agree():
+    """Non-integer `scale` coefficients (DecimalFormat text, truncation of a
+    double index), `join` along the last and a middle dimension, `transpose`,
+    `reshape` and `broadcast`: the same bits from both restatements."""
+    outs = []
+    for d in _devices():
+        T = d.Tensor
+        a = T.random([7, 9], seed=4)
+        b = T.random([7, 9], seed=5)
+        s = a.scale([12, 5]).translate([0.5, -1.25])
+        j = T.join([a, b * T.fill(2.0, [7, 9]), T.abs(a - b)])
+        j1 = T.join([a, b], 1)
+        t = (a.transpose() + b.transpose()).reshape([3, 21])
+        c = T.random([1, 9], seed=6).broadcast([7, 9]) * a
+        outs.append([np.asarray(v.flatArray(), np.float32) for v in (s, j, j1, t, c)])
+    for x, y in zip(*outs):
+        assert x.shape == y.shape
+        assert np.array_equal(x.view(np.int32), y.view(np.int32))
