@@ -223,6 +223,7 @@ def setup(workload, d):
             sets.append([buf, bias._cached])
         out = rt.alloc(n * h * w * 4)
         return dict(prog=prog, sets=sets, out=out, bytes=c2_bytes(n, c, h, w), copies=copies,
+                    owned=[s_[0] for s_ in sets],
                     keep=[x, bias], ser=ser, shape=(n, c, h, w),
                     config={"workload": arm_workload("c2"),
                             "x": [n, c, h, w], "bias": [c], "out": [n, h, w],
@@ -245,6 +246,7 @@ def setup(workload, d):
             sets.append(trip)
         out = rt.alloc(4)
         return dict(prog=prog, sets=sets, out=out, bytes=c1_bytes(n, m), copies=copies, keep=abc, ser=ser,
+                    owned=[b_ for trip in sets for b_ in trip],
                     shape=(n, m),
                     config={"workload": arm_workload("c1"),
                             "l2": "inputs rotate over %d copies of (a,b,c) (%.0f MB > 4x L2)"
@@ -262,14 +264,17 @@ def setup(workload, d):
         xbytes = n * h * w * c * 4
         copies = max(2, -(-4 * L2_BYTES // xbytes))
         sets = []
+        owned = []
         for i in range(copies):
             buf = rt.alloc(xbytes)
+            owned.append(buf)
             rt.random(buf, n * h * w * c, C3_SEED, True)
             by_param = {id(x): buf, id(weight): weight._cached, id(bias): bias._cached}
             sets.append([by_param[id(p)] for p in ser.params])  # parameters in first-use order
         out = rt.alloc(n * h * w * c * 4)
         nbytes = 2 * xbytes + k * k * c * c * 4 + c * 4
         return dict(prog=prog, sets=sets, out=out, bytes=nbytes, copies=copies, keep=(x, weight, bias), ser=ser,
+                    owned=owned,
                     shape=(n, h, w, c),
                     config={"workload": arm_workload("c6"),
                             "flops_per_step": 2 * n * h * w * c * k * k * c,
@@ -287,6 +292,7 @@ def setup(workload, d):
         prog = rt.program(ser.text)
         out = rt.alloc(m * n * 4)
         return dict(prog=prog, sets=[[a._cached, b._cached]], out=out, flops=2.0 * m * n * k, bytes=4 * (m * k + k * n + m * n),
+                    owned=[],
                     keep=[a, b], ser=ser, shape=(m, k, n), copies=1,
                     config={"workload": arm_workload(workload),
                             "method": "split-BF16 (3 planes, 6 products) on tcgen05 tensor cores, FP32 accumulate",
@@ -295,19 +301,29 @@ def setup(workload, d):
     raise SystemExit("unknown workload " + workload)
 
 
+def release(st):
+    """Returns a workload's buffers to the pool."""
+    for b in st["owned"]:
+        b.release()
+    for t in st["keep"]:
+        t.close()
+    st["out"].release()
+
+
 def contraction_extras(d, st):
-    """Error of the split-BF16 result against float64, and the FP32 CUDA-core GEMM's speed and error."""
+    """Error of the split-BF16 result against float64 (512 sampled rows), and the
+    FP32 CUDA-core GEMM's speed, fraction of the FP32 CUDA-core peak and error."""
     import numpy as np
     rt = d.runtime
     m, k, n = st["shape"]
     a, b = st["keep"]
     rt.launch(st["prog"], st["sets"][0], st["out"])
-    c = rt.download(st["out"], m * n).reshape(m, n).astype(np.float64)
-    rows = np.random.RandomState(0).choice(m, size=min(m, 512), replace=False)
+    rows = np.sort(np.random.RandomState(0).choice(m, size=min(m, 512), replace=False))
+    c = np.stack([rt.download(st["out"], n, offset=int(r) * n * 4) for r in rows]).astype(np.float64)
     A = a.flatArray().reshape(m, k)[rows].astype(np.float64)
     B = b.flatArray().reshape(k, n).astype(np.float64)
     ref = A @ B
-    err = float(np.linalg.norm(c[rows] - ref) / np.linalg.norm(ref))
+    err = float(np.linalg.norm(c - ref) / np.linalg.norm(ref))
     out = rt.alloc(m * n * 4)
     args = (a._cached.device_ptr(), b._cached.device_ptr(), out.device_ptr(), m, n, k, rt.GEMM_FP32)
     rt.gemm_ptr(*args)
@@ -317,11 +333,17 @@ def contraction_extras(d, st):
     e1 = rt.event()
     rt.event_wait(e1)
     ms = rt.event_elapsed_ms(e0, e1) / 3
-    c32 = rt.download(out, m * n).reshape(m, n).astype(np.float64)
-    err32 = float(np.linalg.norm(c32[rows] - ref) / np.linalg.norm(ref))
+    c32 = np.stack([rt.download(out, n, offset=int(r) * n * 4) for r in rows]).astype(np.float64)
+    err32 = float(np.linalg.norm(c32 - ref) / np.linalg.norm(ref))
     out.release()
+    info = rt.device_info()
+    # FP32 CUDA-core peak: 128 FP32 lanes per SM, one FMA (2 flops) each per clock, at the maximum SM clock
+    fp32_peak = info["sm_count"] * 128 * 2 * 2070e6 / 1e12
+    fp32 = 2.0 * m * n * k / (ms * 1e-3) / 1e12
     return {"rel_fro_err_vs_fp64": err, "rows_checked": int(len(rows)),
-            "fp32_cuda_core_tflops": 2.0 * m * n * k / (ms * 1e-3) / 1e12, "fp32_cuda_core_rel_fro_err": err32}
+            "fp32_cuda_core_tflops": fp32, "fp32_cuda_core_rel_fro_err": err32,
+            "fp32_cuda_core_peak_tflops": fp32_peak, "fp32_cuda_core_frac_of_peak": fp32 / fp32_peak,
+            "fp32_cuda_core_peak_note": "SMs x 128 FP32 lanes x 2 flops x 2070 MHz (nominal)"}
 
 
 def time_device(rt, st, steps, warmup):
@@ -557,6 +579,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true", help="skip the clock sampling (and its untimed busy loop)")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="default workload only: skip the records of the other configurations")
+    ap.add_argument("--c5-eval-programs", type=int, default=400,
+                    help="tuning workloads the shipped cost model is evaluated on in the default run")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
 
@@ -600,26 +626,41 @@ def main():
         C1["n"] = C1["m"] = args.c1_side
     if args.workload == "c2":
         C2["n"] = args.c2_batch
-    st = setup(args.workload, d)
+    line = measure_fused(d, args.workload, args.steps, warmup, rank=rank, world=world, local_rank=local_rank,
+                         dist=dist, e2e_on=not args.no_e2e, cpu_on=rank == 0 and not args.no_cpu_baseline,
+                         clocks_on=not args.no_clocks)
+    if rank == 0 and world == 1 and args.workload == "c2" and not args.no_workloads:
+        line["workloads"] = measure_all_configs(d, args, warmup, local_rank)
+    if rank == 0:
+        emit(line)
+    if dist:
+        dist.destroy_process_group()
+
+
+def measure_fused(d, workload, steps, warmup, rank=0, world=1, local_rank=0, dist=None, e2e_on=True, cpu_on=True,
+                  clocks_on=True, cpu_budget_s=12.0):
+    """One fused-op workload (c1, c2, c6): the result line, without printing it."""
+    rt = d.runtime
+    st = setup(workload, d)
     sampler = ClockSampler(local_rank)
     if dist:
         dist.barrier()
     rt.synchronize()
-    if not args.no_clocks:
+    if clocks_on:
         sampler.start()
-    ms_total = time_device(rt, st, args.steps, warmup)
+    ms_total = time_device(rt, st, steps, warmup)
     clocks = None
-    if not args.no_clocks:
+    if clocks_on:
         keep_busy(rt, st, 1.5)
         clocks = sampler.stop()
     if dist:
         ms_total = max_over_ranks(dist, ms_total)
         dist.barrier()
-    ms_step = ms_total / args.steps
+    ms_step = ms_total / steps
     gbs_step = st["bytes"] / (ms_step * 1e-3) / 1e9
     value = gbs_step * world
     # the same launches on one input set, which then stays in L2 (reported beside, never as the value)
-    hot_ms = time_device(rt, dict(st, sets=st["sets"][:1]), args.steps, warmup) / args.steps
+    hot_ms = time_device(rt, dict(st, sets=st["sets"][:1]), steps, warmup) / steps
     hot = {"value": st["bytes"] / (hot_ms * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": hot_ms}
     iso_ms = time_isolated(rt, st, 50)
     overlap = {"pdl": rt.config_get("pdl") == 1,
@@ -627,33 +668,90 @@ def main():
                        "kernel's output issues its loads while that kernel drains; its stores wait for it",
                "isolated_launch": {"value": st["bytes"] / (iso_ms * 1e-3) / 1e9, "unit": "GB/s",
                                    "ms": iso_ms, "note": "one launch between two synchronisations, median of 50"}}
-
     e2e = None
-    if not args.no_e2e:
-        dt, h2d, d2h = time_e2e(d, st, steps=max(3, min(args.steps, 20)))
+    if e2e_on:
+        dt, h2d, d2h = time_e2e(d, st, steps=max(3, min(steps, 20)))
         e2e = {"value": st["bytes"] / dt / 1e9 * world, "unit": "GB/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
     peak, peak_kind = _peaks()
     roofline = {"bound": "hbm", "achieved": gbs_step, "peak": peak, "unit": "GB/s", "frac": gbs_step / peak,
-                "traffic": _traffic(args.workload), "peak_source": peak_kind,
+                "traffic": _traffic(workload), "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": st["bytes"]}
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if cpu_on:
         try:
-            r = cpu_reference(args.workload, budget_s=12.0)
+            r = cpu_reference(workload, budget_s=cpu_budget_s)
             cpu = {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port", "sample": r["sample"]}
         except Exception as e:  # the baseline is reported, not required
             cpu = {"value": None, "unit": "GB/s", "cores": None, "kind": "port", "sample": "failed: %s" % e}
-    if rank == 0:
-        line = {"metric": metric, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-                "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
-                "config": dict(st["config"], parallelism="replicas" if world > 1 else "single GPU"),
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-                "clocks": clocks, "hot_l2": hot, "launch_overlap": overlap}
-        emit(line)
-    if dist:
-        dist.destroy_process_group()
+    line = {"metric": "fused-op GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": steps,
+            "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
+            "config": dict(st["config"], parallelism="replicas" if world > 1 else "single GPU"),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": steps,
+            "clocks": clocks, "hot_l2": hot, "launch_overlap": overlap}
+    release(st)
+    return line
+
+
+def measure_all_configs(d, args, warmup, local_rank):
+    """Every other configuration of the benchmark, each as its own record (value,
+    roofline, cpu_baseline, e2e and clocks): the fused elementwise+sum, both
+    contractions, the batched programs and the shipped cost model on programs it
+    has not seen.  A configuration that fails records its error instead."""
+    out = {}
+    rt = d.runtime
+
+    def attempt(name, fn):
+        t0 = time.time()
+        try:
+            rec = fn()
+        except Exception as e:  # one configuration's failure does not hide the others
+            rec = {"error": "%s: %s" % (type(e).__name__, e)}
+        rec["wall_s"] = round(time.time() - t0, 1)
+        out[name] = rec
+        rt.synchronize()
+
+    attempt("c1", lambda: measure_fused(d, "c1", args.steps, warmup, local_rank=local_rank, cpu_budget_s=6.0,
+                                        clocks_on=not args.no_clocks))
+    for w in ("c3", "c3s"):
+        attempt(w, lambda w=w: measure_contraction(d, w, 20, warmup, local_rank=local_rank, cpu_budget_s=6.0,
+                                                   clocks_on=not args.no_clocks))
+    attempt("c4", lambda: measure_batch(d, 2048, 4194304, 20, warmup, local_rank=local_rank, cpu_budget_s=6.0,
+                                        clocks_on=not args.no_clocks))
+    attempt("c5_eval", lambda: measure_tuner_eval(rt, args.c5_eval_programs, 1, SHIPPED_MODEL))
+    return out
+
+
+SHIPPED_MODEL = os.path.join(ROOT, "compute.scala_gb300", "compute", "costmodel_gb300.npz")
+
+
+def measure_tuner_eval(rt, programs, seed, model_path):
+    """The shipped cost model on tuning workloads it was not trained on: every
+    program timed in all 48 configurations (exhaustive), the model's pick, the
+    fixed default and the best fixed configuration compared with the best."""
+    from compute import tuner
+    sm = rt.device_info()["sm_count"]
+    t0 = time.time()
+    progs = tuner.random_programs(programs, seed=seed)
+    recs = tuner.collect(rt, progs, reps=5, flush_l2=True)
+    collect_s = time.time() - t0
+    model = tuner.CostModel(rt, seed=0)
+    try:
+        model.load(model_path)
+        res = tuner.evaluate(model, recs, sm, fixed=30)
+    finally:
+        model.close()
+    return {"metric": "learned-tuner regret (geometric-mean slowdown vs exhaustive best), shipped model on "
+                      "unseen programs",
+            "value": res["learned"]["geomean_slowdown"], "unit": "fraction", "n_gpus": 1, "steps": 0,
+            "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded tuning workloads, seed %d)" % seed,
+            "config": {"workload": "tuning workloads as c5, %d programs, all evaluated" % len(recs),
+                       "model": os.path.relpath(model_path, ROOT),
+                       "timing": "median of 5 launches per config, L2 flushed"},
+            "tuner": res, "seconds": {"compile_and_time": round(collect_s, 1)},
+            "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": None}
 
 
 def main_tuner(args, warmup, rank, world, local_rank):
@@ -674,6 +772,10 @@ def main_tuner(args, warmup, rank, world, local_rank):
     rt = NativeRuntime(local_rank)
     apply_knobs(rt, args.knob)
     sm = rt.device_info()["sm_count"]
+    if args.eval_model and not args.db_in:
+        line = measure_tuner_eval(rt, args.programs, args.seed, args.eval_model)
+        emit(line)
+        return
     t0 = time.time()
     if args.db_in:
         recs = [json.loads(line) for line in open(args.db_in)][:args.programs]
@@ -694,17 +796,17 @@ def main_tuner(args, warmup, rank, world, local_rank):
         model = tuner.CostModel(rt, seed=0)
         model.load(args.eval_model)
         res = tuner.evaluate(model, recs, sm, fixed=30)
+        model.close()
         line = {"metric": "learned-tuner regret (geometric-mean slowdown vs exhaustive best), trained model on "
-                          "unseen programs",
+                          "recorded programs",
                 "value": res["learned"]["geomean_slowdown"], "unit": "fraction", "n_gpus": 1, "steps": 0,
                 "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32", "data": "synthetic (seeded tuning workloads, seed %d)" % args.seed,
-                "config": {"workload": "tuning workloads as c5, all %d programs evaluated" % len(recs),
-                           "model": args.eval_model, "timing": "median of 5 launches per config, L2 flushed"},
-                "tuner": res, "seconds": {"compile_and_time": round(collect_s, 1)},
-                "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": None}
+                "dtype": "f32", "data": "recorded timings (%s)" % args.db_in,
+                "config": {"workload": "tuning workloads as c5, %d programs evaluated" % len(recs),
+                           "model": args.eval_model},
+                "tuner": res, "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None,
+                "clocks": None}
         emit(line)
-        model.close()
         return
     split = int(len(recs) * 0.9)
     train, test = recs[:split], recs[split:]
@@ -745,18 +847,16 @@ def main_tuner(args, warmup, rank, world, local_rank):
     model.close()
 
 
-def main_batch(args, warmup, rank, world, local_rank):
-    """The batched-programs workload: 2048 independent fused programs evaluated by
-    one persistent launch; the same programs launched one by one, and replayed
-    from a CUDA graph, are the comparison."""
-    from compute import Tensors
+def measure_batch(d, programs, max_len, steps, warmup, local_rank=0, e2e_on=True, cpu_on=True, clocks_on=True,
+                  cpu_budget_s=12.0, world=1):
+    """The batched-programs workload: `programs` independent fused programs
+    evaluated by one persistent launch; the same programs launched one by one,
+    and replayed from a CUDA graph, are the comparison."""
     from compute.batch import Batch
-    d = Tensors(device=local_rank)
     rt = d.runtime
-    apply_knobs(rt, args.knob)
     T = d.Tensor
     t0 = time.time()
-    progs = c4_programs(T, seed=0, count=args.programs, hi=args.max_len)
+    progs = c4_programs(T, seed=0, count=programs, hi=max_len)
     tensors = [t for t, _ in progs]
     b = Batch(d, tensors).bind()
     setup_s = time.time() - t0
@@ -768,53 +868,53 @@ def main_batch(args, warmup, rank, world, local_rank):
         nbytes += 4 * n * (len(ser.params) + 1)
     n_progs, n_structs, regs, resident = rt.batch_info(b.handle)
 
-    def timed(mode, steps):
+    def timed(mode, k):
         for _ in range(max(3, warmup)):
             b.run(mode)
         rt.synchronize()
         e0 = rt.event()
-        for _ in range(steps):
+        for _ in range(k):
             b.run(mode)
         e1 = rt.event()
         rt.event_wait(e1, 600 * 10 ** 9)
-        ms = rt.event_elapsed_ms(e0, e1) / steps
+        ms = rt.event_elapsed_ms(e0, e1) / k
         rt.event_release(e0)
         rt.event_release(e1)
         return ms
 
     sampler = ClockSampler(local_rank)
-    if not args.no_clocks:
+    if clocks_on:
         sampler.start()
-    ms_persistent = timed(Batch.PERSISTENT, args.steps)
+    ms_persistent = timed(Batch.PERSISTENT, steps)
     clocks = None
-    if not args.no_clocks:
+    if clocks_on:
         t_end = time.time() + 1.5
         while time.time() < t_end:
             b.run(Batch.PERSISTENT)
             rt.synchronize()
         clocks = sampler.stop()
-    k2 = max(3, min(args.steps, 20))
+    k2 = max(3, min(steps, 20))
     ms_each = timed(Batch.PER_PROGRAM, k2)
     ms_graph = timed(Batch.GRAPH, k2)
     gbs = nbytes / (ms_persistent * 1e-3) / 1e9
     e2e = None
-    if not args.no_e2e:
+    if e2e_on:
         e2e = time_e2e_batch(d, b, progs, nbytes, steps=3)
     cpu = None
-    if not args.no_cpu_baseline:
+    if cpu_on:
         try:
             from oracle import cref
-            r = cref.time_programs(lambda T_: c4_programs(T_, seed=0, count=48, hi=args.max_len), budget_s=12.0)
+            r = cref.time_programs(lambda T_: c4_programs(T_, seed=0, count=48, hi=max_len), budget_s=cpu_budget_s)
             cpu = {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port", "sample": r["sample"]}
         except Exception as e:  # the baseline is reported, not required
             cpu = {"value": None, "unit": "GB/s", "cores": None, "kind": "port", "sample": "failed: %s" % e}
     peak, peak_kind = _peaks()
-    line = {"metric": "fused-op GB/s", "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+    line = {"metric": "fused-op GB/s", "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": steps,
             "warmup": warmup, "ms_per_step": ms_persistent, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
             "config": {"workload": "batched uneven programs: %d random fused programs (3-12 nodes over "
                                    "+,-,*,/,exp,log,tanh,max; 1-4 inputs U[0.1,2]), lengths log-uniform [1K,%d]"
-                                   % (args.programs, args.max_len),
+                                   % (programs, max_len),
                        "programs": n_progs, "distinct_structures": n_structs, "bytes_per_step": nbytes,
                        "persistent_registers": regs, "persistent_blocks_per_sm": resident,
                        "l2": "inputs %.1f GB > L2" % (nbytes / 1e9), "setup_s": round(setup_s, 1),
@@ -823,14 +923,84 @@ def main_batch(args, warmup, rank, world, local_rank):
                          "traffic": _traffic("c4"), "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes},
             "batch": {"persistent_ms": ms_persistent, "per_program_ms": ms_each, "graph_ms": ms_graph,
                       "speedup_vs_per_program": ms_each / ms_persistent, "speedup_vs_graph": ms_graph / ms_persistent},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clocks}
-    emit(line)
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": steps, "clocks": clocks}
     b.close()
+    for _, inputs in progs:
+        for i in inputs:
+            i.close()
+    return line
+
+
+def main_batch(args, warmup, rank, world, local_rank):
+    from compute import Tensors
+    d = Tensors(device=local_rank)
+    apply_knobs(d.runtime, args.knob)
+    line = measure_batch(d, args.programs, args.max_len, args.steps, warmup, local_rank=local_rank,
+                         e2e_on=not args.no_e2e, cpu_on=not args.no_cpu_baseline, clocks_on=not args.no_clocks,
+                         world=world)
+    emit(line)
+
+
+def measure_contraction(d, workload, steps, warmup, local_rank=0, e2e_on=True, cpu_on=True, clocks_on=True,
+                        cpu_budget_s=10.0, world=1):
+    """A contraction workload: TFLOP/s (2*M*N*K per step, counted once) of the
+    split-BF16 tensor-core path, reached through the Tensor API's matmul idiom."""
+    rt = d.runtime
+    saved = rt.config_get("contraction")
+    st = setup(workload, d)
+    try:
+        sampler = ClockSampler(local_rank)
+        rt.synchronize()
+        if clocks_on:
+            sampler.start()
+        ms_total = time_device(rt, st, steps, warmup)
+        clocks = None
+        if clocks_on:
+            keep_busy(rt, st, 1.5)
+            clocks = sampler.stop()
+        ms_step = ms_total / steps
+        tflops = st["flops"] / (ms_step * 1e-3) / 1e12
+        extras = contraction_extras(d, st)
+        e2e = None
+        if e2e_on:
+            dt, h2d, d2h = time_e2e(d, st, steps=3)
+            e2e = {"value": st["flops"] / dt / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
+    finally:
+        release(st)
+        rt.config_set("contraction", saved)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        peak, peak_kind = float(peaks["bf16_tflops"]), "measured"
+        sustained = float(peaks.get("bf16_tflops_sustained", peak))
+    except Exception:
+        peak, peak_kind, sustained = 1900.0, "fallback", 1700.0
+    roofline = {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                "traffic": _traffic(workload), "peak_source": peak_kind,
+                "tensor_work_frac": 6 * tflops / peak,
+                "tensor_work_frac_of_sustained": 6 * tflops / sustained,
+                "note": "achieved counts 2*M*N*K once; the tensor cores execute 6 bf16 products per output term; "
+                        "peak is the burst BF16 rate, the loop runs under the power cap (sustained rate %.1f)"
+                        % sustained}
+    cpu = None
+    if cpu_on:
+        try:
+            from oracle import cref
+            r = cref.time_contraction(C3[workload], budget_s=cpu_budget_s)
+            cpu = {"value": r["tflops"], "unit": "TFLOP/s", "cores": r["threads"], "kind": "port", "sample": r["sample"]}
+        except Exception as e:
+            cpu = {"value": None, "unit": "TFLOP/s", "cores": None, "kind": "port", "sample": "failed: %s" % e}
+    return {"metric": "matmul TFLOP/s", "value": tflops, "unit": "TFLOP/s", "n_gpus": world, "steps": steps,
+            "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3 split of f32 (fp32 accumulate)",
+            "data": "synthetic (seeded reference RNG)",
+            "config": dict(st["config"], parallelism="single GPU"), "roofline": roofline, "accuracy": extras,
+            "speedup_vs_fp32_cuda_core": tflops / extras["fp32_cuda_core_tflops"],
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": steps * 3, "clocks": clocks}
 
 
 def main_contraction(args, warmup, rank, world, local_rank):
-    """The contraction workloads: TFLOP/s (2*M*N*K per step, counted once) of the
-    split-BF16 tensor-core path, reached through the Tensor API's matmul idiom."""
     metric = "matmul TFLOP/s"
     if args.impl == "reference":
         if rank != 0:
@@ -849,57 +1019,9 @@ def main_contraction(args, warmup, rank, world, local_rank):
         return
     from compute import Tensors
     d = Tensors(device=local_rank)
-    rt = d.runtime
-    apply_knobs(rt, args.knob)
-    if args.workload == "c1":
-        C1["n"] = C1["m"] = args.c1_side
-    if args.workload == "c2":
-        C2["n"] = args.c2_batch
-    st = setup(args.workload, d)
-    sampler = ClockSampler(local_rank)
-    rt.synchronize()
-    if not args.no_clocks:
-        sampler.start()
-    ms_total = time_device(rt, st, args.steps, warmup)
-    clocks = None
-    if not args.no_clocks:
-        keep_busy(rt, st, 1.5)
-        clocks = sampler.stop()
-    ms_step = ms_total / args.steps
-    tflops = st["flops"] / (ms_step * 1e-3) / 1e12
-    extras = contraction_extras(d, st)
-    e2e = None
-    if not args.no_e2e:
-        dt, h2d, d2h = time_e2e(d, st, steps=3)
-        e2e = {"value": st["flops"] / dt / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-        peak, peak_kind = float(peaks["bf16_tflops"]), "measured"
-        sustained = float(peaks.get("bf16_tflops_sustained", peak))
-    except Exception:
-        peak, peak_kind, sustained = 1900.0, "fallback", 1700.0
-    roofline = {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
-                "traffic": _traffic(args.workload), "peak_source": peak_kind,
-                "tensor_work_frac": 6 * tflops / peak,
-                "tensor_work_frac_of_sustained": 6 * tflops / sustained,
-                "note": "achieved counts 2*M*N*K once; the tensor cores execute 6 bf16 products per output term; "
-                        "peak is the burst BF16 rate, the loop runs under the power cap (sustained rate %.1f)"
-                        % sustained}
-    cpu = None
-    if not args.no_cpu_baseline:
-        try:
-            from oracle import cref
-            r = cref.time_contraction(C3[args.workload], budget_s=10.0)
-            cpu = {"value": r["tflops"], "unit": "TFLOP/s", "cores": r["threads"], "kind": "port", "sample": r["sample"]}
-        except Exception as e:
-            cpu = {"value": None, "unit": "TFLOP/s", "cores": None, "kind": "port", "sample": "failed: %s" % e}
-    line = {"metric": metric, "value": tflops, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
-            "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16x3 split of f32 (fp32 accumulate)", "data": "synthetic (seeded reference RNG)",
-            "config": dict(st["config"], parallelism="single GPU"), "roofline": roofline, "accuracy": extras,
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * 3, "clocks": clocks}
+    apply_knobs(d.runtime, args.knob)
+    line = measure_contraction(d, args.workload, args.steps, warmup, local_rank=local_rank, e2e_on=not args.no_e2e,
+                               cpu_on=not args.no_cpu_baseline, clocks_on=not args.no_clocks, world=world)
     emit(line)
 
 

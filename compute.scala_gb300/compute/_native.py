@@ -141,6 +141,13 @@ _SIGNATURES = {
     "cc_compile_check": [ctypes.c_char_p, c_size, ctypes.c_int, ctypes.c_int, ctypes.c_uint32],
     "cc_launch": [c_handle, ctypes.POINTER(c_handle), ctypes.c_int, c_handle],
     "cc_launch_ptrs": [c_handle, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64],
+    "cc_launch_ev": [c_handle, ctypes.POINTER(c_handle), ctypes.c_int, c_handle, ctypes.POINTER(c_handle), ctypes.c_int,
+                     ctypes.POINTER(c_handle)],
+    "cc_buf_upload_ev": [c_handle, c_size, ctypes.c_void_p, c_size, ctypes.POINTER(c_handle), ctypes.c_int,
+                         ctypes.POINTER(c_handle)],
+    "cc_buf_download_ev": [c_handle, c_size, ctypes.c_void_p, c_size, ctypes.POINTER(c_handle), ctypes.c_int,
+                           ctypes.POINTER(c_handle)],
+    "cc_stream_wait_events": [ctypes.POINTER(c_handle), ctypes.c_int],
     "cc_reduce_sum_f32": [ctypes.c_uint64, c_size, ctypes.c_uint64, ctypes.c_uint64],
     "cc_reduce_sum_f32_noalloc": [ctypes.c_uint64, c_size, ctypes.c_uint64, ctypes.c_uint64],
     "cc_random": [c_handle, c_size, ctypes.c_uint32, ctypes.c_int],

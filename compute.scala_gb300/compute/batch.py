@@ -37,7 +37,9 @@ class Batch:
         self.outputs = []
         for k, (t, ser) in enumerate(zip(self.tensors, self.serialized)):
             for p in ser.params:
-                ptrs.append(p._buffer(self._ev).device_ptr())
+                buf = p._buffer(self._ev)
+                self._ev.wait(buf)  # the batch runs on the context stream
+                ptrs.append(buf.device_ptr())
             out = outputs[k] if outputs is not None else rt.alloc(max(1, _product(t.shape)) * 4)
             if outputs is None:
                 self._ev.owned.append(out)

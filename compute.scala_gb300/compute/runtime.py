@@ -144,6 +144,44 @@ class NativeRuntime:
         arr = (ctypes.c_uint64 * max(1, n))(*input_ptrs)
         call("cc_launch_ptrs", c_handle(prog.handle), arr, n, ctypes.c_uint64(out_ptr), ctypes.c_uint64(stream))
 
+    # -- the asynchronous DAG (a pool of streams ordered by event wait lists)
+    @staticmethod
+    def _wait_list(wait):
+        wait = list(wait or ())
+        return (c_handle * max(1, len(wait)))(*wait), len(wait)
+
+    def launch_ev(self, prog: Program, inputs: Sequence[DeviceBuffer], out: DeviceBuffer, wait=()) -> int:
+        """Kernel.enqueue with waitingEvents: returns the event of this launch."""
+        n = len(inputs)
+        arr = (c_handle * max(1, n))(*[b.handle for b in inputs])
+        w, nw = self._wait_list(wait)
+        ev = c_handle()
+        call("cc_launch_ev", c_handle(prog.handle), arr, n, c_handle(out.handle), w, nw, ctypes.byref(ev))
+        return ev.value
+
+    def upload_ev(self, buf: DeviceBuffer, host_ptr: int, nbytes: int, offset: int = 0, wait=()) -> int:
+        w, nw = self._wait_list(wait)
+        ev = c_handle()
+        call("cc_buf_upload_ev", c_handle(buf.handle), ctypes.c_size_t(offset), ctypes.c_void_p(host_ptr),
+             ctypes.c_size_t(nbytes), w, nw, ctypes.byref(ev))
+        return ev.value
+
+    def download_ev(self, buf: DeviceBuffer, host_ptr: int, nbytes: int, offset: int = 0, wait=()) -> int:
+        w, nw = self._wait_list(wait)
+        ev = c_handle()
+        call("cc_buf_download_ev", c_handle(buf.handle), ctypes.c_size_t(offset), ctypes.c_void_p(host_ptr),
+             ctypes.c_size_t(nbytes), w, nw, ctypes.byref(ev))
+        return ev.value
+
+    def stream_wait(self, events):
+        w, nw = self._wait_list(events)
+        call("cc_stream_wait_events", w, nw)
+
+    def event_query(self, ev: int) -> bool:
+        done = ctypes.c_int()
+        call("cc_event_query", c_handle(ev), ctypes.byref(done))
+        return bool(done.value)
+
     # -- fixed kernels
     def random(self, buf: DeviceBuffer, n: int, seed: int, normal: bool):
         call("cc_random", c_handle(buf.handle), ctypes.c_size_t(int(n)), ctypes.c_uint32(seed & 0xFFFFFFFF),

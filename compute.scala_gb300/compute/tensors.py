@@ -56,15 +56,32 @@ def _product(shape) -> int:
 
 class _Evaluation:
     """One slow action: memoises each tensor's buffer and releases the
-    intermediates at the end (the reference's ``Do`` resource scope)."""
+    intermediates at the end (the reference's ``Do`` resource scope).
+
+    With the device's queue pool on, a buffer may still be pending: ``events``
+    maps its handle to the event after which it holds its values (the
+    reference's ``PendingBuffer.eventOption``, Tensors.scala:253-299)."""
 
     def __init__(self, device: "Tensors"):
         self.device = device
         self.memo: Dict[int, object] = {}
         self.owned: List[object] = []
         self.keep: List[object] = []
+        self.events: Dict[int, int] = {}
+
+    def event_of(self, buf) -> Optional[int]:
+        return self.events.get(buf.handle) if self.events else None
+
+    def wait(self, buf) -> None:
+        """Blocks until ``buf`` holds its values (Event.waitFor)."""
+        e = self.event_of(buf)
+        if e is not None:
+            self.device.runtime.event_wait(e, 600 * 10 ** 9)
 
     def close(self, keep=None):
+        for e in self.events.values():
+            self.device.runtime.event_release(e)
+        self.events.clear()
         for b in self.owned:
             if b is not keep:
                 b.release()
@@ -236,6 +253,7 @@ class Tensor:
         ev = _Evaluation(self.device)
         try:
             buf = self._buffer(ev)
+            ev.wait(buf)
             buf.retain()
         finally:
             ev.close()
@@ -246,7 +264,17 @@ class Tensor:
         ev = _Evaluation(self.device)
         try:
             buf = self._buffer(ev)
-            return self.device.runtime.download(buf, _product(self.shape))
+            rt = self.device.runtime
+            if ev.event_of(buf) is None:
+                return rt.download(buf, _product(self.shape))
+            # toHostBuffer: a read that waits for the buffer's event (OpenCL.scala:698-715)
+            out = np.empty(_product(self.shape), dtype=np.float32)
+            done = rt.download_ev(buf, out.ctypes.data, out.nbytes, wait=[ev.event_of(buf)])
+            try:
+                rt.event_wait(done, 600 * 10 ** 9)
+            finally:
+                rt.event_release(done)
+            return out
         finally:
             ev.close()
 
@@ -499,6 +527,8 @@ class _TensorCompanion:
             buf = device.runtime.alloc(max(1, alloc) * 4)
             ev.owned.append(buf)
             device.runtime.random(buf, size, seed32, normal)
+            if device.queues:
+                ev.events[buf.handle] = device.runtime.event()  # on the context stream
             return buf
 
         return NonInlineTensor(device, shape, padding, compute, kind="randomNormal" if normal else "random")
@@ -574,9 +604,15 @@ class Tensors:
     runtime (``_native``/``runtime.NativeRuntime``) is created on first use.
     """
 
-    def __init__(self, device: int = 0, flags: int = 0, planner: Optional[trees.Planner] = None, runtime=None):
+    def __init__(self, device: int = 0, flags: int = 0, planner: Optional[trees.Planner] = None, runtime=None,
+                 queues: bool = False):
         self.device_ordinal = device
         self.flags = flags
+        # queues=True: every kernel of an action goes to the runtime's queue pool and
+        # waits only for the events of the buffers it reads, as the reference's
+        # CompiledKernel.run enqueues with its inputs' events (Tensors.scala:1331-1381);
+        # independent subgraphs then run concurrently.  False: one ordered stream.
+        self.queues = queues
         self.planner = planner if planner is not None else trees.Planner()
         self._runtime = runtime
         self.Tensor = _TensorCompanion(self)
@@ -623,5 +659,9 @@ class Tensors:
         n_out = 1 if kind == "sum" else _product(shape) * tuple_len
         out = self.runtime.alloc(max(1, n_out) * 4)
         ev.owned.append(out)
-        self.runtime.launch(prog, inputs, out)
+        if self.queues:
+            wait = [e for e in (ev.event_of(b) for b in inputs) if e is not None]
+            ev.events[out.handle] = self.runtime.launch_ev(prog, inputs, out, wait)
+        else:
+            self.runtime.launch(prog, inputs, out)
         return out

@@ -606,13 +606,12 @@ template <int BN, int STAGES, int ACC_BUFS, int KC>
 cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc, int sm_count,
                            int group_m, int *err, cudaStream_t stream) {
   using Cfg = TcCfg<BN, STAGES, ACC_BUFS>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS, KC>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  // The dynamic shared-memory limit is a per-device attribute of the kernel; set
+  // it on every launch (a cheap host call) so a second device, or another thread,
+  // never launches without it.
+  cudaError_t e = cudaFuncSetAttribute(gemm_bf16x6_kernel<BN, STAGES, ACC_BUFS, KC>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmemBytes);
+  if (e != cudaSuccess) return e;
   const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
   const int num_tiles = tiles_m * tiles_n;
   const int num_kb = K_padded / BK;

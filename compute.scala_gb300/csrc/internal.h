@@ -3,6 +3,7 @@
 
 #include <cuda.h>
 
+#include <atomic>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -47,6 +48,12 @@ struct Driver {
   decltype(&::cuLinkDestroy) LinkDestroy = nullptr;
 };
 extern Driver g_drv;
+
+// Operations enqueued by entry points that run without the context lock (the
+// sum without a context, cc_reduce_sum_f32_noalloc): a generated kernel starts
+// its loads early only if this count has not moved since the previous
+// generated kernel was launched.
+extern std::atomic<uint64_t> g_foreign_enqueues;
 
 // ---- IR (the alpha-converted expression tree; format documented in compute/trees.py)
 enum class NodeKind : uint8_t { Param, Literal, Extract, View, Unary, Binary, Tuple };

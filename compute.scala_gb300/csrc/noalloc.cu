@@ -13,6 +13,8 @@
 #include <cstdint>
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "device_common.cuh"
 #include "internal.h"
@@ -30,7 +32,7 @@ constexpr size_t kNoAllocScratchBytes = kNoAllocPartialBytes + 256;             
 
 // The scratch itself.  In host code `g_noalloc_scratch` names a host-side
 // stand-in, not device memory: host code must use the address that
-// cudaGetSymbolAddress returns for the current device (see scratch_address).
+// cudaGetSymbolAddress returns in the current context (see scratch_address).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Each block sums its own chunk [blockIdx.x * kNoAllocChunk, +kNoAllocChunk)
@@ -60,25 +62,70 @@ __global__ void __launch_bounds__(256) sum_noalloc_kernel(const float *__restric
   cc_grid_finish(s, c, partials, counter, out);
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void *g_scratch_addr[kMaxDevices] = {};
+// The scratch's device address belongs to the CUDA context that loaded this
+// library's module on the device (the primary context, or a host framework's
+// own driver-API context), not to the device number: after cudaDeviceReset, or
+// under another context, the same array has another address.  Set-up therefore
+// runs once per context, keyed by the context's unique ID (cuCtxGetId, which a
+// re-created context never repeats), with that context current.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
 
-// Set-up, once per device, with that device current: the device address of the
-// scratch array.  The first call of the entry point on a device performs it.
-void *scratch_address(int device) {
-  if (device < 0 || device >= kMaxDevices) fail(CC_ERR_INVALID_VALUE, "device ordinal out of range");
-  std::lock_guard<std::mutex> g(g_setup_mu);
-  if (!g_scratch_addr[device]) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) {
-      cudaGetLastError();
-      fail(CC_ERR_CUDA, std::string("cudaGetSymbolAddress of the sum scratch failed: ") + cudaGetErrorString(e));
-    }
-    g_scratch_addr[device] = ptr;
+struct ScratchSetup {
+  std::mutex mu;
+  bool resolved = false;
+  CtxGetCurrentFn ctx_get_current = nullptr;
+  CtxGetIdFn ctx_get_id = nullptr;
+  std::vector<std::pair<unsigned long long, void *>> addr;  // context ID -> scratch address
+};
+ScratchSetup g_setup;
+
+template <class F>
+F driver_entry(const char *symbol) {
+  cudaDriverEntryPointQueryResult q;
+  void *p = nullptr;
+  cudaError_t e = cudaGetDriverEntryPointByVersion(symbol, &p, 12000, cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+    cudaGetLastError();
+    fail(CC_ERR_CUDA, std::string("driver entry point ") + symbol + " is unavailable");
   }
-  return g_scratch_addr[device];
+  return reinterpret_cast<F>(p);
+}
+
+void *symbol_address() {
+  void *ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess || !ptr) {
+    cudaGetLastError();
+    fail(CC_ERR_CUDA, std::string("cudaGetSymbolAddress of the sum scratch failed: ") + cudaGetErrorString(e));
+  }
+  return ptr;
+}
+
+// The device address of the scratch in the calling thread's current context.
+void *scratch_address() {
+  std::lock_guard<std::mutex> g(g_setup.mu);
+  if (!g_setup.resolved) {
+    g_setup.ctx_get_current = driver_entry<CtxGetCurrentFn>("cuCtxGetCurrent");
+    g_setup.ctx_get_id = driver_entry<CtxGetIdFn>("cuCtxGetId");
+    g_setup.resolved = true;
+  }
+  CUcontext cur = nullptr;
+  if (g_setup.ctx_get_current(&cur) != CUDA_SUCCESS) cur = nullptr;
+  void *fresh = nullptr;
+  if (!cur) {
+    // No context is current yet: this runtime call makes the current device's
+    // primary context current (it allocates nothing).
+    fresh = symbol_address();
+    if (g_setup.ctx_get_current(&cur) != CUDA_SUCCESS || !cur) fail(CC_ERR_CUDA, "no current CUDA context");
+  }
+  unsigned long long id = 0;
+  if (g_setup.ctx_get_id(cur, &id) != CUDA_SUCCESS) fail(CC_ERR_CUDA, "cuCtxGetId failed");
+  for (const auto &kv : g_setup.addr)
+    if (kv.first == id) return kv.second;
+  if (!fresh) fresh = symbol_address();
+  g_setup.addr.emplace_back(id, fresh);
+  return fresh;
 }
 
 }  // namespace
@@ -92,18 +139,14 @@ extern "C" int cc_reduce_sum_f32_noalloc(uint64_t in_ptr, size_t n, uint64_t out
       fail(CC_ERR_INVALID_VALUE, "cc_reduce_sum_f32_noalloc: n = " + std::to_string(n) +
                                      " exceeds the fixed scratch capacity of " +
                                      std::to_string(kNoAllocMaxElements) + " floats");
-    int device = 0;
-    cudaError_t e = cudaGetDevice(&device);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      fail(CC_ERR_DEVICE_NOT_FOUND, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    }
-    char *scratch = static_cast<char *>(scratch_address(device));
+    char *scratch = static_cast<char *>(scratch_address());
+    // a generated kernel launched next must not start its loads before this sum ends
+    g_foreign_enqueues.fetch_add(1, std::memory_order_acq_rel);
     auto *partials = reinterpret_cast<float2 *>(scratch);
     auto *counter = reinterpret_cast<unsigned int *>(scratch + kNoAllocPartialBytes);
     auto s = reinterpret_cast<cudaStream_t>(stream);
     // The array keeps the previous call's contents; the completion counter must start at zero.
-    e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) {
       cudaGetLastError();
       fail(CC_ERR_CUDA, std::string("cudaMemsetAsync of the sum counter: ") + cudaGetErrorString(e));

@@ -44,6 +44,8 @@ void record_error(const std::string &message) { t_last_error = message; }
 // library loads (and its GPU-free entry points work) on hosts without a driver.
 Driver g_drv;
 
+std::atomic<uint64_t> g_foreign_enqueues{0};
+
 namespace {
 
 void check_cuda(cudaError_t e, const char *what) {
@@ -96,13 +98,41 @@ void check_cu(CUresult r, const char *what) {
   fail(code, std::string(what) + ": " + (name ? name : "?") + " (" + (str ? str : "?") + ")");
 }
 
+// ---------------------------------------------------------------- fences
+//
+// A point recorded in a stream (a CUDA event without timing), shared by every
+// holder: an event handle returned by an *_ev entry point, or a block of the
+// pool released while work on several streams may still use it.  Its CUDA
+// event returns to a free list when the last holder drops it.
+struct Fence {
+  cudaEvent_t ev = nullptr;
+  cudaStream_t stream = nullptr;
+};
+using FencePtr = std::shared_ptr<Fence>;
+
+bool fences_done(std::vector<FencePtr> &fences) {
+  for (auto it = fences.begin(); it != fences.end();) {
+    cudaError_t r = cudaEventQuery((*it)->ev);
+    if (r == cudaSuccess) {
+      it = fences.erase(it);
+    } else {
+      if (r != cudaErrorNotReady) cudaGetLastError();
+      return false;
+    }
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------- buffer pool
 //
 // Blocks are binned by size class (eight classes per power of two above 4 KiB,
-// so at most 12.5% slack).  A released block goes back to its class's free
-// list; work is ordered on the context stream, so a later allocation may reuse
-// it at once.  A cap (cc_pool_set_limit) turns allocations past it into
-// CC_ERR_OUT_OF_MEMORY, the reference's MemObjectAllocationFailure.
+// so at most 12.5% slack).  While all work is ordered on the context stream, a
+// released block goes back to its class's free list and a later allocation may
+// reuse it at once.  Once the queue pool is in use (the *_ev entry points), a
+// released block carries fences recorded on every stream that may still read
+// or write it and waits on a deferred list until they have all completed.  A
+// cap (cc_pool_set_limit) turns allocations past it into CC_ERR_OUT_OF_MEMORY,
+// the reference's MemObjectAllocationFailure.
 class Pool {
  public:
   static size_t size_class(size_t bytes) {
@@ -120,6 +150,7 @@ class Pool {
   void *alloc(size_t bytes, size_t *cls_out) {
     size_t cls = size_class(bytes == 0 ? 1 : bytes);
     *cls_out = cls;
+    reclaim();
     auto it = free_.find(cls);
     if (it != free_.end() && !it->second.empty()) {
       void *p = it->second.back();
@@ -150,13 +181,29 @@ class Pool {
     return p;
   }
 
-  void release(void *p, size_t cls) {
+  void release(void *p, size_t cls, std::vector<FencePtr> fences = {}) {
     in_use_ -= cls;
     cached_ += cls;
-    free_[cls].push_back(p);
+    if (fences.empty())
+      free_[cls].push_back(p);
+    else
+      deferred_.push_back(Deferred{p, cls, std::move(fences)});
+  }
+
+  // Deferred blocks whose fences have all completed become free.
+  void reclaim() {
+    for (auto it = deferred_.begin(); it != deferred_.end();) {
+      if (fences_done(it->fences)) {
+        free_[it->cls].push_back(it->p);
+        it = deferred_.erase(it);
+      } else {
+        ++it;
+      }
+    }
   }
 
   void trim() {
+    reclaim();
     for (auto &kv : free_) {
       for (void *p : kv.second) {
         cudaFree(p);
@@ -170,7 +217,13 @@ class Pool {
   uint64_t allocs_ = 0, reuses_ = 0;
 
  private:
+  struct Deferred {
+    void *p;
+    size_t cls;
+    std::vector<FencePtr> fences;
+  };
   std::map<size_t, std::vector<void *>> free_;
+  std::vector<Deferred> deferred_;
 };
 
 struct Buffer {
@@ -257,8 +310,14 @@ struct Program {
 };
 
 struct Event {
-  cudaEvent_t ev = nullptr;
+  cudaEvent_t ev = nullptr;  // a timing event (cc_event_record), or the fence's event
+  FencePtr fence;            // set for events returned by the *_ev entry points
 };
+
+// The queue pool: streams that the *_ev entry points spread independent work
+// over, as the reference's CommandQueuePool spreads it over command queues
+// (OpenCL.scala:423-448, 5 per device).
+constexpr int kQueues = 5;
 
 // Many independent programs evaluated together (cc_batch_*).
 struct Batch {
@@ -292,6 +351,7 @@ struct Context {
   uint32_t flags = 0;
 
   std::recursive_mutex mu;
+  std::vector<cudaEvent_t> free_events;  // of dropped fences (declared before the pool, which holds fences)
   Pool pool;
   uint64_t next_id = 1;
   std::unordered_map<uint64_t, Buffer *> buffers;
@@ -330,15 +390,28 @@ struct Context {
   int pdl = 1;           // launch generated kernels with programmatic dependent launch
   int copy_kernel = 0;   // copies between pinned host memory and the device by the SMs
   // The output range of the last generated kernel launched, and its stream: a
-  // kernel that reads none of it may start its loads before that kernel ends.
+  // kernel that reads none of it may start its loads before that kernel ends,
+  // provided nothing else was enqueued on the stream since.  Every entry point
+  // that enqueues other work under the context lock clears `valid`
+  // (end_pdl_chain); the sum without a context (cc_reduce_sum_f32_noalloc)
+  // bumps g_foreign_enqueues instead, which `foreign` remembers.
   struct {
     cudaStream_t stream = nullptr;
     uint64_t lo = 0, hi = 0;
+    uint64_t foreign = 0;
     bool valid = false;
   } last_write;
   int tc_group_m = 1;    // tensor-core GEMM: tile rows per group of the tile order (1 = row-major)
   cudaStream_t copy_streams[8] = {};
   cudaEvent_t copy_events[9] = {};
+
+  // The queue pool, created by the first *_ev call (multi_queue then stays on).
+  bool multi_queue = false;
+  cudaStream_t queues[kQueues] = {};
+  bool queue_dirty[kQueues] = {};  // work enqueued since the last cc_synchronize
+  int next_queue = 0;
+  void *queue_scratch[kQueues] = {};  // each queue's sum partials and counter
+  size_t queue_scratch_cls[kQueues] = {};
 
   // Scratch of the grid sums: kMaxSumBlocks float2 partials, then the counter.
   void *sum_scratch = nullptr;
@@ -376,6 +449,101 @@ Context &ctx() {
 
 uint64_t tag_of(uint64_t h) { return h >> 56; }
 
+// Work other than a generated kernel is about to be enqueued: the next
+// generated kernel must wait for it before its first load.
+void end_pdl_chain(Context &c) { c.last_write.valid = false; }
+
+// ---------------------------------------------------------------- queue pool and fences
+
+constexpr size_t kSumScratchBytes = sizeof(float2) * kMaxSumBlocks + 256;  // partials, counter, flags
+
+// A fence recorded on `s` now (the context lock is held).
+FencePtr record_fence(Context &c, cudaStream_t s) {
+  cudaEvent_t ev = nullptr;
+  if (!c.free_events.empty()) {
+    ev = c.free_events.back();
+    c.free_events.pop_back();
+  } else {
+    check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+  }
+  cudaError_t r = cudaEventRecord(ev, s);
+  if (r != cudaSuccess) {
+    c.free_events.push_back(ev);
+    check_cuda(r, "cudaEventRecord");
+  }
+  Context *cp = &c;
+  return FencePtr(new Fence{ev, s}, [cp](Fence *f) {
+    cp->free_events.push_back(f->ev);
+    delete f;
+  });
+}
+
+// The queue pool starts after everything already enqueued on the context
+// stream, so blocks that stream released earlier are safe to reuse there.
+void enter_multi_queue(Context &c) {
+  if (c.multi_queue) return;
+  for (int i = 0; i < kQueues; ++i) {
+    if (!c.queues[i]) check_cuda(cudaStreamCreateWithFlags(&c.queues[i], cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!c.queue_scratch[i]) {
+      c.queue_scratch[i] = c.pool.alloc(kSumScratchBytes, &c.queue_scratch_cls[i]);
+      check_cuda(cudaMemsetAsync(c.queue_scratch[i], 0, kSumScratchBytes, c.stream), "cudaMemsetAsync");
+    }
+  }
+  FencePtr f = record_fence(c, c.stream);
+  for (int i = 0; i < kQueues; ++i) check_cuda(cudaStreamWaitEvent(c.queues[i], f->ev, 0), "cudaStreamWaitEvent");
+  c.multi_queue = true;
+}
+
+// The next queue, round robin (the reference's dispatch takes one from its pool).
+int pick_queue(Context &c) {
+  enter_multi_queue(c);
+  const int q = c.next_queue;
+  c.next_queue = (q + 1) % kQueues;
+  return q;
+}
+
+int queue_index(const Context &c, cudaStream_t s) {
+  for (int i = 0; i < kQueues; ++i)
+    if (c.multi_queue && c.queues[i] == s) return i;
+  return -1;
+}
+
+// Returns a block to the pool.  With the queue pool in use, work on the
+// context stream and on every queue that has work pending may still use the
+// block, so it is deferred behind a fence on each of them.
+void release_block(Context &c, void *p, size_t cls) {
+  if (!c.multi_queue) {
+    c.pool.release(p, cls);
+    return;
+  }
+  std::vector<FencePtr> fences;
+  fences.push_back(record_fence(c, c.stream));
+  for (int i = 0; i < kQueues; ++i)
+    if (c.queue_dirty[i]) fences.push_back(record_fence(c, c.queues[i]));
+  c.pool.release(p, cls, std::move(fences));
+}
+
+// The partials and completion counter a grid sum on stream `s` uses: the
+// context's own on the context stream, each queue's own on the queues (sums on
+// different streams may run at once and must not share them).  Any other
+// (caller) stream gets a temporary block, zeroed on that stream; *temporary is
+// then set and the caller releases it after synchronising the stream.
+void *sum_scratch_for(Context &c, cudaStream_t s, size_t *temporary_cls) {
+  *temporary_cls = 0;
+  if (s == c.stream) return c.sum_scratch;
+  const int q = queue_index(c, s);
+  if (q >= 0) return c.queue_scratch[q];
+  size_t cls = 0;
+  void *p = c.pool.alloc(kSumScratchBytes, &cls);
+  cudaError_t e = cudaMemsetAsync(static_cast<char *>(p) + sizeof(float2) * kMaxSumBlocks, 0, 256, s);
+  if (e != cudaSuccess) {
+    c.pool.release(p, cls);
+    check_cuda(e, "cudaMemsetAsync");
+  }
+  *temporary_cls = cls;
+  return p;
+}
+
 Buffer &buffer_of(Context &c, cc_handle h) {
   auto it = c.buffers.find(h);
   if (tag_of(h) != kTagBuffer || it == c.buffers.end())
@@ -393,6 +561,22 @@ Event &event_of(Context &c, cc_handle h) {
   auto it = c.events.find(h);
   if (tag_of(h) != kTagEvent || it == c.events.end()) fail(CC_ERR_INVALID_EVENT, "not a live event handle");
   return *it->second;
+}
+
+// Makes `s` wait for every event of a wait list (Kernel.enqueue's waitingEvents).
+void wait_events(Context &c, cudaStream_t s, const cc_handle *wait, int n_wait) {
+  if (n_wait < 0 || (n_wait > 0 && !wait)) fail(CC_ERR_INVALID_VALUE, "bad wait list");
+  for (int i = 0; i < n_wait; ++i) check_cuda(cudaStreamWaitEvent(s, event_of(c, wait[i]).ev, 0), "cudaStreamWaitEvent");
+}
+
+// A new event handle for a fence (what the *_ev entry points return).
+cc_handle fence_handle(Context &c, FencePtr f) {
+  auto e = std::make_unique<Event>();
+  e->ev = f->ev;
+  e->fence = std::move(f);
+  uint64_t h = c.make_handle(kTagEvent);
+  c.events[h] = e.release();
+  return h;
 }
 
 // ---------------------------------------------------------------- NVRTC
@@ -470,7 +654,7 @@ void run_gemm(Context &c, const float *A, const float *B, float *C, int m, int n
   try {
     pb = c.pool.alloc(bytes_b, &cls_b);
   } catch (...) {
-    c.pool.release(pa, cls_a);
+    release_block(c, pa, cls_a);
     throw;
   }
   cudaError_t e = launch_split_a(A, lda, m, k, static_cast<__nv_bfloat16 *>(pa), Mp, Kp, c.sm_count, s);
@@ -486,15 +670,16 @@ void run_gemm(Context &c, const float *A, const float *B, float *C, int m, int n
                          gemm_tc_box_n(c.tc_variant) / 2);
       }
     } catch (...) {
-      c.pool.release(pa, cls_a);
-      c.pool.release(pb, cls_b);
+      release_block(c, pa, cls_a);
+      release_block(c, pb, cls_b);
       throw;
     }
     e = launch_gemm_bf16x6(maps, C, m, n, Kp, ldc, c.sm_count, c.error_flag(), c.tc_variant, c.tc_group_m, s);
   }
-  if (s != c.stream && e == cudaSuccess) e = cudaStreamSynchronize(s);  // the pool is ordered on the context stream
-  c.pool.release(pa, cls_a);
-  c.pool.release(pb, cls_b);
+  // blocks of the pool are ordered on the context stream and the queues; wait for other streams
+  if (s != c.stream && queue_index(c, s) < 0 && e == cudaSuccess) e = cudaStreamSynchronize(s);
+  release_block(c, pa, cls_a);
+  release_block(c, pb, cls_b);
   check_cuda(e, "bf16x6 contraction launch");
 }
 
@@ -504,7 +689,7 @@ std::shared_ptr<TuneModule> load_tune_module(const std::vector<char> &cubin);
 void load_tune_entry(TuneEntry &e, const Ir &ir, std::shared_ptr<TuneModule> mod, const std::string &suffix);
 
 void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
-  if (p.tune || p.is_contraction) c.last_write.valid = false;
+  if (p.tune || p.is_contraction) end_pdl_chain(c);
   if (p.tune) {
     launch_tuned_program(c, p, in, out, stream);
     return;
@@ -533,9 +718,11 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   int64_t nn = n;
   uint64_t partials = 0, counter = 0;
   unsigned grid;
+  size_t temporary = 0;  // a sum on a caller stream: its own scratch block, released after the launch
   if (p.kind == ProgramKind::Sum) {
-    partials = reinterpret_cast<uint64_t>(c.partials());
-    counter = reinterpret_cast<uint64_t>(c.counter());
+    char *scratch = static_cast<char *>(sum_scratch_for(c, stream, &temporary));
+    partials = reinterpret_cast<uint64_t>(scratch);
+    counter = reinterpret_cast<uint64_t>(scratch + sizeof(float2) * kMaxSumBlocks);
     args.push_back(&partials);
     args.push_back(&counter);
     grid = (unsigned)sum_grid_for(work, block, c.sm_count * c.sum_blocks_per_sm);
@@ -547,10 +734,14 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   }
   args.push_back(&out_ptr);
   args.push_back(&nn);
-  // early start: none of this kernel's inputs overlaps what the previous
-  // generated kernel on this stream writes (its stores still wait for it)
+  // early start: the previous operation on the context's own stream is the
+  // generated kernel last_write describes, and none of this kernel's inputs
+  // overlaps what it writes (the stores still wait for it).  A caller stream
+  // may carry the caller's own work, so launches there never start early.
+  const uint64_t foreign = g_foreign_enqueues.load(std::memory_order_acquire);
   int early = 0;
-  if (c.pdl && c.last_write.valid && c.last_write.stream == stream) {
+  if (c.pdl == 1 && c.last_write.valid && c.last_write.stream == stream && stream == c.own_stream &&
+      c.last_write.foreign == foreign) {
     early = 1;
     for (size_t i = 0; i < in.size(); ++i) {
       const uint64_t lo = in[i];
@@ -562,8 +753,10 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
   c.last_write.stream = stream;
   c.last_write.lo = out;
   c.last_write.hi = out + (uint64_t)(p.gen.out_elems > 0 ? p.gen.out_elems : 1) * sizeof(float);
-  c.last_write.valid = c.pdl != 0;
+  c.last_write.foreign = foreign;
+  c.last_write.valid = c.pdl == 1;
   const unsigned smem = vec || vl ? 0 : (unsigned)m.smem_bytes;
+  CUresult r;
   if (c.pdl) {
     // programmatic dependent launch: this grid may be scheduled while the
     // previous kernel in the stream drains; its cc_pdl_begin / cc_pdl_gate keep the order
@@ -581,11 +774,16 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
     cfg.hStream = (CUstream)stream;
     cfg.attrs = &attr;
     cfg.numAttrs = 1;
-    check_cu(g_drv.LaunchKernelEx(&cfg, f, args.data(), nullptr), "cuLaunchKernelEx");
-    return;
+    r = g_drv.LaunchKernelEx(&cfg, f, args.data(), nullptr);
+  } else {
+    r = g_drv.LaunchKernel(f, grid, 1, 1, block, 1, 1, smem, (CUstream)stream, args.data(), nullptr);
   }
-  check_cu(g_drv.LaunchKernel(f, grid, 1, 1, block, 1, 1, smem, (CUstream)stream, args.data(), nullptr),
-           "cuLaunchKernel");
+  if (temporary) {
+    cudaError_t se = r == CUDA_SUCCESS ? cudaStreamSynchronize(stream) : cudaSuccess;
+    c.pool.release(reinterpret_cast<void *>(partials), temporary);
+    check_cuda(se, "cudaStreamSynchronize");
+  }
+  check_cu(r, "cuLaunchKernel");
 }
 
 // Upload striped over the context's copy streams, ordered after the work
@@ -618,7 +816,7 @@ bool sm_copy(Context &c, void *dst, const void *src, size_t bytes, bool to_devic
     check_cuda(cudaMemcpyAsync(static_cast<char *>(dst) + body, static_cast<const char *>(src) + body, bytes - body,
                                to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, c.stream),
                "cudaMemcpyAsync");
-  c.last_write.valid = false;
+  end_pdl_chain(c);
   return true;
 }
 
@@ -725,25 +923,28 @@ int cc_shutdown(void) {
   cudaSetDevice(c->device);
   g_drv.CtxSetCurrent(c->cuctx);
   cudaStreamSynchronize(c->stream);
+  for (int i = 0; i < kQueues; ++i)
+    if (c->queues[i]) cudaStreamSynchronize(c->queues[i]);
+  c->multi_queue = false;  // every stream is idle: blocks go straight back to the pool
   for (auto &kv : c->programs) delete kv.second;
   c->modules.clear();
   for (auto &kv : c->batches) {
     Batch *b = kv.second;
     if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->table) c->pool.release(b->table, b->table_cls);
+    if (b->table) release_block(*c, b->table, b->table_cls);
     if (b->module) g_drv.ModuleUnload(b->module);
     delete b;
   }
   c->batches.clear();
   for (auto &kv : c->tune_sets) {
-    if (kv.second->flush) c->pool.release(kv.second->flush, kv.second->flush_cls);
+    if (kv.second->flush) release_block(*c, kv.second->flush, kv.second->flush_cls);
     delete kv.second;
   }
   c->tune_sets.clear();
   for (auto &kv : c->mlps) {
-    if (kv.second->scratch) c->pool.release(kv.second->scratch, kv.second->scratch_cls);
-    if (kv.second->state) c->pool.release(kv.second->state, kv.second->state_cls);
+    if (kv.second->scratch) release_block(*c, kv.second->scratch, kv.second->scratch_cls);
+    if (kv.second->state) release_block(*c, kv.second->state, kv.second->state_cls);
     delete kv.second;
   }
   c->mlps.clear();
@@ -753,11 +954,18 @@ int cc_shutdown(void) {
     delete kv.second;
   }
   for (auto &kv : c->events) {
-    cudaEventDestroy(kv.second->ev);
+    if (!kv.second->fence) cudaEventDestroy(kv.second->ev);
     delete kv.second;
   }
-  c->pool.release(c->sum_scratch, c->sum_scratch_cls);
+  c->events.clear();
+  release_block(*c, c->sum_scratch, c->sum_scratch_cls);
+  for (int i = 0; i < kQueues; ++i)
+    if (c->queue_scratch[i]) release_block(*c, c->queue_scratch[i], c->queue_scratch_cls[i]);
   c->pool.trim();
+  for (cudaEvent_t ev : c->free_events) cudaEventDestroy(ev);
+  c->free_events.clear();
+  for (int i = 0; i < kQueues; ++i)
+    if (c->queues[i]) cudaStreamDestroy(c->queues[i]);
   for (int i = 0; i < 8; ++i) cudaStreamDestroy(c->copy_streams[i]);
   for (int i = 0; i < 9; ++i) cudaEventDestroy(c->copy_events[i]);
   cudaStreamDestroy(c->own_stream);
@@ -787,6 +995,7 @@ int cc_set_stream(uint64_t stream) {
   CC_API_BEGIN
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   // Blocks freed so far may still be read by work on the old stream.
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
   c.stream = stream ? reinterpret_cast<cudaStream_t>(stream) : c.own_stream;
@@ -828,8 +1037,9 @@ int cc_config_set(const char *key, int64_t value) {
     if (value < 1 || value > 64) fail(CC_ERR_INVALID_VALUE, "tc_group_m must be in [1, 64]");
     c.tc_group_m = (int)value;
   } else if (k == "pdl") {
-    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "pdl must be 0 or 1");
+    if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "pdl must be 0, 1 or 2");
     c.pdl = (int)value;
+    end_pdl_chain(c);
   } else if (k == "ew_batch_loads") {
     if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "ew_batch_loads must be 0 or 1");
     c.ew_batch_loads = (int)value;
@@ -906,7 +1116,23 @@ int cc_config_get(const char *key, int64_t *value) {
 
 int cc_synchronize(void) {
   CC_API_BEGIN
-  check_cuda(cudaStreamSynchronize(ctx().stream), "cudaStreamSynchronize");
+  Context &c = ctx();
+  cudaStream_t s;
+  bool multi;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    s = c.stream;
+    multi = c.multi_queue;
+  }
+  check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  if (multi) {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    for (int i = 0; i < kQueues; ++i) {
+      check_cuda(cudaStreamSynchronize(c.queues[i]), "cudaStreamSynchronize");
+      c.queue_dirty[i] = false;
+    }
+    c.pool.reclaim();
+  }
   CC_API_END
 }
 
@@ -940,7 +1166,7 @@ int cc_buf_release(cc_handle h) {
   std::lock_guard<std::recursive_mutex> g(c.mu);
   Buffer &b = buffer_of(c, h);
   if (--b.refs == 0) {
-    c.pool.release(b.ptr, b.cls);
+    release_block(c, b.ptr, b.cls);
     delete &b;
     c.buffers.erase(h);
   }
@@ -971,6 +1197,7 @@ int cc_buf_upload(cc_handle h, size_t offset, const void *host, size_t bytes) {
   void *dst;
   {
     std::lock_guard<std::recursive_mutex> g(c.mu);
+    end_pdl_chain(c);
     Buffer &b = buffer_of(c, h);
     if (offset > b.bytes || bytes > b.bytes - offset) fail(CC_ERR_INVALID_VALUE, "upload range exceeds the buffer");
     dst = static_cast<char *>(b.ptr) + offset;
@@ -988,6 +1215,7 @@ int cc_buf_upload_async(cc_handle h, size_t offset, const void *host, size_t byt
   void *dst;
   {
     std::lock_guard<std::recursive_mutex> g(c.mu);
+    end_pdl_chain(c);
     Buffer &b = buffer_of(c, h);
     if (offset > b.bytes || bytes > b.bytes - offset) fail(CC_ERR_INVALID_VALUE, "upload range exceeds the buffer");
     dst = static_cast<char *>(b.ptr) + offset;
@@ -1004,6 +1232,7 @@ int cc_buf_download(cc_handle h, size_t offset, void *host, size_t bytes) {
   void *src;
   {
     std::lock_guard<std::recursive_mutex> g(c.mu);
+    end_pdl_chain(c);
     Buffer &b = buffer_of(c, h);
     if (offset > b.bytes || bytes > b.bytes - offset) fail(CC_ERR_INVALID_VALUE, "download range exceeds the buffer");
     src = static_cast<char *>(b.ptr) + offset;
@@ -1022,6 +1251,7 @@ int cc_buf_download_async(cc_handle h, size_t offset, void *host, size_t bytes) 
   void *src;
   {
     std::lock_guard<std::recursive_mutex> g(c.mu);
+    end_pdl_chain(c);
     Buffer &b = buffer_of(c, h);
     if (offset > b.bytes || bytes > b.bytes - offset) fail(CC_ERR_INVALID_VALUE, "download range exceeds the buffer");
     src = static_cast<char *>(b.ptr) + offset;
@@ -1373,6 +1603,80 @@ int cc_launch_ptrs(cc_handle prog, const uint64_t *input_ptrs, int n_inputs, uin
   CC_API_END
 }
 
+// ---------------------------------------------------------------- the asynchronous DAG
+
+int cc_launch_ev(cc_handle prog, const cc_handle *inputs, int n_inputs, cc_handle output, const cc_handle *wait,
+                 int n_wait, cc_handle *event) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Program &p = program_of(c, prog);
+  if (n_inputs != p.gen.n_inputs)
+    fail(CC_ERR_INVALID_KERNEL_ARGS, "program takes " + std::to_string(p.gen.n_inputs) + " inputs, got " +
+                                         std::to_string(n_inputs));
+  if (n_inputs > 0 && !inputs) fail(CC_ERR_INVALID_VALUE, "null input list");
+  std::vector<uint64_t> ptrs;
+  for (int i = 0; i < n_inputs; ++i) ptrs.push_back(reinterpret_cast<uint64_t>(buffer_of(c, inputs[i]).ptr));
+  Buffer &o = buffer_of(c, output);
+  if (o.bytes < (size_t)p.gen.out_elems * sizeof(float))
+    fail(CC_ERR_INVALID_VALUE, "output buffer holds " + std::to_string(o.bytes) + " bytes, the program writes " +
+                                   std::to_string(p.gen.out_elems * sizeof(float)));
+  if (n_wait < 0 || (n_wait > 0 && !wait)) fail(CC_ERR_INVALID_VALUE, "bad wait list");
+  for (int i = 0; i < n_wait; ++i) event_of(c, wait[i]);  // every handle valid before anything is enqueued
+  const int q = pick_queue(c);
+  cudaStream_t s = c.queues[q];
+  c.queue_dirty[q] = true;
+  wait_events(c, s, wait, n_wait);
+  launch_program(c, p, ptrs, reinterpret_cast<uint64_t>(o.ptr), s);
+  if (event) *event = fence_handle(c, record_fence(c, s));
+  CC_API_END
+}
+
+namespace {
+int copy_ev(cc_handle h, size_t offset, void *host, size_t bytes, bool to_device, const cc_handle *wait, int n_wait,
+            cc_handle *event) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Buffer &b = buffer_of(c, h);
+  if (offset > b.bytes || bytes > b.bytes - offset)
+    fail(CC_ERR_INVALID_VALUE, to_device ? "upload range exceeds the buffer" : "download range exceeds the buffer");
+  if (bytes && !host) fail(CC_ERR_INVALID_VALUE, "null host pointer");
+  if (n_wait < 0 || (n_wait > 0 && !wait)) fail(CC_ERR_INVALID_VALUE, "bad wait list");
+  for (int i = 0; i < n_wait; ++i) event_of(c, wait[i]);
+  const int q = pick_queue(c);
+  cudaStream_t s = c.queues[q];
+  c.queue_dirty[q] = true;
+  wait_events(c, s, wait, n_wait);
+  char *dev = static_cast<char *>(b.ptr) + offset;
+  if (bytes)
+    check_cuda(cudaMemcpyAsync(to_device ? static_cast<void *>(dev) : host, to_device ? static_cast<const void *>(host) : dev,
+                               bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s),
+               to_device ? "cudaMemcpyAsync H2D" : "cudaMemcpyAsync D2H");
+  if (event) *event = fence_handle(c, record_fence(c, s));
+  CC_API_END
+}
+}  // namespace
+
+int cc_buf_upload_ev(cc_handle buf, size_t offset, const void *host, size_t bytes, const cc_handle *wait, int n_wait,
+                     cc_handle *event) {
+  return copy_ev(buf, offset, const_cast<void *>(host), bytes, true, wait, n_wait, event);
+}
+
+int cc_buf_download_ev(cc_handle buf, size_t offset, void *host, size_t bytes, const cc_handle *wait, int n_wait,
+                       cc_handle *event) {
+  return copy_ev(buf, offset, host, bytes, false, wait, n_wait, event);
+}
+
+int cc_stream_wait_events(const cc_handle *events, int n_events) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
+  wait_events(c, c.stream, events, n_events);
+  CC_API_END
+}
+
 // ---------------------------------------------------------------- sums and random numbers
 
 int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stream) {
@@ -1380,6 +1684,7 @@ int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stre
   Context &c = ctx();
   if (!out_ptr || (n && !in_ptr)) fail(CC_ERR_INVALID_VALUE, "null pointer");
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   // Scratch for this call from the pool: partials, then the zeroed counter.
   size_t cls = 0;
@@ -1391,8 +1696,9 @@ int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stre
   if (e == cudaSuccess)
     e = launch_sum(reinterpret_cast<const float *>(in_ptr), (long long)n, partials, counter,
                    reinterpret_cast<float *>(out_ptr), c.sm_count, s);
-  if (s != c.stream && e == cudaSuccess) e = cudaStreamSynchronize(s);  // the pool is ordered on the context stream
-  c.pool.release(scratch, cls);
+  // blocks of the pool are ordered on the context stream and the queues; wait for other streams
+  if (s != c.stream && queue_index(c, s) < 0 && e == cudaSuccess) e = cudaStreamSynchronize(s);
+  release_block(c, scratch, cls);
   check_cuda(e, "sum launch");
   CC_API_END
 }
@@ -1404,6 +1710,7 @@ int cc_gemm_f32(uint64_t a_ptr, uint64_t b_ptr, uint64_t c_ptr, int m, int n, in
   if (!a_ptr || !b_ptr || !c_ptr) fail(CC_ERR_INVALID_VALUE, "null pointer");
   if (m < 0 || n < 0 || k <= 0 || lda < k || ldb < n || ldc < n) fail(CC_ERR_INVALID_VALUE, "bad matrix shape");
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   run_gemm(c, reinterpret_cast<const float *>(a_ptr), reinterpret_cast<const float *>(b_ptr),
            reinterpret_cast<float *>(c_ptr), m, n, k, lda, ldb, ldc, mode, s);
@@ -1415,7 +1722,7 @@ int cc_probe_bounded_wait(uint64_t limit_ns, int flag_value) {
   if (limit_ns > 10000000000ull) fail(CC_ERR_INVALID_VALUE, "limit_ns above 10 s");
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
-  c.last_write.valid = false;
+  end_pdl_chain(c);
   check_cuda(cudaMemsetAsync(c.probe_flag(), flag_value ? 1 : 0, sizeof(int), c.stream), "set probe flag");
   check_cuda(launch_flag_wait(c.probe_flag(), limit_ns, c.error_flag(), CC_DEVICE_ERR_PROBE_TIMEOUT, c.stream),
              "probe launch");
@@ -1427,6 +1734,7 @@ int cc_device_errors(int *code) {
   if (!code) fail(CC_ERR_INVALID_VALUE, "null pointer");
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   int v = 0;
   check_cuda(cudaMemcpyAsync(&v, c.error_flag(), sizeof(int), cudaMemcpyDeviceToHost, c.stream), "read error flag");
   check_cuda(cudaMemsetAsync(c.error_flag(), 0, sizeof(int), c.stream), "clear error flag");
@@ -1439,6 +1747,7 @@ int cc_random(cc_handle output, size_t n, uint32_t seed, int normal) {
   CC_API_BEGIN
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   Buffer &b = buffer_of(c, output);
   size_t need = normal ? ((n + 1) / 2) * 2 : n;
   if (b.bytes < need * sizeof(float)) fail(CC_ERR_INVALID_VALUE, "output buffer too small for the random numbers");
@@ -1520,7 +1829,7 @@ int cc_event_release(cc_handle h) {
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
   Event &e = event_of(c, h);
-  cudaEventDestroy(e.ev);
+  if (!e.fence) cudaEventDestroy(e.ev);  // a fence's event goes back to the free list with the fence
   delete &e;
   c.events.erase(h);
   CC_API_END
@@ -1822,6 +2131,7 @@ int cc_batch_create(const char *const *irs, const size_t *lens, int n_programs, 
              "cuFuncSetAttribute");
   check_cu(g_drv.OccupancyMaxActiveBlocks(&b->resident, b->persistent, kBatchBlock, smem), "occupancy");
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   uint64_t h = c.make_handle(kTagBatch);
   c.batches[h] = b.release();
   *out = h;
@@ -1869,6 +2179,7 @@ int cc_batch_bind(cc_handle batch, const uint64_t *ptrs, size_t n_ptrs) {
   CC_API_BEGIN
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   Batch &b = batch_of(c, batch);
   size_t need = 0;
   for (size_t p = 0; p < b.sid.size(); ++p) need += b.n_inputs[p] + 1;
@@ -1908,6 +2219,7 @@ int cc_batch_run(cc_handle batch, int mode, uint64_t stream) {
   CC_API_BEGIN
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   Batch &b = batch_of(c, batch);
   if (!b.bound) fail(CC_ERR_INVALID_OPERATION, "bind the batch's buffers first");
   cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
@@ -1962,7 +2274,7 @@ int cc_batch_release(cc_handle batch) {
   Batch &b = batch_of(c, batch);
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
   batch_drop_graph(b);
-  if (b.table) c.pool.release(b.table, b.table_cls);
+  if (b.table) release_block(c, b.table, b.table_cls);
   g_drv.ModuleUnload(b.module);
   delete &b;
   c.batches.erase(batch);
@@ -2024,8 +2336,10 @@ void launch_tune_entry(Context &c, TuneEntry &e, int config, const std::vector<u
   std::vector<uint64_t> ptrs(in);
   std::vector<void *> args;
   for (auto &v : ptrs) args.push_back(&v);
-  uint64_t partials = reinterpret_cast<uint64_t>(c.partials());
-  uint64_t counter = reinterpret_cast<uint64_t>(c.counter());
+  size_t temporary = 0;
+  char *scratch = sum ? static_cast<char *>(sum_scratch_for(c, s, &temporary)) : nullptr;
+  uint64_t partials = reinterpret_cast<uint64_t>(scratch);
+  uint64_t counter = reinterpret_cast<uint64_t>(scratch + sizeof(float2) * kMaxSumBlocks);
   uint64_t o = out;
   long long n = e.n;
   if (sum) {
@@ -2034,8 +2348,13 @@ void launch_tune_entry(Context &c, TuneEntry &e, int config, const std::vector<u
   }
   args.push_back(&o);
   args.push_back(&n);
-  check_cu(g_drv.LaunchKernel(e.fn[k], (unsigned)grid, 1, 1, t.block, 1, 1, 0, (CUstream)s, args.data(), nullptr),
-           "cuLaunchKernel");
+  CUresult r = g_drv.LaunchKernel(e.fn[k], (unsigned)grid, 1, 1, t.block, 1, 1, 0, (CUstream)s, args.data(), nullptr);
+  if (temporary) {
+    cudaError_t se = r == CUDA_SUCCESS ? cudaStreamSynchronize(s) : cudaSuccess;
+    c.pool.release(scratch, temporary);
+    check_cuda(se, "cudaStreamSynchronize");
+  }
+  check_cu(r, "cuLaunchKernel");
 }
 
 // Median device time (ms) over `reps` launches of each configuration, after
@@ -2097,7 +2416,7 @@ void mlp_reserve(Context &c, Mlp &m, int batch) {
   const size_t floats = (size_t)batch * acts + 2 * (size_t)batch * w + (size_t)colsum_chunks(batch) * w + 64;
   if (m.scratch) {
     check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
-    c.pool.release(m.scratch, m.scratch_cls);
+    release_block(c, m.scratch, m.scratch_cls);
     m.scratch = nullptr;
     m.cap = 0;
   }
@@ -2160,10 +2479,10 @@ int choose_exhaustive(Context &c, TuneEntry &e, const std::vector<uint64_t> &in,
   try {
     time_tune_entry(c, e, configs.data(), kTuneConfigs, in, out, 3, flush, kFlushBytes, ms.data());
   } catch (...) {
-    c.pool.release(flush, cls);
+    release_block(c, flush, cls);
     throw;
   }
-  c.pool.release(flush, cls);
+  release_block(c, flush, cls);
   int best = -1;
   for (int i = 0; i < kTuneConfigs; ++i)
     if (ms[i] >= 0.0f && (best < 0 || ms[i] < ms[best])) best = i;
@@ -2191,10 +2510,10 @@ int choose_learned(Context &c, TuneEntry &e, const std::vector<uint64_t> &in, ui
                "download");
     check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
   } catch (...) {
-    c.pool.release(dx, cls);
+    release_block(c, dx, cls);
     throw;
   }
-  c.pool.release(dx, cls);
+  release_block(c, dx, cls);
   int best = -1;
   for (int i = 0; i < kTuneConfigs; ++i)
     if (tune_config_fits(e, i, in, out) && (best < 0 || y[i] < y[best])) best = i;
@@ -2318,6 +2637,7 @@ int cc_tune_create(const char *const *irs, const size_t *lens, int n_programs, c
       load_tune_entry(ts->entries[p], parsed[p], mod, "_" + std::to_string(p));
   }
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   uint64_t h = c.make_handle(kTagTuneSet);
   c.tune_sets[h] = ts.release();
   *set = h;
@@ -2347,6 +2667,7 @@ int cc_tune_launch(cc_handle set, int program, const uint64_t *ptrs, size_t n_pt
   CC_API_BEGIN
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   TuneSet &ts = tune_set_of(c, set);
   if (program < 0 || program >= (int)ts.entries.size()) fail(CC_ERR_INVALID_VALUE, "program index out of range");
   TuneEntry &e = ts.entries[program];
@@ -2361,6 +2682,7 @@ int cc_tune_time(cc_handle set, int program, const uint64_t *ptrs, size_t n_ptrs
   if (!configs || !ms || n_configs <= 0) fail(CC_ERR_INVALID_VALUE, "no configurations");
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   TuneSet &ts = tune_set_of(c, set);
   if (program < 0 || program >= (int)ts.entries.size()) fail(CC_ERR_INVALID_VALUE, "program index out of range");
   TuneEntry &e = ts.entries[program];
@@ -2380,7 +2702,7 @@ int cc_tune_release(cc_handle set) {
   std::lock_guard<std::recursive_mutex> g(c.mu);
   TuneSet &ts = tune_set_of(c, set);
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
-  if (ts.flush) c.pool.release(ts.flush, ts.flush_cls);
+  if (ts.flush) release_block(c, ts.flush, ts.flush_cls);
   delete &ts;
   c.tune_sets.erase(set);
   CC_API_END
@@ -2416,6 +2738,7 @@ int cc_mlp_create(const int *dims, int n_dims, cc_handle *mlp) {
   }
   m->n_params = off;
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   m->state = c.pool.alloc(4 * off * sizeof(float), &m->state_cls);
   check_cuda(cudaMemsetAsync(m->state, 0, 4 * off * sizeof(float), c.stream), "cudaMemsetAsync");
   uint64_t h = c.make_handle(kTagMlp);
@@ -2438,6 +2761,7 @@ int cc_mlp_set_params(cc_handle mlp, const float *host, size_t n) {
   CC_API_BEGIN
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   Mlp &m = mlp_of(c, mlp);
   if (!host || n != m.n_params) fail(CC_ERR_INVALID_VALUE, "expected " + std::to_string(m.n_params) + " parameters");
   check_cuda(cudaMemcpyAsync(m.params(), host, n * sizeof(float), cudaMemcpyHostToDevice, c.stream), "upload");
@@ -2451,6 +2775,7 @@ int cc_mlp_get_params(cc_handle mlp, float *host, size_t n) {
   CC_API_BEGIN
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   Mlp &m = mlp_of(c, mlp);
   if (!host || n != m.n_params) fail(CC_ERR_INVALID_VALUE, "expected " + std::to_string(m.n_params) + " parameters");
   check_cuda(cudaMemcpyAsync(host, m.params(), n * sizeof(float), cudaMemcpyDeviceToHost, c.stream), "download");
@@ -2463,6 +2788,7 @@ int cc_mlp_forward(cc_handle mlp, uint64_t x, int batch, uint64_t y, uint64_t st
   if (!x || !y || batch <= 0) fail(CC_ERR_INVALID_VALUE, "null pointer or empty batch");
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   Mlp &m = mlp_of(c, mlp);
   cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c.stream;
   if (s != c.stream) check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
@@ -2477,6 +2803,7 @@ int cc_mlp_gradients(cc_handle mlp, uint64_t x, uint64_t t, int batch, float *lo
   if (!x || !t || batch <= 0) fail(CC_ERR_INVALID_VALUE, "null pointer or empty batch");
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   Mlp &m = mlp_of(c, mlp);
   mlp_reserve(c, m, batch);
   mlp_backward(c, m, reinterpret_cast<const float *>(x), reinterpret_cast<const float *>(t), batch, c.stream);
@@ -2497,6 +2824,7 @@ int cc_mlp_train_step(cc_handle mlp, uint64_t x, uint64_t t, int batch, float lr
     fail(CC_ERR_INVALID_VALUE, "Adam needs lr > 0, betas in [0, 1) and eps > 0");
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   Mlp &m = mlp_of(c, mlp);
   mlp_reserve(c, m, batch);
   mlp_backward(c, m, reinterpret_cast<const float *>(x), reinterpret_cast<const float *>(t), batch, c.stream);
@@ -2519,8 +2847,8 @@ int cc_mlp_release(cc_handle mlp) {
   std::lock_guard<std::recursive_mutex> g(c.mu);
   Mlp &m = mlp_of(c, mlp);
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
-  if (m.scratch) c.pool.release(m.scratch, m.scratch_cls);
-  c.pool.release(m.state, m.state_cls);
+  if (m.scratch) release_block(c, m.scratch, m.scratch_cls);
+  release_block(c, m.state, m.state_cls);
   if (c.cost_model == mlp) c.cost_model = 0;
   delete &m;
   c.mlps.erase(mlp);
@@ -2531,6 +2859,7 @@ int cc_tuner_set_model(cc_handle mlp, const float *mean, const float *inv_std) {
   CC_API_BEGIN
   Context &c = ctx();
   std::lock_guard<std::recursive_mutex> g(c.mu);
+  end_pdl_chain(c);
   if (!mlp) {
     c.cost_model = 0;
     return CC_OK;

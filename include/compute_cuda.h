@@ -19,7 +19,8 @@
  *     on the calling thread is returned by cc_last_error.
  *   - Handles are opaque 64-bit values (0 is never a valid handle).
  *   - All functions are thread-safe.  Work is ordered on one CUDA stream per
- *     context (cc_get_stream / cc_set_stream).
+ *     context (cc_get_stream / cc_set_stream), except the *_ev entry points,
+ *     which spread work over a pool of streams ordered by event wait lists.
  *   - Completion is reported by polling or by blocking waits with a timeout;
  *     the library never calls back into the caller from a driver thread.
  */
@@ -90,7 +91,12 @@ int cc_synchronize(void);
  *                       CTAs running together share A and B panels in L2 (1 = row-major; default 1)
  *   "pdl"               1 (default) = launch generated kernels with programmatic dependent launch: a kernel is
  *                       scheduled while the previous one drains and waits (griddepcontrol.wait)
- *                       before its first memory access, so results and ordering are unchanged
+ *                       before its first memory access, so results and ordering are unchanged; on the
+ *                       context's own stream, a kernel that follows another generated kernel (nothing
+ *                       else enqueued by this library in between) and reads none of its output loads
+ *                       early and waits before its first store.  A caller that enqueues its own work on
+ *                       that stream between launches (cc_get_stream) sets 2: programmatic launch, every
+ *                       kernel waiting before its first load.  0 = ordinary launches
  *   "ew_smem_ring"      generic kernels: per-thread slots of a shared-memory ring through which loads
  *                       with zero padding are staged by cp.async (0 = loads into registers; 4..64)
  *   "ew_vector_loads"   1 (default) = generic elementwise kernels whose reads at a constant innermost index
@@ -190,6 +196,29 @@ int cc_launch(cc_handle program, const cc_handle *inputs, int n_inputs, cc_handl
 int cc_launch_ptrs(cc_handle program, const uint64_t *input_ptrs, int n_inputs, uint64_t output_ptr,
                    uint64_t stream);
 
+/* ---- the asynchronous DAG: Kernel.enqueue(commandQueue, ..., waitingEvents) returning an Event
+ *      (OpenCL.scala:787-844), dispatched to a queue of the CommandQueuePool (:423-448, :1298-1329),
+ *      and the non-blocking enqueueWriteBuffer / enqueueReadBuffer with their events (:1206-1244,
+ *      :1415-1431), as CompiledKernel.run drives them: each kernel waits for the events of the
+ *      buffers it reads (Tensors.scala:1331-1381, PendingBuffer / EventBuffer :253-299).
+ *      Each call takes the next stream of a pool of five (round robin), makes it wait for every
+ *      event of `wait` (n_wait of them; NULL when 0), enqueues its work there and, when `event` is
+ *      not NULL, returns an event that completes with it (release it with cc_event_release; it
+ *      has no timing, so cc_event_elapsed refuses it).  Work without a chain of events between it
+ *      runs concurrently.  Work on the context stream (cc_launch, cc_buf_upload, ...) is ordered
+ *      after the pool's work only through cc_stream_wait_events.  Once the pool is in use, a
+ *      released buffer is reused only after every stream that may still use it has passed it.
+ *      A host copy must leave `host` unchanged (upload) or unread (download) until the event
+ *      completes; pinned memory (cc_host_alloc) makes the copy asynchronous to the host. --------- */
+int cc_launch_ev(cc_handle program, const cc_handle *inputs, int n_inputs, cc_handle output, const cc_handle *wait,
+                 int n_wait, cc_handle *event);
+int cc_buf_upload_ev(cc_handle buf, size_t offset, const void *host, size_t bytes, const cc_handle *wait, int n_wait,
+                     cc_handle *event);
+int cc_buf_download_ev(cc_handle buf, size_t offset, void *host, size_t bytes, const cc_handle *wait, int n_wait,
+                       cc_handle *event);
+/* Later work on the context stream waits for these events (also those of cc_event_record). */
+int cc_stream_wait_events(const cc_handle *events, int n_events);
+
 /* ---- reductions: Tensor.sum -> reduce(PlusPrograms) (Tensors.scala:303-392,
  *      :673-771).  A fused sum is a kind-1 program run by cc_launch; this is the
  *      plain sum of n floats at a device address, written to one float at
@@ -210,8 +239,13 @@ int cc_reduce_sum_f32(uint64_t in_ptr, size_t n, uint64_t out_ptr, uint64_t stre
  * that device's default stream.
  *   - n may be at most 134,217,728 floats (16384 blocks of 8192); larger n is
  *     rejected with CC_ERR_INVALID_VALUE and nothing is launched.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - The array's device address belongs to the CUDA context current on the
+ *     calling thread (the device's primary context, or a driver-API context
+ *     of the caller's own).  The first call in each context looks it up
+ *     (cudaGetSymbolAddress) and keeps it under the context's unique ID
+ *     (cuCtxGetId), so a context created after cudaDeviceReset, or another
+ *     context on the same device, gets its own address.  Make that first call
+ *     in a context before any stream capture.
  *   - Every call shares the one array, which keeps the last call's contents:
  *     each call zeroes the counter on `stream` first, so calls ordered on one
  *     stream are safe, but calls that can overlap on the GPU (on different

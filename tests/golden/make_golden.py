@@ -1,8 +1,8 @@
 """Extracts the expected values of the reference's own tests into reference_goldens.json.
 
-Run in a checkout that has the Compute.scala sources (default
-/root/reference); the JSON it writes is committed, so the tests never need the
-reference at run time.  For every test block named below it records, in source
+Run with the path of a Compute.scala checkout, as the first argument or in
+the COMPUTE_SCALA_REFERENCE environment variable; the JSON it writes is
+committed, so the tests never need the reference at run time.  For every test block named below it records, in source
 order, each expected value of a ``should be(...)`` assertion: string literals
 (joined when the Scala source concatenates them with ``+``), float literals,
 and ``Array(...)``/``Seq(...)`` of float or string literals, each with its
@@ -16,7 +16,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("COMPUTE_SCALA_REFERENCE")
+if __name__ == "__main__" and not REF:
+    raise SystemExit("usage: make_golden.py <Compute.scala checkout> (or set COMPUTE_SCALA_REFERENCE)")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
 
 FILES = {

@@ -143,3 +143,41 @@ def test_matmul_idiom_through_the_api_in_every_contraction_mode(cuda_device):
     assert rel_fro(got[3], ref64) <= 1e-6
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("shape", [(4096, 4096, 4096), (16384, 256, 16384)])
+def test_benchmark_shapes_through_the_api(cuda_device, shape):
+    """The two contraction configurations at full size (A[4096,4096] x B[4096,4096];
+    A[16384,256] x B[256,16384], both ~ N(0,1)), through the Tensor API's matmul
+    idiom on the split-BF16 tensor cores, and the FP32 CUDA-core GEMM on the same
+    operands: relative Frobenius error of 512 sampled rows against float64 at
+    most 1e-6 for both, and no device error."""
+    rt = cuda_device.runtime
+    m, k, n = shape
+    a, b = _operands(cuda_device, m, k, n)
+    saved = rt.config_get("contraction")
+    try:
+        rt.config_set("contraction", 3)
+        c = _api_matmul(cuda_device, a, b)
+        ser = cuda_device.serialize(c.closure, c.shape)
+        prog = rt.program(ser.text)
+        out = rt.alloc(m * n * 4)
+        rt.launch(prog, [a._cached, b._cached], out)
+        assert rt.device_errors() == 0
+        rows = np.sort(np.random.RandomState(1).choice(m, size=512, replace=False))
+        got = np.stack([rt.download(out, n, offset=int(r) * n * 4) for r in rows])
+        fp32 = rt.alloc(m * n * 4)
+        rt.gemm_ptr(a._cached.device_ptr(), b._cached.device_ptr(), fp32.device_ptr(), m, n, k, rt.GEMM_FP32)
+        got32 = np.stack([rt.download(fp32, n, offset=int(r) * n * 4) for r in rows])
+        out.release()
+        fp32.release()
+    finally:
+        rt.config_set("contraction", saved)
+    A = a.flatArray().reshape(m, k)[rows].astype(np.float64)
+    B = b.flatArray().reshape(k, n).astype(np.float64)
+    ref = A @ B
+    err, err32 = rel_fro(got, ref), rel_fro(got32, ref)
+    assert err <= 1e-6, err
+    assert err32 <= 1e-5, err32  # the plain FP32 GEMM, for comparison (about 1e-6 at K = 4096)
+    a.close()
+    b.close()

@@ -78,3 +78,61 @@ def test_early_start_keeps_write_after_read_and_write_after_write(cuda_device):
         nan = np.isnan(w)
         assert np.array_equal(nan, np.isnan(g_))
         assert np.array_equal(w[~nan].view(np.int32), g_[~nan].view(np.int32))
+
+
+def test_precompiled_kernels_between_generated_ones_keep_their_writes_visible(cuda_device):
+    """A generated kernel G1 writes Z; a precompiled kernel (random numbers, the
+    pooled sum, the sum without a context, the FP32 GEMM) writes X; a generated
+    kernel G2 reads X.  The precompiled kernels never release their dependents
+    early, so G2 must not load X before they end: the results are the bits of
+    the same sequence launched without programmatic dependent launch."""
+    import ctypes
+    from compute import _native
+    from compute.tensors import NonInlineTensor
+    d = cuda_device
+    rt = d.runtime
+    T = d.Tensor
+    n = 1 << 22
+    p = NonInlineTensor(d, (n,), 0.0, None)
+    g1 = rt.program(d.serialize((p * T.fill(2.0, [n])).closure, (n,)).text)            # Z = 2A
+    g2 = rt.program(d.serialize((p + T.fill(1.0, [n])).closure, (n,)).text)            # Y = X + 1
+    lib = _native.load()
+    a0 = np.random.RandomState(1).uniform(-1, 1, n).astype(np.float32)
+
+    def run(pdl):
+        rt.config_set("pdl", pdl)
+        A, Z, X, Y = (rt.alloc(4 * n) for _ in range(4))
+        rt.upload(A, a0)
+        pa, pz, px, py = A.device_ptr(), Z.device_ptr(), X.device_ptr(), Y.device_ptr()
+        outs = []
+        for seed in range(6):
+            rt.launch_ptrs(g1, [pa], pz)
+            rt.random(X, n, seed, seed % 2 == 1)           # X = random numbers
+            rt.launch_ptrs(g2, [px], py)                    # reads X
+            outs.append(rt.download(Y, n))
+            rt.launch_ptrs(g1, [pa], pz)
+            rt.reduce_sum_ptr(pz, n, px)                     # X[0] = sum(Z)
+            rt.launch_ptrs(g2, [px], py)
+            outs.append(rt.download(Y, 1))
+            rt.launch_ptrs(g1, [pa], pz)
+            _native.check(lib.cc_reduce_sum_f32_noalloc(ctypes.c_uint64(pa), ctypes.c_size_t(n), ctypes.c_uint64(px + 4),
+                                                        ctypes.c_uint64(rt.stream())),
+                          "cc_reduce_sum_f32_noalloc")     # X[1] = sum(A), without the context
+            rt.launch_ptrs(g2, [px], py)
+            outs.append(rt.download(Y, 2))
+            rt.launch_ptrs(g1, [pa], pz)
+            rt.gemm_ptr(pa, pa, px, 64, 64, 64, rt.GEMM_FP32)  # X[:4096] = A[:64,:64] @ A[:64,:64]
+            rt.launch_ptrs(g2, [px], py)
+            outs.append(rt.download(Y, 4096))
+        rt.synchronize()
+        for buf in (A, Z, X, Y):
+            buf.release()
+        return outs
+
+    try:
+        want = run(0)
+        got = run(1)
+    finally:
+        rt.config_set("pdl", 1)
+    for w, g_ in zip(want, got):
+        assert np.array_equal(w.view(np.int32), g_.view(np.int32))
