@@ -149,6 +149,8 @@ def conv_expr(T, x, weight, bias, parts=False):
 
 
 C3 = {"c3": (4096, 4096, 4096), "c3s": (16384, 256, 16384)}
+# The inner-axis fold t.split(1).reduce(_ + _) over x[16384, 4096] ~ N(0,1).
+C7 = {"rows": 16384, "cols": 4096}
 # Exactly one index per seed makes the Wang hash 0 (log(0) = -inf in Box-Muller);
 # seeds with bit 30 set move it past 2^30, beyond these tensors.
 C3_SEED = 0x40000000
@@ -280,6 +282,27 @@ def setup(workload, d):
                             "flops_per_step": 2 * n * h * w * c * k * k * c,
                             "l2": "inputs rotate over %d copies of x (%.0f MB > 4x L2)"
                                   % (copies, copies * xbytes / 1e6)})
+    if workload == "c7":
+        R, J = C7["rows"], C7["cols"]
+        x = T.randomNormal([R, J], seed=C3_SEED).doCache()
+        s = x.split(1).reduce(lambda a, b: a + b)
+        ser = d.serialize(s.closure, s.shape)
+        prog = rt.program(ser.text)
+        xbytes = R * J * 4
+        copies = max(2, -(-4 * L2_BYTES // xbytes))
+        sets, owned = [], []
+        for _ in range(copies):
+            buf = rt.alloc(xbytes)
+            rt.random(buf, R * J, C3_SEED, True)
+            sets.append([buf])
+            owned.append(buf)
+        out = rt.alloc(R * 4)
+        return dict(prog=prog, sets=sets, out=out, bytes=xbytes + R * 4, copies=copies, keep=[x], ser=ser,
+                    owned=owned, shape=(R, J),
+                    config={"workload": arm_workload("c7"),
+                            "kernel": "TMA-staged row tiles (64 rows x 32 floats, 128-byte swizzle), one output "
+                                      "per thread folded left to right",
+                            "l2": "inputs rotate over %d copies of x (%.0f MB > 4x L2)" % (copies, copies * xbytes / 1e6)})
     if workload in C3:
         m, k, n = C3[workload]
         rt.config_set("contraction", 3)  # split-BF16 on the tensor cores
@@ -513,6 +536,8 @@ def arm_workload(workload):
     if workload in C3:
         m, k, n = C3[workload]
         return "contraction via broadcast+split(1).reduce: A[%d,%d] x B[%d,%d] ~ N(0,1)" % (m, k, k, n)
+    if workload == "c7":
+        return "inner-axis sum: x[%d,%d] ~ N(0,1) .split(1).reduce(_+_) -> [%d]" % (C7["rows"], C7["cols"], C7["rows"])
     raise SystemExit("unknown workload " + workload)
 
 
@@ -531,10 +556,25 @@ def max_over_ranks(dist, value: float) -> float:
     return float(t.item())
 
 
-def cpu_reference(workload, budget_s=15.0, threads=None):
+def cpu_reference(workload, budget_s=15.0, threads=None, contract="off"):
     """Times the reference's CPU implementation (the oracle's C restatement of the
-    generated OpenCL C, OpenMP over all host threads) on a bounded sample."""
+    generated OpenCL C, OpenMP over all host threads) on a bounded sample;
+    ``contract`` is gcc's -ffp-contract mode for the generated C."""
     from oracle import cref
+    if contract != "off":
+        return cref.time_workload(workload, budget_s=budget_s, threads=threads, contract=contract)
+    if workload == "c7":
+        R, J = 1024, C7["cols"]
+
+        def make_fold(T):
+            x = T.randomNormal([R, J], seed=C3_SEED).doCache()
+            return x.split(1).reduce(lambda a, b: a + b)
+
+        r = cref.time_expression(make_fold, 4 * (R * J + R), budget_s=budget_s, threads=threads)
+        r["config"] = {"workload": "inner-axis sum (reference CPU path, OpenCL C on host cores)"}
+        r["sample"] = ("x[%d,%d] (%d of %d rows), %d reps; one work item per output, its %d-term fold of "
+                       "split views" % (R, J, R, C7["rows"], r["reps"], J))
+        return r
     if workload == "c6":
         n, h, w, c, k = C6["n"], C6["h"], C6["w"], C6["c"], C6["k"]
 
@@ -560,7 +600,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s", "c4", "c5", "c6"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c3s", "c4", "c5", "c6", "c7"])
     ap.add_argument("--programs", type=int, default=2048,
                     help="c4: programs in the batch; c5: tuning workloads to time (the last 10%% held out)")
     ap.add_argument("--max-len", type=int, default=4194304, help="c4: longest program (lengths log-uniform from 1024)")
@@ -677,19 +717,29 @@ def measure_fused(d, workload, steps, warmup, rank=0, world=1, local_rank=0, dis
     roofline = {"bound": "hbm", "achieved": gbs_step, "peak": peak, "unit": "GB/s", "frac": gbs_step / peak,
                 "traffic": _traffic(workload), "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": st["bytes"]}
-    cpu = None
+    cpu = cpu_fast = None
     if cpu_on:
         try:
             r = cpu_reference(workload, budget_s=cpu_budget_s)
-            cpu = {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port", "sample": r["sample"]}
+            cpu = {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port", "sample": r["sample"],
+                   "fp_contract": "off"}
         except Exception as e:  # the baseline is reported, not required
             cpu = {"value": None, "unit": "GB/s", "cores": None, "kind": "port", "sample": "failed: %s" % e}
+        if workload in ("c1", "c2"):
+            try:
+                r = cpu_reference(workload, budget_s=cpu_budget_s / 2, contract="fast")
+                cpu_fast = {"value": r["gbs"], "unit": "GB/s", "cores": r["threads"], "kind": "port",
+                            "sample": r["sample"], "fp_contract": "fast"}
+            except Exception as e:
+                cpu_fast = {"value": None, "unit": "GB/s", "sample": "failed: %s" % e, "fp_contract": "fast"}
     line = {"metric": "fused-op GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": steps,
             "warmup": warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded reference RNG)",
             "config": dict(st["config"], parallelism="replicas" if world > 1 else "single GPU"),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": steps,
             "clocks": clocks, "hot_l2": hot, "launch_overlap": overlap}
+    if cpu_fast is not None:
+        line["cpu_baseline_fp_contract_fast"] = cpu_fast
     release(st)
     return line
 
@@ -714,6 +764,8 @@ def measure_all_configs(d, args, warmup, local_rank):
 
     attempt("c1", lambda: measure_fused(d, "c1", args.steps, warmup, local_rank=local_rank, cpu_budget_s=6.0,
                                         clocks_on=not args.no_clocks))
+    attempt("c7", lambda: measure_fused(d, "c7", min(args.steps, 50), warmup, local_rank=local_rank,
+                                        cpu_budget_s=6.0, clocks_on=not args.no_clocks))
     for w in ("c3", "c3s"):
         attempt(w, lambda w=w: measure_contraction(d, w, 20, warmup, local_rank=local_rank, cpu_budget_s=6.0,
                                                    clocks_on=not args.no_clocks))

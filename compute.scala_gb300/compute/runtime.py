@@ -111,6 +111,10 @@ class NativeRuntime:
         call("cc_pool_stats", ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d))
         return {"in_use": a.value, "cached": b.value, "allocs": c.value, "reuses": d.value}
 
+    def pool_trim(self):
+        """Frees the pool's cached blocks (cudaFree)."""
+        call("cc_pool_trim")
+
     def pool_set_limit(self, nbytes: int):
         call("cc_pool_set_limit", ctypes.c_size_t(int(nbytes)))
 

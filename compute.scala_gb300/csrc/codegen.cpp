@@ -284,12 +284,18 @@ struct Stmt {
   bool batchable = false;
 };
 
+}  // namespace
+
+thread_local bool g_codegen_fma = false;
+
+namespace {
+
 class Generator {
  public:
   Generator(const Ir &ir, bool contiguous_mode, bool asm_loads = false, int64_t prefetch_min_bytes = -1,
             bool shared_transcendentals = false)
       : ir_(ir), contig_(contiguous_mode), asm_loads_(asm_loads), prefetch_min_bytes_(prefetch_min_bytes),
-        shared_transcendentals_(shared_transcendentals) {}
+        shared_transcendentals_(shared_transcendentals), fma_(g_codegen_fma) {}
 
   // Returns the name of the variable holding node `n` evaluated in frame `f`;
   // the statements computing it are appended to the statement list.
@@ -319,6 +325,31 @@ class Generator {
         break;
       }
       case NodeKind::Binary: {
+        if (fma_ && (node.op == (uint8_t)BinOp::Add || node.op == (uint8_t)BinOp::Sub)) {
+          // FMA contraction: a product operand of + or - fuses into one fmaf
+          // (the left one when both are products), rounded once:
+          //   p*q + c, c + p*q -> fmaf(p, q, c);  p*q - c -> fmaf(p, q, -c);  c - p*q -> fmaf(-p, q, c)
+          const IrNode &na = ir_.nodes[node.a], &nb = ir_.nodes[node.b];
+          const bool a_mul = na.kind == NodeKind::Binary && na.op == (uint8_t)BinOp::Mul;
+          const bool b_mul = nb.kind == NodeKind::Binary && nb.op == (uint8_t)BinOp::Mul;
+          if (a_mul || b_mul) {
+            const IrNode &m = a_mul ? na : nb;
+            std::string p = gen(m.a, f);
+            std::string q = gen(m.b, f);
+            std::string c = gen(a_mul ? node.b : node.a, f);
+            v = fresh();
+            std::string e;
+            if (node.op == (uint8_t)BinOp::Add)
+              e = "__fmaf_rn(" + p + ", " + q + ", " + c + ")";
+            else if (a_mul)
+              e = "__fmaf_rn(" + p + ", " + q + ", -" + c + ")";
+            else
+              e = "__fmaf_rn(-" + p + ", " + q + ", " + c + ")";
+            if (reuse("B " + e, v)) break;
+            add(Cat::Compute, "const float " + v + " = " + e + ";");
+            break;
+          }
+        }
         std::string a = gen(node.a, f);
         std::string b = gen(node.b, f);
         v = fresh();
@@ -782,6 +813,7 @@ class Generator {
   int ring_ = 0;
   int ring_loads_ = 0;
   std::set<int> varying_params_;  // parameters read at least once at a per-thread index
+  bool fma_ = false;              // contract a product operand of + / - into fmaf
 };
 
 bool is_contiguous_identity(const IrNode &x, const IrNode &p, const std::vector<int64_t> &out_shape) {
@@ -857,6 +889,264 @@ bool match_contraction(const Ir &ir, Contraction *out) {
   out->k = J;
   out->n = K;
   return true;
+}
+
+namespace {
+
+// Row y of view matrix `m` (cols columns) selects coordinate y and nothing else.
+bool row_selects(const std::vector<double> &m, int cols, int y, int coord) {
+  for (int c = 0; c < cols; ++c)
+    if (m[(size_t)y * cols + c] != (c == coord ? 1.0 : 0.0)) return false;
+  return true;
+}
+
+// The last row of a split's view matrix: no coordinate, the constant j.
+bool row_is_constant(const std::vector<double> &m, int cols, int y, double value) {
+  for (int c = 0; c + 1 < cols; ++c)
+    if (m[(size_t)y * cols + c] != 0.0) return false;
+  return m[(size_t)y * cols + cols - 1] == value;
+}
+
+// A read of a tensor of shape [1, ..., 1, J] at the frame's last coordinate:
+// the rows of the size-one dimensions have no term (index 0, as a broadcast
+// reads them) and the last row selects coordinate frame_rank - 1.
+bool is_column_read(const IrNode &x, const IrNode &p, int64_t J, int frame_rank) {
+  if (p.dims.empty() || p.dims.back() != J) return false;
+  const int rows = (int)p.dims.size(), cols = frame_rank + 1;
+  if (x.cols != cols || (int)x.m.size() != rows * cols) return false;
+  for (int y = 0; y + 1 < rows; ++y) {
+    if (p.dims[y] != 1) return false;
+    for (int c = 0; c < cols; ++c)
+      if (x.m[(size_t)y * cols + c] != 0.0) return false;
+  }
+  return row_selects(x.m, cols, rows - 1, frame_rank - 1);
+}
+
+}  // namespace
+
+bool match_row_fold(const Ir &ir, RowFold *out, std::string *why) {
+  auto no = [&](const char *m) {
+    if (why) *why = m;
+    return false;
+  };
+  if (ir.kind != ProgramKind::Elementwise) return no("not an elementwise program");
+  std::vector<int> terms;
+  int node = ir.root;
+  while (ir.nodes[node].kind == NodeKind::Binary && ir.nodes[node].op == (uint8_t)BinOp::Add) {
+    terms.push_back(ir.nodes[node].b);
+    node = ir.nodes[node].a;
+  }
+  terms.push_back(node);
+  const int64_t J = (int64_t)terms.size();
+  if (J < kRowFoldMinTerms) return no("fewer terms than the fold skeleton takes");
+  std::reverse(terms.begin(), terms.end());
+  const int out_rank = (int)ir.out_shape.size();
+  std::vector<int64_t> frame = ir.out_shape;
+  frame.push_back(J);
+  const int cols = out_rank + 1;
+  // every term: the same fused tensor (a View of one node) or the same parameter,
+  // of shape `frame`, at coordinates (g, j)
+  const IrNode &first = ir.nodes[terms[0]];
+  if (first.kind != NodeKind::View && first.kind != NodeKind::Extract) return no("terms are not views");
+  const bool fused = first.kind == NodeKind::View;
+  for (int64_t j = 0; j < J; ++j) {
+    const IrNode &v = ir.nodes[terms[j]];
+    if (v.kind != first.kind || v.a != first.a || v.cols != cols) return no("terms differ");
+    const std::vector<int64_t> &dims = fused ? v.dims : ir.nodes[v.a].dims;
+    if (dims != frame) return no("terms do not split the last dimension");
+    for (int y = 0; y < out_rank; ++y)
+      if (!row_selects(v.m, cols, y, y)) return no("terms are not read at the output's coordinates");
+    if (!row_is_constant(v.m, cols, out_rank, (double)j)) return no("terms are not in split order");
+  }
+  RowFold rf;
+  rf.rows = 1;
+  for (int64_t d : ir.out_shape) rf.rows *= d;
+  rf.cols = J;
+  rf.is_row.assign(ir.n_params, false);
+  std::vector<bool> is_col(ir.n_params, false);
+  if (!fused) {
+    rf.term = terms[0];
+    rf.term_frame = ir.out_shape;
+    rf.is_row[ir.nodes[first.a].param_index] = true;
+  } else {
+    rf.term = first.a;
+    rf.term_frame = frame;
+    // the template: literals, operators and reads of row or column inputs
+    std::vector<int> stack{first.a};
+    std::set<int> seen;
+    while (!stack.empty()) {
+      const int n = stack.back();
+      stack.pop_back();
+      if (!seen.insert(n).second) continue;
+      const IrNode &x = ir.nodes[n];
+      switch (x.kind) {
+        case NodeKind::Literal: break;
+        case NodeKind::Unary: stack.push_back(x.a); break;
+        case NodeKind::Binary:
+          stack.push_back(x.a);
+          stack.push_back(x.b);
+          break;
+        case NodeKind::Extract: {
+          const IrNode &p = ir.nodes[x.a];
+          const int fc = (int)frame.size() + 1;
+          if (x.cols != fc) return no("template read of another rank");
+          if (is_contiguous_identity(x, p, frame)) {
+            rf.is_row[p.param_index] = true;
+          } else if (is_column_read(x, p, J, (int)frame.size())) {
+            is_col[p.param_index] = true;
+          } else {
+            return no("template reads an input through a view");
+          }
+          break;
+        }
+        default: return no("template holds a nested view or tuple");
+      }
+    }
+  }
+  for (int k = 0; k < ir.n_params; ++k) {
+    if (rf.is_row[k] && is_col[k]) return no("an input read both as a row and as a column");
+    if (rf.is_row[k]) rf.row_inputs.push_back(k);
+  }
+  if (rf.row_inputs.empty()) return no("no row input");
+  if ((int)rf.row_inputs.size() > kRowFoldMaxInputs) return no("more row inputs than the ring stages");
+  if (J % 4 != 0) return no("rows are not a multiple of 16 bytes");
+  if (rf.rows >= (int64_t(1) << 31) || J >= (int64_t(1) << 31)) return no("too many rows or terms for TMA coordinates");
+  if (out) *out = rf;
+  return true;
+}
+
+int row_fold_stages(int row_inputs) {
+  const int per_stage = row_inputs * kRowFoldRows * 128;
+  int s = (96 * 1024) / (per_stage > 0 ? per_stage : 1);
+  return s < 2 ? 2 : s > 8 ? 8 : s;
+}
+
+int row_fold_smem_bytes(int row_inputs) { return row_fold_stages(row_inputs) * row_inputs * kRowFoldRows * 128 + 1024; }
+
+std::string row_fold_source(const Ir &ir, const RowFold &rf) {
+  Generator gen(ir, true, false, -1, false);
+  std::ostringstream body;
+  Frame f0{0, {}, rf.term_frame};
+  const std::string r = gen.gen(rf.term, f0);
+  gen.emit(body, 2, 0);
+  const int n = ir.n_params, nin = (int)rf.row_inputs.size(), S = row_fold_stages(nin);
+  std::vector<int> slot(n, -1);  // parameter -> row-input slot
+  for (int i = 0; i < nin; ++i) slot[rf.row_inputs[i]] = i;
+  std::ostringstream o;
+  o << "// generated by compute.scala_gb300 for sm_103a: inner-axis fold of " << rf.cols << " terms per output\n"
+    << kPrelude << "\n";
+  o << "#define CC_RF_ROWS " << kRowFoldRows << "\n#define CC_RF_NIN " << nin << "\n#define CC_RF_STAGES " << S
+    << "\n#define CC_RF_TILE (CC_RF_ROWS * 128)\n\n";
+  // one term of the fold, from its inputs' values at (g, j)
+  o << "__device__ __forceinline__ float cc_rf_term(";
+  for (int k = 0; k < n; ++k) o << (k ? ", " : "") << "const float a" << k;
+  o << ") {\n" << body.str() << "  return " << r << ";\n}\n\n";
+  std::ostringstream params;
+  for (int i = 0; i < nin; ++i) params << "const __grid_constant__ cc_tensor_map tm" << i << ", ";
+  for (int k = 0; k < n; ++k) params << "const float *__restrict__ in" << k << ", ";
+  params << "float *__restrict__ out, long long rows, int cols, int *__restrict__ err";
+  // the term at column expression `j` with row-input values `val(i)`
+  auto call = [&](const std::function<std::string(int)> &val, const std::string &j) {
+    std::string s = "cc_rf_term(";
+    for (int k = 0; k < n; ++k) {
+      if (k) s += ", ";
+      s += slot[k] >= 0 ? val(slot[k]) : "__ldg(in" + std::to_string(k) + " + " + j + ")";
+    }
+    return s + ")";
+  };
+  static const char *comp[] = {"x", "y", "z", "w"};
+  // ---- cc_rowfold: TMA tiles of 64 rows x 32 floats (128 bytes, swizzled), one per row input
+  o << "// Each block folds CC_RF_ROWS outputs, one per thread, in the order j = 0, 1, 2, ...\n"
+       "// Thread 0 keeps CC_RF_STAGES tiles of every row input in flight (TMA, 128-byte swizzle:\n"
+       "// 16-byte chunk c of tile row r sits at chunk c ^ (r % 8), so eight threads reading their\n"
+       "// own rows' chunk c hit eight different bank groups).\n";
+  o << "extern \"C\" __global__ void __launch_bounds__(CC_RF_ROWS) cc_rowfold(" << params.str() << ") {\n"
+    << "  extern __shared__ unsigned char cc_rf_raw[];\n"
+    << "  __shared__ __align__(8) unsigned long long cc_rf_full[CC_RF_STAGES];\n"
+    << "  __shared__ int cc_rf_abort;\n"
+    << "  unsigned char *const ring = (unsigned char *)(((unsigned long long)cc_rf_raw + 1023ull) & ~1023ull);\n"
+    << "  const int tid = threadIdx.x;\n"
+    << "  const long long row0 = (long long)blockIdx.x * CC_RF_ROWS;\n"
+    << "  const int ntiles = (cols + 31) >> 5;\n"
+    << "  if (tid == 0) {\n"
+    << "    for (int s = 0; s < CC_RF_STAGES; ++s) cc_mbar_init(cc_smem_addr(&cc_rf_full[s]), 1);\n"
+    << "    cc_mbar_init_fence();\n"
+    << "    cc_rf_abort = 0;\n"
+    << "  }\n"
+    << "  __syncthreads();\n"
+    << "  cc_pdl_wait_then_release();\n";
+  std::ostringstream issue;
+  issue << "      const unsigned bar = cc_smem_addr(&cc_rf_full[(u) % CC_RF_STAGES]);\n"
+        << "      cc_mbar_expect_tx(bar, CC_RF_NIN * CC_RF_TILE);\n";
+  for (int i = 0; i < nin; ++i)
+    issue << "      cc_tma_load_2d(cc_smem_addr(ring + ((u) % CC_RF_STAGES * CC_RF_NIN + " << i
+          << ") * CC_RF_TILE), &tm" << i << ", (u) << 5, (int)row0, bar);\n";
+  o << "  if (tid == 0)\n    for (int u = 0; u < CC_RF_STAGES && u < ntiles; ++u) {\n" << issue.str() << "    }\n";
+  o << "  float acc = 0.0f;\n"
+    << "  int t = 0;\n"
+    << "  for (; t < ntiles; ++t) {\n"
+    << "    const int s = t % CC_RF_STAGES;\n"
+    << "    if (!cc_mbar_wait_bounded(cc_smem_addr(&cc_rf_full[s]), (unsigned)((t / CC_RF_STAGES) & 1), 2000000000ull)) {\n"
+    << "      atomicCAS(err, 0, " << kRowFoldWaitCode << ");\n"
+    << "      cc_rf_abort = 1;\n"
+    << "    }\n"
+    << "    const unsigned char *tile = ring + s * CC_RF_NIN * CC_RF_TILE + tid * 128;\n"
+    << "    const int j0 = t << 5;\n"
+    << "    if (t > 0 && cols - j0 >= 32) {\n";
+  for (int g = 0; g < 2; ++g) {
+    // g = 0: a full tile, no bounds; g = 1: the first or a partial tile
+    if (g == 1) o << "    } else {\n      const int hi = cols - j0 < 32 ? cols - j0 : 32;\n";
+    o << "#pragma unroll\n      for (int c = 0; c < 8; ++c) {\n"
+      << "        const int off = (c ^ (tid & 7)) << 4;\n";
+    for (int i = 0; i < nin; ++i)
+      o << "        const float4 q" << i << " = *reinterpret_cast<const float4 *>(tile + " << i
+        << " * CC_RF_TILE + off);\n";
+    for (int e = 0; e < 4; ++e) {
+      const std::string j = "(j0 + c * 4 + " + std::to_string(e) + ")";
+      const std::string term = call([&](int i) { return "q" + std::to_string(i) + "." + comp[e]; }, j);
+      if (g == 0) {
+        o << "        acc = acc + " << term << ";\n";
+      } else {
+        o << "        if (c * 4 + " << e << " < hi) {\n"
+          << "          const float v = " << term << ";\n"
+          << "          acc = " << j << " == 0 ? v : acc + v;\n"
+          << "        }\n";
+      }
+    }
+    o << "      }\n";
+  }
+  o << "    }\n"
+    << "    __syncthreads();\n"
+    << "    if (cc_rf_abort) break;\n"
+    << "    if (tid == 0 && t + CC_RF_STAGES < ntiles) {\n"
+    << "      const int u = t + CC_RF_STAGES;\n"
+    << issue.str()
+    << "    }\n"
+    << "  }\n"
+    << "  if (cc_rf_abort) {\n"
+    << "    // loads still in flight land before the block's shared memory is given up\n"
+    << "    if (tid == 0)\n"
+    << "      for (int u = t; u < ntiles && u < t + CC_RF_STAGES; ++u)\n"
+    << "        cc_mbar_wait_bounded(cc_smem_addr(&cc_rf_full[u % CC_RF_STAGES]), (unsigned)((u / CC_RF_STAGES) & 1), "
+       "100000000ull);\n"
+    << "    return;\n"
+    << "  }\n"
+    << "  if (row0 + tid < rows) out[row0 + tid] = acc;\n"
+    << "}\n\n";
+  // ---- cc_rowfold_plain: the same fold with direct loads (row inputs not 16-byte aligned)
+  o << "extern \"C\" __global__ void __launch_bounds__(CC_RF_ROWS) cc_rowfold_plain(" << params.str() << ") {\n"
+    << "  cc_pdl_wait_then_release();\n"
+    << "  const long long row = (long long)blockIdx.x * CC_RF_ROWS + threadIdx.x;\n"
+    << "  if (row >= rows) return;\n";
+  for (int i = 0; i < nin; ++i)
+    o << "  const float *r" << i << " = in" << rf.row_inputs[i] << " + row * (long long)cols;\n";
+  const std::string t0 = call([&](int i) { return "__ldg(r" + std::to_string(i) + ")"; }, "0");
+  const std::string tj = call([&](int i) { return "__ldg(r" + std::to_string(i) + " + j)"; }, "j");
+  o << "  float acc = " << t0 << ";\n"
+    << "  for (int j = 1; j < cols; ++j) acc = acc + " << tj << ";\n"
+    << "  out[row] = acc;\n"
+    << "}\n";
+  return o.str();
 }
 
 bool is_batchable(const Ir &ir, std::string *why) {

@@ -145,3 +145,62 @@ __device__ __forceinline__ void cc_prefetch(const float *p, int ok) {
   asm volatile(
       "{\n .reg .pred q;\n setp.ne.b32 q, %1, 0;\n @q prefetch.global.L2 [%0];\n}\n" ::"l"(p), "r"(ok));
 }
+
+// ---- shared-memory staging by the Tensor Memory Accelerator (generated
+// inner-axis folds).  A tensor map is an opaque 128-byte, 64-byte aligned
+// descriptor passed by value as a __grid_constant__ kernel parameter.
+struct __align__(64) cc_tensor_map {
+  unsigned long long words[16];
+};
+
+__device__ __forceinline__ unsigned cc_smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long cc_globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void cc_mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+// Makes the initialised barriers visible to the async proxy (the TMA unit).
+__device__ __forceinline__ void cc_mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void cc_mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool cc_mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for phase `parity` of a barrier for at most limit_ns of %globaltimer
+// time; false when the limit ran out.
+__device__ __forceinline__ bool cc_mbar_wait_bounded(unsigned bar, unsigned parity, unsigned long long limit_ns) {
+  if (cc_mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = cc_globaltimer();
+  for (;;) {
+    if (cc_mbar_try_wait(bar, parity)) return true;
+    if (cc_globaltimer() - t0 > limit_ns) return false;
+    __nanosleep(32);
+  }
+}
+
+// A 2-D tile of a tensor map into shared memory, completing on `bar`.  The
+// innermost coordinate x must be a multiple of 16 bytes (here of 4 floats).
+__device__ __forceinline__ void cc_tma_load_2d(unsigned dst, const cc_tensor_map *map, int x, int y, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}

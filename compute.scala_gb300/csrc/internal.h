@@ -126,6 +126,18 @@ struct Generated {
   bool has_vl = false;               // cc_ew_vl / cc_sum_vl exists (float4 grouped reads; aligned inputs)
 };
 
+// FMA contraction of the code generated on this thread (CC_FLAG_FMA_CONTRACT):
+// every + or - with a product operand becomes one fmaf of that product (the
+// left one when both operands are products), rounded once.  Set it around
+// generate_cuda, row_fold_source, point_function and tunable_source with
+// FmaScope.
+extern thread_local bool g_codegen_fma;
+struct FmaScope {
+  bool saved;
+  explicit FmaScope(bool on) : saved(g_codegen_fma) { g_codegen_fma = on; }
+  ~FmaScope() { g_codegen_fma = saved; }
+};
+
 Generated generate_cuda(const Ir &ir, const CodegenOptions &opt);
 // The shape information of generate_cuda without generating code.
 Generated describe_program(const Ir &ir);
@@ -144,6 +156,35 @@ struct Contraction {
   int64_t m = 0, k = 0, n = 0;  // C is m x n, the folded dimension has k terms
 };
 bool match_contraction(const Ir &ir, Contraction *out);
+
+// The inner-axis fold `t.split(last).reduce(_ + _)` (Tensors.scala:1035-1074
+// with Scala's left-to-right reduce): after fusion, a left fold over j of J
+// terms that are one template -- the viewed tensor t at coordinates
+// (g_0..g_{r-1}, j) -- so out[g] = ((t(g,0) + t(g,1)) + t(g,2)) + ...  The
+// template reads "row inputs" (tensors of t's shape, read at (g, j)), "column
+// inputs" (one-dimensional tensors of J elements, read at j) and literals.
+// On a match the runtime stages tiles of the row inputs through shared memory
+// by TMA and each thread folds one output's terms in the reference's order.
+struct RowFold {
+  int term = -1;                  // the template node, evaluated in frame `term_frame`
+  std::vector<int64_t> term_frame;  // t's shape (a fused view), or the output's (a parameter read directly)
+  int64_t rows = 0, cols = 0;     // outputs, and J
+  std::vector<int> row_inputs;    // parameter indices read as rows, in order
+  std::vector<bool> is_row;       // per parameter: a row input (else a column input)
+};
+// Terms below this count stay on the generic fold (a short fold is cheap to unroll).
+constexpr int64_t kRowFoldMinTerms = 32;
+constexpr int kRowFoldRows = 64;       // outputs (threads) per block
+constexpr int kRowFoldMaxInputs = 4;   // row inputs staged per tile
+constexpr int kRowFoldWaitCode = 31;   // device error code: a tile's barrier wait ran out
+bool match_row_fold(const Ir &ir, RowFold *out, std::string *why = nullptr);
+// Stages of the shared-memory ring for `row_inputs` staged inputs.
+int row_fold_stages(int row_inputs);
+// Dynamic shared memory of cc_rowfold (ring + alignment slack).
+int row_fold_smem_bytes(int row_inputs);
+// Kernels cc_rowfold (TMA-staged tiles) and cc_rowfold_plain (direct loads,
+// for row inputs that are not 16-byte aligned), with the prelude.
+std::string row_fold_source(const Ir &ir, const RowFold &rf);
 
 // Batching: a program is batchable when it is an elementwise program whose
 // inputs are all read contiguously with the output's shape (the float4 form)

@@ -307,6 +307,9 @@ struct Program {
   bool is_contraction = false;  // run as a GEMM (cc_gemm_f32 mode contraction_mode)
   int contraction_mode = 0;
   Contraction con;
+  bool is_row_fold = false;     // an inner-axis fold: cc_rowfold / cc_rowfold_plain of mod
+  RowFold rf;
+  CUfunction rf_tma = nullptr, rf_plain = nullptr;
 };
 
 struct Event {
@@ -379,6 +382,7 @@ struct Context {
   int sum_block = 256;
   int tc_variant = 5;  // 128x256 tiles, hi*hi restarted every 256 of K
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
+  int row_fold = 1;     // inner-axis folds of at least kRowFoldMinTerms terms: 1 = TMA-staged skeleton
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
   int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel
   int batch_run_tiles = 16;       // tiles a persistent block claims at once
@@ -587,8 +591,10 @@ std::vector<char> compile_cubin(const std::string &source, int cc_major, int cc_
   nvrtcResult r = nvrtcCreateProgram(&prog, source.c_str(), "cc_program.cu", 0, nullptr, nullptr);
   if (r != NVRTC_SUCCESS) fail(CC_ERR_BUILD_PROGRAM_FAILURE, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
   std::string arch = "-arch=sm_" + std::to_string(cc_major) + std::to_string(cc_minor) + "a";
-  std::vector<std::string> opts = {arch, "--std=c++17", "-default-device",
-                                   (flags & CC_FLAG_FMA_CONTRACT) ? "--fmad=true" : "--fmad=false"};
+  // Contraction is never the compiler's choice: with CC_FLAG_FMA_CONTRACT the
+  // generated code holds explicit fmaf calls (FmaScope), so both modes are deterministic.
+  (void)flags;
+  std::vector<std::string> opts = {arch, "--std=c++17", "-default-device", "--fmad=false"};
   if (relocatable) opts.push_back("-rdc=true");
   if (max_registers > 0) opts.push_back("--maxrregcount=" + std::to_string(max_registers));
   std::vector<const char *> optp;
@@ -688,8 +694,52 @@ void launch_tuned_program(Context &c, Program &p, const std::vector<uint64_t> &i
 std::shared_ptr<TuneModule> load_tune_module(const std::vector<char> &cubin);
 void load_tune_entry(TuneEntry &e, const Ir &ir, std::shared_ptr<TuneModule> mod, const std::string &suffix);
 
+// An inner-axis fold: one thread per output, 64 per block; tiles of the row
+// inputs staged by TMA when every row input is 16-byte aligned, else direct loads.
+void launch_row_fold(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
+  const RowFold &rf = p.rf;
+  if (rf.rows == 0) return;
+  const int nin = (int)rf.row_inputs.size();
+  bool aligned = true;
+  for (int k : rf.row_inputs) aligned = aligned && (in[k] & 15u) == 0;
+  CUtensorMap maps[kRowFoldMaxInputs];
+  if (aligned) {
+    for (int i = 0; i < nin; ++i) {
+      const cuuint64_t dims[2] = {(cuuint64_t)rf.cols, (cuuint64_t)rf.rows};
+      const cuuint64_t strides[1] = {(cuuint64_t)rf.cols * 4};
+      const cuuint32_t box[2] = {32, (cuuint32_t)kRowFoldRows};
+      const cuuint32_t estr[2] = {1, 1};
+      check_cu(g_drv.TensorMapEncodeTiled(&maps[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                                          reinterpret_cast<void *>(in[rf.row_inputs[i]]), dims, strides, box, estr,
+                                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE),
+               "cuTensorMapEncodeTiled");
+    }
+  }
+  std::vector<void *> args;
+  for (int i = 0; i < nin; ++i) args.push_back(&maps[i]);
+  std::vector<uint64_t> ptrs(in);
+  for (auto &v : ptrs) args.push_back(&v);
+  uint64_t o = out;
+  long long rows = rf.rows;
+  int cols = (int)rf.cols;
+  uint64_t err = reinterpret_cast<uint64_t>(c.error_flag());
+  args.push_back(&o);
+  args.push_back(&rows);
+  args.push_back(&cols);
+  args.push_back(&err);
+  const unsigned grid = (unsigned)((rf.rows + kRowFoldRows - 1) / kRowFoldRows);
+  check_cu(g_drv.LaunchKernel(aligned ? p.rf_tma : p.rf_plain, grid, 1, 1, kRowFoldRows, 1, 1,
+                              aligned ? (unsigned)row_fold_smem_bytes(nin) : 0u, (CUstream)stream, args.data(), nullptr),
+           "cuLaunchKernel");
+}
+
 void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
-  if (p.tune || p.is_contraction) end_pdl_chain(c);
+  if (p.tune || p.is_contraction || p.is_row_fold) end_pdl_chain(c);
+  if (p.is_row_fold) {
+    launch_row_fold(c, p, in, out, stream);
+    return;
+  }
   if (p.tune) {
     launch_tuned_program(c, p, in, out, stream);
     return;
@@ -878,7 +928,9 @@ int cc_init(int device_ordinal, uint32_t flags) {
   std::lock_guard<std::mutex> g(g_init_mu);
   if (g_ctx) {
     if (g_ctx->device != device_ordinal) fail(CC_ERR_INVALID_OPERATION, "already initialised on another device");
-    g_ctx->flags = flags;
+    if (g_ctx->flags != flags)
+      fail(CC_ERR_INVALID_OPERATION, "already initialised with flags " + std::to_string(g_ctx->flags) +
+                                         " (cc_shutdown first to change them)");
     return CC_OK;
   }
   int count = 0;
@@ -1064,6 +1116,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "batch_inline") {
     if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "batch_inline must be 0, 1 or 2");
     c.batch_inline = (int)value;
+  } else if (k == "row_fold") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "row_fold must be 0 or 1");
+    c.row_fold = (int)value;
   } else if (k == "contraction") {
     if (value < 0 || value > 3) fail(CC_ERR_INVALID_VALUE, "contraction must be in [0, 3]");
     c.contraction = (int)value;
@@ -1099,6 +1154,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "sum_block") *value = c.sum_block;
   else if (k == "tc_variant") *value = c.tc_variant;
   else if (k == "contraction") *value = c.contraction;
+  else if (k == "row_fold") *value = c.row_fold;
   else if (k == "batch_inline") *value = c.batch_inline;
   else if (k == "tuner") *value = c.tuner;
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
@@ -1331,8 +1387,9 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
          " blocks " + std::to_string(-opt.min_blocks) + " block " + std::to_string(opt.block) + " unroll " + std::to_string(opt.vec_unroll) +
          " prefetch " + std::to_string(opt.prefetch_min_bytes) + " ring " + std::to_string(opt.smem_ring) + " points " + std::to_string(opt.points_per_thread) + " vl " + std::to_string((int)opt.vector_loads) + " bl " + std::to_string((int)opt.batch_loads) +
          " sumblock " + std::to_string(c.sum_block) +
-         " contraction " + std::to_string(c.contraction) + " tc " + std::to_string(c.tc_variant) + " tuner " +
-         std::to_string(c.tuner) + "\n";
+         " contraction " + std::to_string(c.contraction) + " rowfold " + std::to_string(c.row_fold) +
+         " tc " + std::to_string(c.tc_variant) + " tuner " +
+         std::to_string(c.tuner) + " flags " + std::to_string(c.flags) + "\n";
   {
     std::lock_guard<std::recursive_mutex> g(c.mu);
     auto it = c.cache.find(key);
@@ -1354,6 +1411,7 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   }
   Ir ir = parse_ir(ir_text, ir_len);
   if (ir.kind == ProgramKind::Sum) opt.block = c.sum_block;
+  FmaScope fma_scope((c.flags & CC_FLAG_FMA_CONTRACT) != 0);
   Contraction con;
   int contraction_knob;
   {
@@ -1371,6 +1429,36 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     p->gen.domain = con.m * con.n;
     p->gen.source = "// contraction: C[" + std::to_string(con.m) + "," + std::to_string(con.n) + "] = A * B over " +
                     std::to_string(con.k) + " terms, cc_gemm_f32 mode " + std::to_string(p->contraction_mode) + "\n";
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    uint64_t h = c.make_handle(kTagProgram);
+    c.programs[h] = p.release();
+    c.cache[key] = h;
+    ++c.cache_misses;
+    *out = h;
+    return CC_OK;
+  }
+  int row_fold_knob;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    row_fold_knob = c.row_fold;
+  }
+  RowFold rf;
+  if (row_fold_knob && match_row_fold(ir, &rf)) {
+    auto p = std::make_unique<Program>();
+    p->kind = ProgramKind::Elementwise;
+    p->gen = describe_program(ir);
+    p->is_row_fold = true;
+    p->rf = rf;
+    auto mod = std::make_shared<Module>();
+    mod->source = row_fold_source(ir, rf);
+    std::vector<char> cubin = compile_cubin(mod->source, c.cc_major, c.cc_minor, c.flags);
+    check_cu(g_drv.ModuleLoadData(&mod->module, cubin.data()), "cuModuleLoadData");
+    check_cu(g_drv.ModuleGetFunction(&p->rf_tma, mod->module, "cc_rowfold"), "cuModuleGetFunction");
+    check_cu(g_drv.ModuleGetFunction(&p->rf_plain, mod->module, "cc_rowfold_plain"), "cuModuleGetFunction");
+    check_cu(g_drv.FuncSetAttribute(p->rf_tma, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                                    row_fold_smem_bytes((int)rf.row_inputs.size())),
+             "cuFuncSetAttribute");
+    p->mod = mod;
     std::lock_guard<std::recursive_mutex> g(c.mu);
     uint64_t h = c.make_handle(kTagProgram);
     c.programs[h] = p.release();
@@ -1469,8 +1557,11 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
 
 namespace {
 // "block=128 lookahead=8 ring=32 unroll=4 min_blocks=11 asm=1" (any subset; NULL = defaults).
-CodegenOptions parse_codegen_options(const char *text) {
+// "rowfold=0" generates an inner-axis fold as the generic fold (default 1: the skeleton).
+CodegenOptions parse_codegen_options(const char *text, bool *row_fold = nullptr, bool *fma = nullptr) {
   CodegenOptions o;
+  if (row_fold) *row_fold = true;
+  if (fma) *fma = false;
   if (!text) return o;
   std::istringstream in(text);
   std::string item;
@@ -1488,7 +1579,11 @@ CodegenOptions parse_codegen_options(const char *text) {
     else if (k == "points") o.points_per_thread = (int)v;
     else if (k == "vl") o.vector_loads = v != 0;
     else if (k == "batch") o.batch_loads = v != 0;
-    else fail(CC_ERR_INVALID_VALUE, "unknown code-generation option '" + k + "'");
+    else if (k == "rowfold") {
+      if (row_fold) *row_fold = v != 0;
+    } else if (k == "fma") {
+      if (fma) *fma = v != 0;
+    } else fail(CC_ERR_INVALID_VALUE, "unknown code-generation option '" + k + "'");
   }
   return o;
 }
@@ -1502,7 +1597,15 @@ int cc_codegen_with(const char *ir_text, size_t ir_len, const char *options, cha
   CC_API_BEGIN
   if (!ir_text) fail(CC_ERR_INVALID_VALUE, "null pointer");
   Ir ir = parse_ir(ir_text, ir_len);
-  Generated gen = generate_cuda(ir, parse_codegen_options(options));
+  bool row_fold = true, fma = false;
+  CodegenOptions opt = parse_codegen_options(options, &row_fold, &fma);
+  FmaScope fma_scope(fma);
+  RowFold rf;
+  Generated gen;
+  if (row_fold && match_row_fold(ir, &rf))
+    gen.source = row_fold_source(ir, rf);
+  else
+    gen = generate_cuda(ir, opt);
   Contraction con;
   if (match_contraction(ir, &con))
     gen.source = "// contraction m=" + std::to_string(con.m) + " n=" + std::to_string(con.n) + " k=" +
@@ -1526,8 +1629,14 @@ int cc_compile_check_with(const char *ir_text, size_t ir_len, int cc_major, int 
   CC_API_BEGIN
   if (!ir_text) fail(CC_ERR_INVALID_VALUE, "null pointer");
   Ir ir = parse_ir(ir_text, ir_len);
-  Generated gen = generate_cuda(ir, parse_codegen_options(options));
-  compile_cubin(gen.source, cc_major, cc_minor, flags);
+  bool row_fold = true, fma = false;
+  CodegenOptions opt = parse_codegen_options(options, &row_fold, &fma);
+  FmaScope fma_scope(fma || (flags & CC_FLAG_FMA_CONTRACT) != 0);
+  RowFold rf;
+  if (row_fold && match_row_fold(ir, &rf))
+    compile_cubin(row_fold_source(ir, rf), cc_major, cc_minor, flags);
+  else
+    compile_cubin(generate_cuda(ir, opt).source, cc_major, cc_minor, flags);
   CC_API_END
 }
 
@@ -2018,6 +2127,7 @@ std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::v
                                     int cc_major, int cc_minor, uint32_t flags, bool link, int inline_level,
                                     int max_registers) {
   std::vector<std::string> sources;
+  FmaScope fma_scope((flags & CC_FLAG_FMA_CONTRACT) != 0);
   for (size_t first = 0; first < structs.size(); first += kBatchChunk)
     sources.push_back(batch_chunk_source(structs, struct_inputs, first,
                                          std::min(structs.size(), first + (size_t)kBatchChunk), inline_level));
@@ -2627,6 +2737,7 @@ int cc_tune_create(const char *const *irs, const size_t *lens, int n_programs, c
   std::vector<std::vector<char>> cubins;
   {
     std::lock_guard<std::mutex> cg(c.compile_mu);
+    FmaScope fma_scope((c.flags & CC_FLAG_FMA_CONTRACT) != 0);
     cubins = compile_parallel(tune_sources(parsed), c.cc_major, c.cc_minor, c.flags, false, 0);
   }
   auto ts = std::make_unique<TuneSet>();

@@ -54,12 +54,18 @@ typedef uint64_t cc_handle;
 #define CC_ERR_DEVICE_REPORTED       (-1004) /* a kernel set its error flag (bounded wait expired) */
 
 /* ---- flags for cc_init ----------------------------------------------------- */
-#define CC_FLAG_FMA_CONTRACT   0x1u  /* let the compiler fuse a*b+c into one FMA (off: every
-                                        SSA statement rounds separately, as written) */
+#define CC_FLAG_FMA_CONTRACT   0x1u  /* FMA contraction, as a vendor compiler under the reference's
+                                        -cl-unsafe-math-optimizations (OpenCL.scala:1131-1135) may
+                                        apply it: every + or - with a product operand is one fmaf of
+                                        that product (the left one when both operands are products),
+                                        rounded once; the compiler itself never contracts.  Off (the
+                                        default): every SSA statement rounds separately, as written */
 #define CC_FLAG_NO_FUSION_SUM  0x2u  /* reserved */
 
 /* ---- context: replaces OpenCL.UseAllDevicesByType + context + CommandQueuePool
  *      (OpenCL.scala:340-374, :423-448, :1375-1393) ------------------------- */
+/* Initialises the context on a device; calling it again with the same device
+ * and flags does nothing, other flags are refused (CC_ERR_INVALID_OPERATION). */
 int cc_init(int device_ordinal, uint32_t flags);
 int cc_shutdown(void);
 /* Copies the message of this thread's last failure (NUL-terminated, truncated to len). */
@@ -80,6 +86,11 @@ int cc_synchronize(void);
  *   "upload_streams"    copy streams a large cc_buf_upload is striped over (1..8; default 4)
  *   "ew_lookahead"      loads a generated kernel keeps in flight ahead of its arithmetic (0..256; default 8)
  *   "ew_asm_loads"      1: those loads are volatile inline PTX so the compiler keeps their order (default 1)
+ *   "row_fold"          1 (default) = a program that folds the last axis of a tensor, t.split(last).reduce(_ + _)
+ *                       with at least 32 terms whose term reads inputs of t's shape at (g, j), one-dimensional
+ *                       inputs at j and literals, runs as a skeleton that stages tiles of those inputs in
+ *                       shared memory by TMA and folds each output's terms in order (bit-identical to the
+ *                       generated fold); 0 = the generated fold
  *   "contraction"       how a program that is the library's matmul idiom runs (a left fold over j
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,

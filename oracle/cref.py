@@ -55,15 +55,21 @@ float cc_reduce_sequential(const float *restrict buffer, unsigned int length) {
 """
 
 
-def _compile(source: str, tag: str) -> ctypes.CDLL:
+def _compile(source: str, tag: str, contract: str = "off") -> ctypes.CDLL:
+    """Builds the generated C.  ``contract``: gcc's -ffp-contract mode, "off"
+    (every statement rounds as written) or "fast" (gcc fuses a*b+c where the
+    target has FMA, as a vendor OpenCL compiler may under the reference's
+    -cl-unsafe-math-optimizations)."""
+    if contract not in ("off", "fast"):
+        raise ValueError(contract)
     os.makedirs(CACHE, exist_ok=True)
-    h = hashlib.sha1(source.encode()).hexdigest()[:16]
+    h = hashlib.sha1((contract + source).encode()).hexdigest()[:16]
     so = os.path.join(CACHE, "%s_%s.so" % (tag, h))
     if not os.path.exists(so):
         c = so[:-3] + ".c"
         with open(c, "w") as f:
             f.write(source)
-        cmd = ["gcc", "-O3", "-std=gnu11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+        cmd = ["gcc", "-O3", "-std=gnu11", "-fopenmp", "-ffp-contract=" + contract, "-fPIC", "-shared",
                "-I", HERE, c, "-o", so + ".tmp", "-lm"]
         p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if p.returncode != 0:
@@ -114,14 +120,14 @@ class CBuffer:
 
 
 class CProgram:
-    def __init__(self, text):
+    def __init__(self, text, contract="off"):
         self.text = text
         self.kind = text.split("\n", 1)[0].split()[2]
         ew_text = text.replace("ccir 1 sum", "ccir 1 ew", 1)
         src, info = clgen.kernel_source(ew_text)
         info["param_types"], info["out_type"] = _param_types(src, info)
         self.info = info
-        self.lib = _compile(_driver(src, info), "k")
+        self.lib = _compile(_driver(src, info), "k", contract)
         self.lib.cc_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         self.lib.cc_run.restype = None
 
@@ -151,9 +157,10 @@ def _reducer():
 class CRuntime:
     """Runs Tensor programs as the reference's OpenCL C compiled for the host."""
 
-    def __init__(self, threads=None):
+    def __init__(self, threads=None, contract="off"):
         if threads:
             os.environ["OMP_NUM_THREADS"] = str(threads)
+        self.contract = contract
         self._programs = {}
 
     def alloc(self, nbytes):
@@ -169,7 +176,7 @@ class CRuntime:
     def program(self, text):
         p = self._programs.get(text)
         if p is None:
-            p = CProgram(text)
+            p = CProgram(text, self.contract)
             self._programs[text] = p
         return p
 
@@ -197,13 +204,13 @@ def _threads():
         return os.cpu_count() or 1
 
 
-def time_workload(workload: str, budget_s: float = 15.0, threads=None):
+def time_workload(workload: str, budget_s: float = 15.0, threads=None, contract="off"):
     """GB/s of the reference's CPU path on a bounded sample of a benchmark workload."""
     root = os.path.dirname(HERE)
     sys.path.insert(0, os.path.join(root, "compute.scala_gb300"))
     from compute import Tensors, trees
     threads = threads or _threads()
-    d = Tensors(runtime=CRuntime(threads), planner=trees.Planner(enabled=False))
+    d = Tensors(runtime=CRuntime(threads, contract), planner=trees.Planner(enabled=False))
     T = d.Tensor
     if workload == "c2":
         c, h, w = 128, 56, 56

@@ -141,12 +141,50 @@ def parse(ir_text: str):
     return kind, out_shape, nodes, root
 
 
-def evaluate(ir_text: str, inputs: Sequence[np.ndarray]):
+def fma32(a: np.ndarray, b: np.ndarray, c: np.ndarray) -> np.ndarray:
+    """fmaf(a, b, c) on float32 arrays: a*b + c rounded once to binary32.
+
+    The product of two binary32 values is exact in binary64 (48 significant
+    bits); the sum s = p + c is rounded to binary64 and TwoSum gives its exact
+    error e.  Rounding s to binary32 is then the correct rounding of p + c,
+    except when s lies exactly halfway between two binary32 values and e is
+    not zero: the true sum lies on e's side of that midpoint."""
+    with np.errstate(all="ignore"):
+        p = a.astype(np.float64) * b.astype(np.float64)
+        c64 = c.astype(np.float64)
+        s = p + c64
+        bb = s - p
+        e = (p - (s - bb)) + (c64 - bb)
+        r = s.astype(np.float32)
+        r64 = r.astype(np.float64)
+        other = np.where(s > r64, np.nextafter(r, np.float32(np.inf)), np.nextafter(r, np.float32(-np.inf)))
+        tie = np.isfinite(s) & (s != r64) & ((s - r64) == (other.astype(np.float64) - s))
+        up = tie & (e > 0)
+        down = tie & (e < 0)
+        out = np.where(up, np.maximum(r, other), np.where(down, np.minimum(r, other), r))
+    return out.astype(np.float32)
+
+
+def evaluate(ir_text: str, inputs: Sequence[np.ndarray], transcendental=None, fma: bool = False):
     """Evaluates an IR text on float32 inputs (flat arrays, in parameter order).
 
     Returns the flat float32 output (tuple roots interleaved as the kernel
     stores them) for an ``ew`` program, or the float32 element values that a
     ``sum`` program adds up.
+
+    ``transcendental(op, args)``, when given, supplies the float32 values of
+    exp/log/tanh ("exp", "log" or "tanh" of a float32 array) instead of the
+    correctly rounded ones.  The reference takes these three functions from the
+    vendor's math library, outside its own semantics; a caller that supplies a
+    device's values (checked against their error bound separately) gets that
+    device's bits for everything else the reference specifies: operation order,
+    rounding of every statement, views, padding.
+
+    ``fma``: the FMA-contraction mode (the runtime's CC_FLAG_FMA_CONTRACT):
+    every add or sub whose operand is a mul node computes that product and the
+    sum with one rounding (the left operand when both are products):
+    p*q + c and c + p*q -> fma(p, q, c), p*q - c -> fma(p, q, -c),
+    c - p*q -> fma(-p, q, c).
     """
     kind, out_shape, nodes, root = parse(ir_text)
     params: Dict[int, Tuple[int, Tuple[int, ...], np.float32]] = {}
@@ -185,14 +223,26 @@ def evaluate(ir_text: str, inputs: Sequence[np.ndarray]):
                     out = np.abs(a)
                 elif op == "sqrt":
                     out = np.sqrt(a)
-                elif op == "exp":
-                    out = _f64(np.exp, a)
-                elif op == "log":
-                    out = _f64(np.log, a)
-                elif op == "tanh":
-                    out = _f64(np.tanh, a)
+                elif op in ("exp", "log", "tanh"):
+                    if transcendental is not None:
+                        out = np.asarray(transcendental(op, a.astype(np.float32)), dtype=np.float32)
+                    else:
+                        out = _f64(getattr(np, op), a)
                 else:
                     raise ValueError(op)
+        elif tag == "b" and fma and ln[1] in ("add", "sub") and (
+                nodes[int(ln[2])][:2] == ["b", "mul"] or nodes[int(ln[3])][:2] == ["b", "mul"]):
+            left = nodes[int(ln[2])][:2] == ["b", "mul"]
+            m = nodes[int(ln[2]) if left else int(ln[3])]
+            p = ev(int(m[2]), fr, fid)
+            q = ev(int(m[3]), fr, fid)
+            c = ev(int(ln[3]) if left else int(ln[2]), fr, fid)
+            if ln[1] == "add":
+                out = fma32(p, q, c)
+            elif left:
+                out = fma32(p, q, -c)
+            else:
+                out = fma32(-p, q, c)
         elif tag == "b":
             a = ev(int(ln[2]), fr, fid)
             b = ev(int(ln[3]), fr, fid)
@@ -289,148 +339,3 @@ def window_text(ir_text: str, length: int) -> str:
             raise ValueError("node %s in a contiguous program" % ln[0])
     lines.append("r %d" % root)
     return "\n".join(lines) + "\n"
-
-
-_TRANSCENDENTAL = ("exp", "log", "tanh")
-
-
-def evaluate_with_bound(ir_text: str, inputs: Sequence[np.ndarray], ulps: float = 2.0, safety: float = 4.0,
-                        perturb=None):
-    """The oracle's values of a contiguous elementwise program (no views), and
-    per point a bound on how far a device whose exp/log/tanh are within
-    ``ulps`` ulp of the correctly rounded value (and whose other operations
-    round exactly like the oracle's) can be from them.
-
-    The bound is first-order error propagation: at each transcendental node the
-    device may differ by ``ulps`` ulp of the node's value; every node above one
-    may then round to a neighbouring float, one more ulp of its value; each
-    such difference reaches the output scaled by the output's partial
-    derivative with respect to that node (reverse-mode adjoints on the oracle's
-    values, in binary64, with max/min counted as 1-Lipschitz in both operands).
-    ``safety`` covers second-order terms.  Points where the bound is not finite
-    (a derivative overflows) come back with an infinite bound; the caller
-    decides how to treat them.  Without transcendentals the bound is 0: the
-    device must give the oracle's bits.
-
-    ``perturb`` (a numpy RandomState) turns the evaluation into a model of such
-    a device, for testing the bound itself: every exp/log/tanh result moves by
-    a random whole number of ulps in [-ulps, ulps].
-    """
-    kind, out_shape, nodes, root = parse(ir_text)
-    if kind != "ew":
-        raise ValueError("elementwise programs only")
-    values = []  # per node: float32 values
-    k = 0
-    param_input = {}
-    for i, ln in enumerate(nodes):
-        if ln[0] == "p":
-            param_input[i] = k
-            k += 1
-    if len(inputs) != k:
-        raise ValueError("program takes %d inputs, got %d" % (k, len(inputs)))
-    n = int(np.prod(out_shape, dtype=np.int64)) if out_shape else 1
-    flat = [np.ascontiguousarray(a, dtype=np.float32).ravel()[:n] for a in inputs]
-    affected = [False] * len(nodes)  # has a transcendental at or below it
-    for i, ln in enumerate(nodes):
-        tag = ln[0]
-        with np.errstate(all="ignore"):
-            if tag == "p":
-                v = None
-            elif tag == "x":
-                if ln[2:] != ["2", "1", "0"]:
-                    raise ValueError("views are not supported here")
-                v = flat[param_input[int(ln[1])]]
-            elif tag == "l":
-                v = np.full(n, bits_to_f32(ln[1]), dtype=np.float32)
-            elif tag == "u":
-                a = values[int(ln[2])]
-                op = ln[1]
-                affected[i] = affected[int(ln[2])] or op in _TRANSCENDENTAL
-                if op == "neg":
-                    v = -a
-                elif op == "abs":
-                    v = np.abs(a)
-                elif op == "sqrt":
-                    v = np.sqrt(a)
-                elif op in _TRANSCENDENTAL:
-                    v = _f64(getattr(np, op), a)
-                    if perturb is not None:
-                        for _ in range(int(ulps)):
-                            step = perturb.randint(-1, 2, size=v.shape)
-                            v = np.where(step > 0, np.nextafter(v, np.float32(np.inf)),
-                                         np.where(step < 0, np.nextafter(v, np.float32(-np.inf)), v))
-                        v = v.astype(np.float32)
-                else:
-                    raise ValueError(op)
-            elif tag == "b":
-                a, b = values[int(ln[2])], values[int(ln[3])]
-                affected[i] = affected[int(ln[2])] or affected[int(ln[3])]
-                op = ln[1]
-                v = {"add": np.add, "sub": np.subtract, "mul": np.multiply, "div": np.divide,
-                     "mod": np.fmod, "min": np.fmin, "max": np.fmax}[op](a, b)
-            else:
-                raise ValueError("node %s is not supported here" % tag)
-        values.append(v)
-    out = values[root].astype(np.float32)
-    if not affected[root]:
-        return out, np.zeros(n, dtype=np.float64)
-    # reverse-mode adjoints d out / d node, in binary64
-    adj = [None] * len(nodes)
-    adj[root] = np.ones(n, dtype=np.float64)
-    with np.errstate(all="ignore"):
-        for i in range(root, -1, -1):
-            a_i = adj[i]
-            ln = nodes[i]
-            if a_i is None or ln[0] in ("p", "x", "l"):
-                continue
-
-            def add(j, g):
-                g = np.where(a_i == 0.0, 0.0, g)  # no sensitivity stays none (0 * inf is not NaN here)
-                adj[j] = g if adj[j] is None else adj[j] + g
-
-            if ln[0] == "u":
-                j = int(ln[2])
-                x = values[j].astype(np.float64)
-                op = ln[1]
-                if op == "neg":
-                    add(j, -a_i)
-                elif op == "abs":
-                    add(j, a_i * np.sign(x))
-                elif op == "sqrt":
-                    add(j, a_i / (2.0 * np.sqrt(x)))
-                elif op == "exp":
-                    add(j, a_i * np.exp(x))
-                elif op == "log":
-                    add(j, a_i / x)
-                elif op == "tanh":
-                    add(j, a_i * (1.0 - np.tanh(x) ** 2))
-            else:
-                ja, jb = int(ln[2]), int(ln[3])
-                x = values[ja].astype(np.float64)
-                y = values[jb].astype(np.float64)
-                op = ln[1]
-                if op == "add":
-                    add(ja, a_i)
-                    add(jb, a_i)
-                elif op == "sub":
-                    add(ja, a_i)
-                    add(jb, -a_i)
-                elif op == "mul":
-                    add(ja, a_i * y)
-                    add(jb, a_i * x)
-                elif op == "div":
-                    add(ja, a_i / y)
-                    add(jb, -a_i * x / (y * y))
-                elif op in ("max", "min", "mod"):
-                    add(ja, np.abs(a_i))
-                    add(jb, np.abs(a_i) * (np.abs(x / y) + 1.0 if op == "mod" else 1.0))
-        bound = np.zeros(n, dtype=np.float64)
-        for i, ln in enumerate(nodes):
-            if not affected[i] or adj[i] is None:
-                continue
-            ulp = np.spacing(np.abs(values[i])).astype(np.float64)
-            own = ulps if (ln[0] == "u" and ln[1] in _TRANSCENDENTAL) else 0.0
-            bound += np.where(adj[i] == 0.0, 0.0, np.abs(adj[i]) * ulp * (own + 1.0))
-        bound *= safety
-        bound[~np.isfinite(bound)] = np.inf
-    return out, bound

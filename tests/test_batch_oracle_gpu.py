@@ -3,17 +3,18 @@
 2048 independent fused programs (seed 0), lengths log-uniform on [1K, 4M]
 (about 1.0e9 points), each a random 3-12-node tree over
 {+,-,*,/,exp,log,tanh,max} on 1-4 inputs uniform in [0.1, 2], evaluated by one
-persistent launch, by one launch per program and by a replayed CUDA graph.  The
+persistent launch, by a replayed CUDA graph and by one launch per program.  The
 reference evaluates each tensor with its own kernel (Tensors.scala:1331-1381),
-so every program's output must be what its own kernel computes:
+so every program's output must be what the oracle computes for its tree:
 
-* programs without exp/log/tanh: the oracle's bits (every operation is one
-  correctly rounded binary32 statement on both sides);
-* programs with them: within a per-point bound from first-order error
-  propagation (``oracle.interp.evaluate_with_bound``: the device's exp/log/tanh
-  within 2 ulp of the correctly rounded value, one more ulp of rounding at
-  every node above one, each scaled by the output's derivative with respect to
-  that node, times 4); a NaN must be a NaN, an infinity the same infinity.
+* the oracle takes exp/log/tanh of each transcendental node from the device's
+  own single-operation kernel (the reference takes them from the vendor's math
+  library, outside its own semantics), and every such value is checked within
+  2 ulp of the correctly rounded one; everything else -- the order of the
+  statements, the rounding of each, the operands -- is the oracle's, so every
+  program, with or without transcendentals, must give the oracle's bits.
+  (A derivative bound cannot serve here: one ulp of a logarithm near 1 turns
+  log(log(e)) from -6e-8 into 0 and a following 0/0 into NaN.)
 
 Each program is checked on up to three 4096-point windows: its first, its last
 and one at a seeded random place (the whole program when it is shorter).
@@ -34,21 +35,58 @@ def _windows(n, rs):
     return [(0, WINDOW), (mid, WINDOW), (n - WINDOW, WINDOW)]
 
 
-def _check(got, want, bound, where):
+def _ulp_distance(a, b):
+    """Distance in units in the last place between float32 arrays (finite values)."""
+    ia = a.view(np.int32).astype(np.int64)
+    ib = b.view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, -(ia & 0x7FFFFFFF), ia)
+    ib = np.where(ib < 0, -(ib & 0x7FFFFFFF), ib)
+    return np.abs(ia - ib)
+
+
+class DeviceFunctions:
+    """exp/log/tanh of float32 arrays from the device's single-operation
+    generated kernels, each value checked within 2 ulp of the correctly
+    rounded one (an infinity where the correctly rounded value is the largest
+    finite float, or the reverse, counts as one ulp)."""
+
+    def __init__(self, device):
+        self.rt = device.runtime
+        self.values = 0
+        self.worst = 0
+
+    def __call__(self, op, a):
+        rt = self.rt
+        n = int(a.size)
+        prog = rt.program("ccir 1 ew\no 1 %d\np 1 %d 00000000\nx 0 2 1 0\nu %s 1\nr 2\n" % (n, n, op))
+        src, dst = rt.alloc(4 * n), rt.alloc(4 * n)
+        try:
+            rt.upload(src, a)
+            rt.launch(prog, [src], dst)
+            got = rt.download(dst, n)
+        finally:
+            src.release()
+            dst.release()
+        with np.errstate(all="ignore"):
+            want = getattr(np, op)(a.astype(np.float64)).astype(np.float32)
+        nan = np.isnan(want)
+        assert np.array_equal(nan, np.isnan(got)), op
+        fin = ~nan & np.isfinite(want) & np.isfinite(got)
+        dist = _ulp_distance(got[fin], want[fin])
+        assert dist.size == 0 or dist.max() <= 2, (op, int(dist.max()))
+        edge = ~nan & ~fin
+        big = np.float32(np.finfo(np.float32).max)
+        ok_edge = (got[edge] == want[edge]) | ((np.abs(got[edge]) >= big) & (np.abs(want[edge]) >= big) &
+                                               (np.sign(got[edge]) == np.sign(want[edge])))
+        assert ok_edge.all(), op
+        self.values += n
+        self.worst = max(self.worst, int(dist.max()) if dist.size else 0)
+        return got
+
+
+def _same_bits(got, want):
     nan = np.isnan(want)
-    assert np.array_equal(nan, np.isnan(got)), where
-    exact = (bound == 0) & ~nan
-    assert np.array_equal(got[exact].view(np.int32), want[exact].view(np.int32)), where
-    inf = np.isinf(want) & ~exact
-    assert np.array_equal(got[inf], want[inf]), where
-    rest = ~nan & ~exact & ~inf & np.isfinite(bound)
-    g = got[rest].astype(np.float64)
-    w = want[rest].astype(np.float64)
-    # a finite oracle value next to the overflow threshold may round to infinity on the device
-    near_overflow = np.isinf(g) & (np.abs(w) > 1e38) & (np.sign(g) == np.sign(w))
-    ok = (np.abs(g - w) <= bound[rest]) | near_overflow
-    assert ok.all(), (where, g[~ok][:4], w[~ok][:4], bound[rest][~ok][:4])
-    return int(rest.sum()), int((~nan & ~np.isfinite(bound) & ~inf).sum())
+    return np.array_equal(nan, np.isnan(got)) and np.array_equal(got[~nan].view(np.int32), want[~nan].view(np.int32))
 
 
 def test_every_batched_program_matches_the_oracle_at_the_benchmark_config(cuda_device):
@@ -60,39 +98,34 @@ def test_every_batched_program_matches_the_oracle_at_the_benchmark_config(cuda_d
     progs = bench.c4_programs(d.Tensor, seed=0, count=2048)
     tensors = [t for t, _ in progs]
     b = Batch(d, tensors).bind()
+    fns = DeviceFunctions(d)
     try:
         rs = np.random.RandomState(0)
-        plan = []  # per program: windows, oracle values and bounds
+        plan = []  # per program: windows, and the oracle's values on them
         n_transcendental = 0
         total_points = 0
         for k, (t, ser) in enumerate(zip(tensors, b.serialized)):
             n = int(t.shape[0])
             total_points += n
-            entries = []
-            for start, length in _windows(n, rs):
-                ins = [rt.download(p._cached, length, offset=4 * start) for p in ser.params]
-                want, bound = interp.evaluate_with_bound(interp.window_text(ser.text, length), ins)
-                entries.append((start, length, want, bound))
+            wins = _windows(n, rs)
+            length = sum(w for _, w in wins)
+            # the program is pointwise: its windows, side by side, are one program of their total length
+            ins = [np.concatenate([rt.download(p._cached, w, offset=4 * s) for s, w in wins]) for p in ser.params]
+            want = interp.evaluate(interp.window_text(ser.text, length), ins, transcendental=fns)
             if any(("u %s " % op) in ser.text for op in ("exp", "log", "tanh")):
                 n_transcendental += 1
-            plan.append(entries)
+            plan.append((wins, want))
         assert len(plan) == 2048 and total_points > 9e8
         assert 0 < n_transcendental < 2048
-        checked = unbounded = 0
         for mode in (Batch.PERSISTENT, Batch.GRAPH, Batch.PER_PROGRAM):
-            for k, entries in enumerate(plan):
-                for start, length, _, _ in entries:
-                    rt.upload(b.outputs[k], np.full(length, np.nan, np.float32), offset=4 * start)
+            for k, (wins, _) in enumerate(plan):
+                for s, w in wins:
+                    rt.upload(b.outputs[k], np.full(w, np.nan, np.float32), offset=4 * s)
             b.run(mode)
-            for k, entries in enumerate(plan):
-                for start, length, want, bound in entries:
-                    got = rt.download(b.outputs[k], length, offset=4 * start)
-                    c, u = _check(got, want, bound, (mode, k, start))
-                    checked += c
-                    unbounded += u
-        # points whose bound overflows (an infinity that reaches the output) are checked for NaN-ness only
-        assert checked > 0 and unbounded < checked
-        print("checked %d points within the bound, %d without a finite bound" % (checked, unbounded))
+            for k, (wins, want) in enumerate(plan):
+                got = np.concatenate([rt.download(b.outputs[k], w, offset=4 * s) for s, w in wins])
+                assert _same_bits(got, want), (mode, k)
+        print("device exp/log/tanh: %d values, worst %d ulp" % (fns.values, fns.worst))
     finally:
         b.close()
         for _, inputs in progs:

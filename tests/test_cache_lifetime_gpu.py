@@ -50,7 +50,7 @@ def test_closed_cache_returns_its_block_and_refuses_use(cuda_device):
     T = d.Tensor
     rt.synchronize()
     before = rt.pool_stats()
-    w = T.randomNormal([1000, 1000], seed=5).doCache()
+    w = T.randomNormal([1000, 1000], seed=0x40000005).doCache()  # bit 30: no zero hash (log 0) below 2^30
     mid = rt.pool_stats()
     assert mid["in_use"] >= before["in_use"] + 4 * 10 ** 6
     total = (w * w).sum().readScalar()
@@ -61,6 +61,6 @@ def test_closed_cache_returns_its_block_and_refuses_use(cuda_device):
     assert after["cached"] > mid["cached"]  # the block went back to the pool's free list
     with pytest.raises(IllegalArgumentException):
         (w + w).flatArray()
-    again = T.randomNormal([1000, 1000], seed=6).doCache()
+    again = T.randomNormal([1000, 1000], seed=0x40000006).doCache()
     assert rt.pool_stats()["reuses"] > after["reuses"]  # the released block serves the next cache
     again.close()

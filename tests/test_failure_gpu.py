@@ -22,6 +22,8 @@ def _still_computes(device):
 
 def test_pool_limit_turns_allocations_into_errors(cuda_device):
     rt = cuda_device.runtime
+    rt.synchronize()
+    rt.pool_trim()  # a cached block of the size asked for would be reused within the cap
     in_use = rt.pool_stats()["in_use"]
     rt.pool_set_limit(in_use + (1 << 20))
     try:

@@ -222,7 +222,7 @@ def test_vector_load_codegen():
     assert vl.count("cc_ld4(_") == 18 and "cc_ld(_" not in vl  # 9 offsets x 2 groups of 4 channels
     # the staged weights (filters innermost) and bias as float4 shared reads: 9 x 8 x 2 + 2
     assert vl.count("reinterpret_cast<const float4 *>(cc_sp") == 146
-    assert "__align__(16) float cc_sp2[576]" in vl and "__align__" not in scalar
+    assert "__align__(16) float cc_sp2[576]" in vl and "__align__(16) float cc_sp" not in scalar
     assert runtime.codegen(text, "vl=1 points=2").split("cc_ew_vl(")[1].count("cc_ld4(_") == 24
     runtime.compile_check(text, options="vl=1 points=2")
     # a view whose innermost index varies with the output has nothing to group

@@ -50,7 +50,7 @@ def _two_chains(dev, n, depth):
     y = T.randomNormal([n, 64], seed=32)
     cx, cy = x, y
     for k in range(depth):
-        cx = (T.tanh(cx) * T.fill(1.5, [n, 64]) + T.fill(0.25, [n, 64])).nonInline()
+        cx = (T.abs(cx) * T.fill(-1.5, [n, 64]) + T.fill(0.25, [n, 64])).nonInline()
         cy = (cy * T.fill(0.5, [n, 64]) - T.fill(1.0, [n, 64])).nonInline()
         if k % 3 == 2:
             cx = cx.transpose().transpose().translate([1, 0]).nonInline()  # a view kernel in the chain
@@ -59,7 +59,8 @@ def _two_chains(dev, n, depth):
 
 
 def test_independent_chains_joined_by_wait_lists_match_the_oracle():
-    """Two chains of nonInline kernels that share nothing until the end run on
+    """Two chains of nonInline kernels (no transcendentals: every statement is
+    correctly rounded on both sides) that share nothing until the end run on
     different queues; the kernel that joins them waits for both.  Elementwise
     results are the oracle's bits; the final sum (on a queue, with that queue's
     own partials) is within sqrt(n) * 2^-24 of the oracle's."""
