@@ -387,6 +387,26 @@ def time_device(rt, st, steps, warmup):
     return ms
 
 
+def launch_floor(d, steps=200, warmup=10):
+    """Per-launch time of the fused elementwise+sum program on 4 points (one
+    block, one partial), launched back to back like the benchmark: the fixed
+    cost a launch of this kernel pays whatever its size."""
+    T = d.Tensor
+    rt = d.runtime
+    tiny = [(T.random([1, 4], seed=s) * T.fill(2.0, [1, 4]) - T.fill(1.0, [1, 4])).doCache() for s in (0, 1, 2)]
+    expr = T.tanh(tiny[0] * tiny[1] + tiny[2])
+    prog = rt.program(d.serialize(expr.closure, expr.shape, "sum").text)
+    out = rt.alloc(4)
+    st = {"prog": prog, "sets": [[t._cached for t in tiny]], "out": out}
+    for i in range(warmup):
+        rt.launch_ptrs(prog, [t._cached.device_ptr() for t in tiny], out.device_ptr())
+    ms = time_device(rt, st, steps, warmup) / steps
+    out.release()
+    for t in tiny:
+        t.close()
+    return ms
+
+
 def time_isolated(rt, st, reps):
     """Median device time of single launches, each alone between two synchronisations."""
     prog, sets, out = st["prog"], st["sets"], st["out"]
@@ -740,6 +760,13 @@ def measure_fused(d, workload, steps, warmup, rank=0, world=1, local_rank=0, dis
             "clocks": clocks, "hot_l2": hot, "launch_overlap": overlap}
     if cpu_fast is not None:
         line["cpu_baseline_fp_contract_fast"] = cpu_fast
+    if workload == "c1":
+        floor_ms = launch_floor(d, steps, warmup)
+        bytes_ms = st["bytes"] / (peak * 1e9) * 1e3
+        line["launch_floor"] = {
+            "ms": floor_ms, "note": "the same kernel on 4 points (one block), back to back",
+            "bound_ms": bytes_ms + floor_ms, "frac_of_bound": (bytes_ms + floor_ms) / ms_step,
+            "bound_note": "algorithmic bytes at the measured HBM peak plus the per-launch floor"}
     release(st)
     return line
 
@@ -786,7 +813,7 @@ def measure_tuner_eval(rt, programs, seed, model_path):
     sm = rt.device_info()["sm_count"]
     t0 = time.time()
     progs = tuner.random_programs(programs, seed=seed)
-    recs = tuner.collect(rt, progs, reps=5, flush_l2=True)
+    recs = tuner.collect(rt, progs, reps=5, flush_l2=True, standard=True)
     collect_s = time.time() - t0
     model = tuner.CostModel(rt, seed=0)
     try:

@@ -192,11 +192,39 @@ def random_programs(count: int, seed: int = 0, max_points: int = MAX_POINTS, max
     return [random_program(r, d, max_points, max_dim) for _ in range(count)]
 
 
+def time_standard(runtime, ir_text: str, ptrs: Sequence[int], flush, reps: int = 5) -> float:
+    """Median device time (ms) of the program's standard generated kernel (the
+    runtime's default path), one untimed launch first, each timed launch after
+    ``flush`` (a buffer larger than L2) is rewritten."""
+    saved = runtime.config_get("tuner")
+    if saved:
+        runtime.config_set("tuner", 0)
+    try:
+        prog = runtime.program(ir_text)
+    finally:
+        if saved:
+            runtime.config_set("tuner", saved)
+    runtime.launch_ptrs(prog, ptrs[:-1], ptrs[-1])
+    times = []
+    for r in range(reps):
+        if flush is not None:
+            runtime.random(flush, flush.nbytes // 4, r, False)
+        e0 = runtime.event()
+        runtime.launch_ptrs(prog, ptrs[:-1], ptrs[-1])
+        e1 = runtime.event()
+        runtime.event_wait(e1, 60 * 10 ** 9)
+        times.append(runtime.event_elapsed_ms(e0, e1))
+        runtime.event_release(e0)
+        runtime.event_release(e1)
+    return float(sorted(times)[reps // 2])
+
+
 def collect(runtime, programs: Sequence[dict], reps: int = 5, flush_l2: bool = True, chunk: int = 256,
-            log=None, time_budget_s: Optional[float] = None) -> List[dict]:
+            log=None, time_budget_s: Optional[float] = None, standard: bool = False) -> List[dict]:
     """Times every configuration of every program; returns one record per program
     ({"ir", "params", "kind", "points", "ms": [48 floats]}), and appends them to
-    the file-like ``log`` as JSON lines when given.
+    the file-like ``log`` as JSON lines when given.  With ``standard`` a record
+    also holds "std_ms", the time of the program's standard generated kernel.
 
     Inputs are four shared device buffers of MAX_POINTS floats uniform in
     [0.1, 2] (input i of every program reads buffer i), the output another."""
@@ -214,6 +242,7 @@ def collect(runtime, programs: Sequence[dict], reps: int = 5, flush_l2: bool = T
         bufs.append(b)
     ptr_in = [b.device_ptr() for b in bufs]
     ptr_out = out.device_ptr()
+    flush = runtime.alloc(256 << 20) if (standard and flush_l2) else None
     records = []
     t0 = time.time()
     firsts = list(range(0, len(programs), chunk))
@@ -236,6 +265,8 @@ def collect(runtime, programs: Sequence[dict], reps: int = 5, flush_l2: bool = T
                     ms = ts.time(k, ptrs, reps=reps, flush_l2=flush_l2)
                     rec = dict(q)
                     rec["ms"] = [float(x) for x in ms]
+                    if standard:
+                        rec["std_ms"] = time_standard(runtime, q["ir"], ptrs, flush, reps)
                     records.append(rec)
                     if log is not None:
                         log.write(json.dumps(rec) + "\n")
@@ -253,6 +284,8 @@ def collect(runtime, programs: Sequence[dict], reps: int = 5, flush_l2: bool = T
         for b in bufs:
             b.release()
         out.release()
+        if flush is not None:
+            flush.release()
     return records
 
 
@@ -477,6 +510,23 @@ def evaluate(model: CostModel, records: Sequence[dict], sm_count: int, fixed: Op
     if fixed is not None:
         out["best_fixed"] = summary([fixed] * len(records))
         out["best_fixed"]["config"] = fixed
+    if all("std_ms" in r for r in records):
+        # the runtime's tuner also times the standard generated kernel (the product's
+        # default) and keeps the faster: learned = min(model's first choice, standard)
+        std = np.array([r["std_ms"] for r in records], dtype=np.float64)
+        pick = np.array([ms[i, p] if ms[i, p] > 0 else np.inf for i, p in enumerate(learned)])
+        tuned = np.minimum(pick, std)
+        best49 = np.minimum(np.where(ms > 0, ms, np.inf).min(axis=1), std)
+        out["vs_standard_kernel"] = {
+            "learned_speedup_geomean": float(np.exp(np.mean(np.log(std / tuned)))),
+            "learned_speedup_total": float(std.sum() / tuned.sum()),
+            "exhaustive_speedup_geomean": float(np.exp(np.mean(np.log(std / best49)))),
+            "exhaustive_speedup_total": float(std.sum() / best49.sum()),
+            "learned_regret_vs_exhaustive_geomean": float(np.exp(np.mean(np.log(tuned / best49)))) - 1.0,
+            "standard_wins": int((std <= pick).sum()),
+            "note": "standard = the runtime's default generated kernel; learned = the faster of the model's "
+                    "first choice and the standard kernel (what the learned tuner keeps); exhaustive = the "
+                    "fastest of the 48 configurations and the standard kernel"}
     return out
 
 

@@ -1500,12 +1500,12 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << contig_scalar << "    cc_acc(s_, c_, " << contig_call("") << ");\n  }\n"
-        << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n"
+        << "  cc_grid_finish_pdl(s_, c_, partials, counter, out, cc_early);\n}\n\n"
         << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum_v4(" << params
         << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
         << "  float s_ = 0.0f, c_ = 0.0f;\n"
         << vec4_loop(ir.n_params, U, false, contig_call)
-        << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+        << "  cc_grid_finish_pdl(s_, c_, partials, counter, out, cc_early);\n}\n\n";
   } else if (ir.kind == ProgramKind::Elementwise) {
     auto ew_kernel = [&](const std::string &name, const std::string &ring, const std::string &body,
                          const std::vector<std::vector<std::string>> &point_results) {
@@ -1559,7 +1559,7 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
         << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
         << generic.str() << "    cc_acc(s_, c_, " << results[0] << ");\n  }\n"
-        << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+        << "  cc_grid_finish_pdl(s_, c_, partials, counter, out, cc_early);\n}\n\n";
     if (g.has_vl) {
       // the same points in the same order: only the reads differ, so the sum's bits do not
       src << "extern \"C\" __global__ void __launch_bounds__(" << lb << ") cc_sum_vl(" << params
@@ -1568,14 +1568,14 @@ Generated generate_cuda(const Ir &ir, const CodegenOptions &opt) {
           << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
           << "  for (cc_i64 lin = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x; lin < n; lin += stride) {\n"
           << vl_body.str() << "    cc_acc(s_, c_, " << vl_res[0][0] << ");\n  }\n"
-          << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+          << "  cc_grid_finish_pdl(s_, c_, partials, counter, out, cc_early);\n}\n\n";
     }
     if (contiguous) {
       src << "extern \"C\" __global__ void __launch_bounds__(" << block << ") cc_sum_v4(" << params
           << "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out, cc_i64 n) {\n"
           << "  float s_ = 0.0f, c_ = 0.0f;\n"
           << vec4_loop(ir.n_params, U, false, contig_call)
-          << "  cc_pdl_gate(cc_early);\n  cc_grid_finish(s_, c_, partials, counter, out);\n}\n\n";
+          << "  cc_grid_finish_pdl(s_, c_, partials, counter, out, cc_early);\n}\n\n";
     }
   }
   g.source = src.str();

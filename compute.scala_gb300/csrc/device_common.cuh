@@ -120,6 +120,51 @@ __device__ __forceinline__ void cc_pdl_gate(int &early) {
   }
 }
 
+// The grid sum's finish in generated kernels launched with programmatic
+// dependent launch.  The partials and the completion counter are the launch's
+// own (the runtime alternates two scratch blocks between consecutive sums on
+// its stream), so only the last block, before it writes `out`, waits for the
+// previous kernel (`early` = 1; with early = 0 the kernel waited at entry):
+// the other blocks publish their partials and leave without waiting, and
+// consecutive sums overlap everything but their final stores.  One block needs
+// no partials at all.  Thread 0's partial store is ordered before its ticket
+// by the atomic's release; the last block's thread 0 acquires every partial
+// through its own ticket and the barrier passes that on to the block.
+__device__ __forceinline__ void cc_grid_finish_pdl(float s, float c, float2 *__restrict__ partials,
+                                                   unsigned int *__restrict__ counter, float *__restrict__ out,
+                                                   int early) {
+  __shared__ float2 ws[32];
+  __shared__ int last;
+  cc_block_merge(s, c, ws);
+  if (gridDim.x == 1) {
+    if (threadIdx.x == 0) {
+      if (early) cc_pdl_wait_then_release();
+      out[0] = isfinite(s) ? __fadd_rn(s, c) : s;
+    }
+    return;
+  }
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = make_float2(s, c);
+    unsigned int ticket;
+    asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(ticket) : "l"(counter) : "memory");
+    last = (ticket == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  s = 0.0f;
+  c = 0.0f;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    float2 p = __ldcg(&partials[i]);
+    cc_merge(s, c, p.x, p.y);
+  }
+  cc_block_merge(s, c, ws);
+  if (threadIdx.x == 0) {
+    if (early) cc_pdl_wait_then_release();
+    out[0] = isfinite(s) ? __fadd_rn(s, c) : s;
+    *counter = 0u;
+  }
+}
+
 // Asynchronous 4-byte copy from global memory into a shared-memory slot
 // (cp.async): the load holds no register while it is in flight, so a thread
 // can have as many loads outstanding as its slots allow.  Each copy is its own

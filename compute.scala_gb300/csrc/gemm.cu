@@ -119,53 +119,98 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 
   l = __float2bfloat16_rn(r2);
 }
 
-// src: rows x cols floats, row-major with leading dimension ld (or, when
-// transpose, the matrix is read as its transpose: element (r, c) = src[c*ld + r]).
-// dst: three planes of prows x pcols bf16, row-major, zero outside rows x cols.
+// Eight floats to three planes of eight bfloat16 each (one 16-byte word per plane).
+__device__ __forceinline__ void split8(const float (&x)[8], uint4 &h, uint4 &m, uint4 &l) {
+  __nv_bfloat16 hh[8], mm[8], ll[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) split3(x[e], hh[e], mm[e], ll[e]);
+  h = *reinterpret_cast<const uint4 *>(hh);
+  m = *reinterpret_cast<const uint4 *>(mm);
+  l = *reinterpret_cast<const uint4 *>(ll);
+}
+
+// src: rows x cols floats, row-major with leading dimension ld.  dst: three
+// planes of prows x pcols bf16, row-major, zero outside rows x cols (pcols a
+// multiple of 32).  Each thread takes runs of eight columns: two 16-byte loads
+// when the run lies inside the matrix and src is 16-byte aligned with ld a
+// multiple of 4, and one 16-byte store per plane.
 __global__ void __launch_bounds__(256) split_planes_kernel(const float *__restrict__ src, long long ld, int rows,
-                                                           int cols, int transpose, __nv_bfloat16 *__restrict__ dst,
+                                                           int cols, int vec, __nv_bfloat16 *__restrict__ dst,
                                                            int prows, int pcols) {
   const long long plane = (long long)prows * pcols;
-  const long long total = plane;
+  const unsigned runs = (unsigned)pcols >> 3;
+  const long long total = (long long)prows * runs;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
-    const int r = (int)(i / pcols), c = (int)(i % pcols);
-    float x = 0.0f;
-    if (r < rows && c < cols) x = transpose ? __ldg(src + (long long)c * ld + r) : __ldg(src + (long long)r * ld + c);
-    __nv_bfloat16 h, m, l;
-    split3(x, h, m, l);
-    dst[i] = h;
-    dst[plane + i] = m;
-    dst[2 * plane + i] = l;
+    const int r = (int)(i / runs), c0 = (int)(i - (long long)r * runs) * 8;
+    float x[8];
+    const float *row = src + (long long)r * ld;
+    if (vec && r < rows && c0 + 8 <= cols) {
+      const float4 a = __ldg(reinterpret_cast<const float4 *>(row + c0));
+      const float4 b = __ldg(reinterpret_cast<const float4 *>(row + c0 + 4));
+      x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+      x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+    } else {
+#pragma unroll
+      for (int e = 0; e < 8; ++e) x[e] = (r < rows && c0 + e < cols) ? __ldg(row + c0 + e) : 0.0f;
+    }
+    uint4 h, m, l;
+    split8(x, h, m, l);
+    const long long o = (long long)r * pcols + c0;
+    *reinterpret_cast<uint4 *>(dst + o) = h;
+    *reinterpret_cast<uint4 *>(dst + plane + o) = m;
+    *reinterpret_cast<uint4 *>(dst + 2 * plane + o) = l;
   }
 }
 
-// Transposing split through shared memory so both the fp32 reads and the bf16
-// writes are coalesced: a 32x32 tile of src (rows = K, cols = N) becomes a
-// 32x32 tile of the planes (rows = N, cols = K).
+// Transposing split through shared memory: a 64 (k) x 64 (n) tile of src
+// (rows = K, cols = N, row-major) becomes a 64 x 64 tile of the planes (rows =
+// N, cols = K).  Loads are 16-byte reads along n (when src allows), stores
+// two 16-byte words per plane, 16 consecutive k of one n per thread.
 __global__ void __launch_bounds__(256) split_planes_t_kernel(const float *__restrict__ src, long long ld, int krows,
-                                                             int ncols, __nv_bfloat16 *__restrict__ dst, int prows,
-                                                             int pcols) {
-  __shared__ float tile[32][33];
+                                                             int ncols, int vec, __nv_bfloat16 *__restrict__ dst,
+                                                             int prows, int pcols) {
+  __shared__ __align__(16) float tile[64][68];
   const long long plane = (long long)prows * pcols;
-  const int k0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-  for (int r = ty; r < 32; r += 8) {
-    const int k = k0 + r, n = n0 + tx;
-    tile[r][tx] = (k < krows && n < ncols) ? __ldg(src + (long long)k * ld + n) : 0.0f;
+  const int k0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
+  const int t = threadIdx.x;
+  const int lc = (t & 15) * 4;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int kr = (t >> 4) + 16 * q;
+    const int k = k0 + kr, n = n0 + lc;
+    float4 v;
+    if (vec && k < krows && n + 4 <= ncols) {
+      v = __ldg(reinterpret_cast<const float4 *>(src + (long long)k * ld + n));
+    } else {
+      const float *p = src + (long long)k * ld;
+      v.x = (k < krows && n + 0 < ncols) ? __ldg(p + n + 0) : 0.0f;
+      v.y = (k < krows && n + 1 < ncols) ? __ldg(p + n + 1) : 0.0f;
+      v.z = (k < krows && n + 2 < ncols) ? __ldg(p + n + 2) : 0.0f;
+      v.w = (k < krows && n + 3 < ncols) ? __ldg(p + n + 3) : 0.0f;
+    }
+    *reinterpret_cast<float4 *>(&tile[kr][lc]) = v;
   }
   __syncthreads();
-  for (int r = ty; r < 32; r += 8) {
-    const int n = n0 + r, k = k0 + tx;
-    if (n < prows && k < pcols) {
-      __nv_bfloat16 h, m, l;
-      split3(tile[tx][r], h, m, l);
-      const long long o = (long long)n * pcols + k;
-      dst[o] = h;
-      dst[plane + o] = m;
-      dst[2 * plane + o] = l;
-    }
+  const int nl = t & 63, kc = (t >> 6) * 16;  // a warp: 32 consecutive n, one run of 16 k
+  const int n = n0 + nl, k = k0 + kc;
+  if (n >= prows || k >= pcols) return;
+  float x[8], y[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    x[e] = tile[kc + e][nl];
+    y[e] = tile[kc + 8 + e][nl];
   }
+  uint4 h0, m0, l0, h1, m1, l1;
+  split8(x, h0, m0, l0);
+  split8(y, h1, m1, l1);
+  const long long o = (long long)n * pcols + k;
+  uint4 *d0 = reinterpret_cast<uint4 *>(dst + o);
+  uint4 *d1 = reinterpret_cast<uint4 *>(dst + plane + o);
+  uint4 *d2 = reinterpret_cast<uint4 *>(dst + 2 * plane + o);
+  d0[0] = h0; d0[1] = h1;
+  d1[0] = m0; d1[1] = m1;
+  d2[0] = l0; d2[1] = l1;
 }
 
 }  // namespace
@@ -184,17 +229,21 @@ cudaError_t launch_sgemm(const float *A, const float *B, float *C, int M, int N,
 
 cudaError_t launch_split_a(const float *A, long long lda, int M, int K, __nv_bfloat16 *planes, int Mp, int Kp,
                            int sm_count, cudaStream_t stream) {
-  long long total = (long long)Mp * Kp;
+  if (Kp % 32 != 0) return cudaErrorInvalidValue;
+  long long total = (long long)Mp * (Kp / 8);
   long long grid = (total + 255) / 256;
-  if (grid > (long long)sm_count * 16) grid = (long long)sm_count * 16;
-  split_planes_kernel<<<(unsigned)grid, 256, 0, stream>>>(A, lda, M, K, 0, planes, Mp, Kp);
+  if (grid > (long long)sm_count * 8) grid = (long long)sm_count * 8;
+  const int vec = ((reinterpret_cast<uintptr_t>(A) & 15u) == 0 && lda % 4 == 0) ? 1 : 0;
+  split_planes_kernel<<<(unsigned)grid, 256, 0, stream>>>(A, lda, M, K, vec, planes, Mp, Kp);
   return cudaGetLastError();
 }
 
 cudaError_t launch_split_bt(const float *B, long long ldb, int K, int N, __nv_bfloat16 *planes, int Np, int Kp,
                             cudaStream_t stream) {
-  dim3 grid((Kp + 31) / 32, (Np + 31) / 32);
-  split_planes_t_kernel<<<grid, 256, 0, stream>>>(B, ldb, K, N, planes, Np, Kp);
+  if (Kp % 32 != 0 || Np % 64 != 0) return cudaErrorInvalidValue;
+  dim3 grid((Kp + 63) / 64, Np / 64);
+  const int vec = ((reinterpret_cast<uintptr_t>(B) & 15u) == 0 && ldb % 4 == 0) ? 1 : 0;
+  split_planes_t_kernel<<<grid, 256, 0, stream>>>(B, ldb, K, N, vec, planes, Np, Kp);
   return cudaGetLastError();
 }
 

@@ -209,6 +209,8 @@ struct TuneConfig {
   int block = 256, vec = 1, ept = 1, split = 1;
 };
 constexpr int kTuneConfigs = 48;
+// The tuner's choice "the program's standard generated kernel" (no tunable configuration).
+constexpr int kStdConfig = kTuneConfigs;
 constexpr int kTuneKernels = 6;  // (vec, ept) pairs compiled per program
 constexpr int kFeatures = 64;
 TuneConfig tune_config(int index);

@@ -16,6 +16,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -420,12 +421,14 @@ struct Context {
   // Scratch of the grid sums: kMaxSumBlocks float2 partials, then the counter.
   void *sum_scratch = nullptr;
   size_t sum_scratch_cls = 0;
+  // A second block that consecutive sums on the context stream alternate with:
+  // a generated sum's blocks publish their partials without waiting for the
+  // previous kernel, which may be the previous sum.
+  void *sum_scratch_alt = nullptr;
+  size_t sum_scratch_alt_cls = 0;
+  int sum_parity = 0;
 
   uint64_t make_handle(uint64_t tag) { return (tag << 56) | (next_id++); }
-  float2 *partials() { return reinterpret_cast<float2 *>(sum_scratch); }
-  unsigned int *counter() {
-    return reinterpret_cast<unsigned int *>(static_cast<char *>(sum_scratch) + sizeof(float2) * kMaxSumBlocks);
-  }
   // Device error flag of the kernels with bounded waits (in the same scratch block).
   int *error_flag() {
     return reinterpret_cast<int *>(static_cast<char *>(sum_scratch) + sizeof(float2) * kMaxSumBlocks + 128);
@@ -534,7 +537,10 @@ void release_block(Context &c, void *p, size_t cls) {
 // then set and the caller releases it after synchronising the stream.
 void *sum_scratch_for(Context &c, cudaStream_t s, size_t *temporary_cls) {
   *temporary_cls = 0;
-  if (s == c.stream) return c.sum_scratch;
+  if (s == c.stream) {
+    c.sum_parity ^= 1;
+    return c.sum_parity ? c.sum_scratch_alt : c.sum_scratch;
+  }
   const int q = queue_index(c, s);
   if (q >= 0) return c.queue_scratch[q];
   size_t cls = 0;
@@ -734,6 +740,8 @@ void launch_row_fold(Context &c, Program &p, const std::vector<uint64_t> &in, ui
            "cuLaunchKernel");
 }
 
+void launch_generated(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream);
+
 void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
   if (p.tune || p.is_contraction || p.is_row_fold) end_pdl_chain(c);
   if (p.is_row_fold) {
@@ -750,6 +758,11 @@ void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uin
              reinterpret_cast<float *>(out), (int)q.m, (int)q.n, (int)q.k, q.k, q.n, q.n, p.contraction_mode, stream);
     return;
   }
+  launch_generated(c, p, in, out, stream);
+}
+
+// The standard generated kernels (cc_ew / cc_ew_v4 / cc_ew_vl, cc_sum*) of a program.
+void launch_generated(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
   const Module &m = *p.mod;
   const int block = m.block;
   const int64_t n = p.gen.domain;
@@ -962,6 +975,9 @@ int cc_init(int device_ordinal, uint32_t flags) {
   c->stream = c->own_stream;
   c->sum_scratch = c->pool.alloc(sizeof(float2) * kMaxSumBlocks + 256, &c->sum_scratch_cls);
   check_cuda(cudaMemsetAsync(c->sum_scratch, 0, sizeof(float2) * kMaxSumBlocks + 256, c->stream), "cudaMemsetAsync");
+  c->sum_scratch_alt = c->pool.alloc(sizeof(float2) * kMaxSumBlocks + 256, &c->sum_scratch_alt_cls);
+  check_cuda(cudaMemsetAsync(c->sum_scratch_alt, 0, sizeof(float2) * kMaxSumBlocks + 256, c->stream),
+             "cudaMemsetAsync");
   check_cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
   g_ctx = c.release();
   CC_API_END
@@ -1011,6 +1027,7 @@ int cc_shutdown(void) {
   }
   c->events.clear();
   release_block(*c, c->sum_scratch, c->sum_scratch_cls);
+  release_block(*c, c->sum_scratch_alt, c->sum_scratch_alt_cls);
   for (int i = 0; i < kQueues; ++i)
     if (c->queue_scratch[i]) release_block(*c, c->queue_scratch[i], c->queue_scratch_cls[i]);
   c->pool.trim();
@@ -1364,6 +1381,74 @@ int cc_pool_trim(void) {
 
 // ---------------------------------------------------------------- programs
 
+}  // extern "C"
+
+namespace {
+
+// The standard kernels of a program (cc_ew / cc_ew_v4 / cc_ew_vl or cc_sum*),
+// compiled and loaded; contiguous programs share one module per structure.
+std::shared_ptr<Module> standard_module(Context &c, const Ir &ir, CodegenOptions opt, const std::string &key,
+                                        Generated *gen_out) {
+  int64_t domain = 1;
+  for (int64_t d : ir.out_shape) domain *= d;
+  // Contiguous programs compile once per structure; the shape only sizes the launch.
+  std::string skey = contiguous_structure_key(ir);
+  if (!skey.empty()) {
+    skey += key.substr(key.rfind('#'));
+    opt.min_blocks = 0;
+  } else {
+    // threads, not points: a thread of a multi-point kernel takes several
+    opt.min_blocks = choose_min_blocks(domain / points_for(ir, opt.points_per_thread), opt.block, c.sm_count,
+                                       -opt.min_blocks);
+  }
+  std::shared_ptr<Module> mod;
+  if (!skey.empty()) {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    auto it = c.modules.find(skey);
+    if (it != c.modules.end()) mod = it->second;
+  }
+  if (mod) {
+    (*gen_out) = describe_program(ir);
+  } else {
+    (*gen_out) = generate_cuda(ir, opt);
+    mod = std::make_shared<Module>();
+    mod->source = (*gen_out).source;
+    std::vector<char> cubin = compile_cubin(mod->source, c.cc_major, c.cc_minor, c.flags);
+    check_cu(g_drv.ModuleLoadData(&mod->module, cubin.data()), "cuModuleLoadData");
+    const char *sname = ir.kind == ProgramKind::Sum ? "cc_sum" : "cc_ew";
+    const char *vname = ir.kind == ProgramKind::Sum ? "cc_sum_v4" : "cc_ew_v4";
+    check_cu(g_drv.ModuleGetFunction(&mod->scalar, mod->module, sname), "cuModuleGetFunction");
+    if ((*gen_out).has_vec4) check_cu(g_drv.ModuleGetFunction(&mod->vec4, mod->module, vname), "cuModuleGetFunction");
+    if ((*gen_out).has_vl)
+      check_cu(g_drv.ModuleGetFunction(&mod->vl, mod->module, ir.kind == ProgramKind::Sum ? "cc_sum_vl" : "cc_ew_vl"),
+               "cuModuleGetFunction");
+    mod->block = opt.block;
+    mod->vec_unroll = (*gen_out).vec_unroll;
+    mod->smem_bytes = (*gen_out).smem_bytes;
+    mod->points = (*gen_out).points_per_thread;
+    if (mod->smem_bytes > 48 * 1024)
+      check_cu(g_drv.FuncSetAttribute(mod->scalar, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, mod->smem_bytes),
+               "cuFuncSetAttribute");
+    check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_scalar, mod->scalar, mod->block, mod->smem_bytes),
+             "cuOccupancyMaxActiveBlocks");
+    if (mod->vec4)
+      check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_vec4, mod->vec4, mod->block, 0),
+               "cuOccupancyMaxActiveBlocks");
+    if (mod->vl)
+      check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_vl, mod->vl, mod->block, 0),
+               "cuOccupancyMaxActiveBlocks");
+    if (!skey.empty()) {
+      std::lock_guard<std::recursive_mutex> g(c.mu);
+      c.modules[skey] = mod;
+    }
+  }
+  return mod;
+}
+
+}  // namespace
+
+extern "C" {
+
 int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   CC_API_BEGIN
   if (!ir_text || !out) fail(CC_ERR_INVALID_VALUE, "null pointer");
@@ -1473,15 +1558,16 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     tuner_mode = c.tuner;
   }
   if (tuner_mode > 0 && is_tunable(ir, nullptr)) {
-    // The tunable form alone; the tuner picks its configuration at the first launch.
+    // The tunable form and the standard kernels; the tuner picks among the
+    // tunable configurations and the standard kernel at the first launch.
     auto p = std::make_unique<Program>();
     p->kind = ir.kind;
-    p->gen = describe_program(ir);
-    p->gen.source = std::string("// generated by compute.scala_gb300 for sm_103a (tunable form)\n") + kPrelude + "\n" +
-                    tunable_source(ir, "");
-    std::vector<char> cubin = compile_cubin(p->gen.source, c.cc_major, c.cc_minor, c.flags);
+    const std::string tunable = std::string("// generated by compute.scala_gb300 for sm_103a (tunable form)\n") +
+                                kPrelude + "\n" + tunable_source(ir, "");
+    std::vector<char> cubin = compile_cubin(tunable, c.cc_major, c.cc_minor, c.flags);
     p->tune = std::make_unique<TuneEntry>();
     load_tune_entry(*p->tune, ir, load_tune_module(cubin), "");
+    p->mod = standard_module(c, ir, opt, key, &p->gen);
     std::lock_guard<std::recursive_mutex> g(c.mu);
     uint64_t h = c.make_handle(kTagProgram);
     c.programs[h] = p.release();
@@ -1490,62 +1576,9 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     *out = h;
     return CC_OK;
   }
-  int64_t domain = 1;
-  for (int64_t d : ir.out_shape) domain *= d;
-  // Contiguous programs compile once per structure; the shape only sizes the launch.
-  std::string skey = contiguous_structure_key(ir);
-  if (!skey.empty()) {
-    skey += key.substr(key.rfind('#'));
-    opt.min_blocks = 0;
-  } else {
-    // threads, not points: a thread of a multi-point kernel takes several
-    opt.min_blocks = choose_min_blocks(domain / points_for(ir, opt.points_per_thread), opt.block, c.sm_count,
-                                       -opt.min_blocks);
-  }
   auto p = std::make_unique<Program>();
   p->kind = ir.kind;
-  std::shared_ptr<Module> mod;
-  if (!skey.empty()) {
-    std::lock_guard<std::recursive_mutex> g(c.mu);
-    auto it = c.modules.find(skey);
-    if (it != c.modules.end()) mod = it->second;
-  }
-  if (mod) {
-    p->gen = describe_program(ir);
-  } else {
-    p->gen = generate_cuda(ir, opt);
-    mod = std::make_shared<Module>();
-    mod->source = p->gen.source;
-    std::vector<char> cubin = compile_cubin(mod->source, c.cc_major, c.cc_minor, c.flags);
-    check_cu(g_drv.ModuleLoadData(&mod->module, cubin.data()), "cuModuleLoadData");
-    const char *sname = ir.kind == ProgramKind::Sum ? "cc_sum" : "cc_ew";
-    const char *vname = ir.kind == ProgramKind::Sum ? "cc_sum_v4" : "cc_ew_v4";
-    check_cu(g_drv.ModuleGetFunction(&mod->scalar, mod->module, sname), "cuModuleGetFunction");
-    if (p->gen.has_vec4) check_cu(g_drv.ModuleGetFunction(&mod->vec4, mod->module, vname), "cuModuleGetFunction");
-    if (p->gen.has_vl)
-      check_cu(g_drv.ModuleGetFunction(&mod->vl, mod->module, ir.kind == ProgramKind::Sum ? "cc_sum_vl" : "cc_ew_vl"),
-               "cuModuleGetFunction");
-    mod->block = opt.block;
-    mod->vec_unroll = p->gen.vec_unroll;
-    mod->smem_bytes = p->gen.smem_bytes;
-    mod->points = p->gen.points_per_thread;
-    if (mod->smem_bytes > 48 * 1024)
-      check_cu(g_drv.FuncSetAttribute(mod->scalar, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, mod->smem_bytes),
-               "cuFuncSetAttribute");
-    check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_scalar, mod->scalar, mod->block, mod->smem_bytes),
-             "cuOccupancyMaxActiveBlocks");
-    if (mod->vec4)
-      check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_vec4, mod->vec4, mod->block, 0),
-               "cuOccupancyMaxActiveBlocks");
-    if (mod->vl)
-      check_cu(g_drv.OccupancyMaxActiveBlocks(&mod->resident_vl, mod->vl, mod->block, 0),
-               "cuOccupancyMaxActiveBlocks");
-    if (!skey.empty()) {
-      std::lock_guard<std::recursive_mutex> g(c.mu);
-      c.modules[skey] = mod;
-    }
-  }
-  p->mod = mod;
+  p->mod = standard_module(c, ir, opt, key, &p->gen);
   std::lock_guard<std::recursive_mutex> g(c.mu);
   uint64_t h = c.make_handle(kTagProgram);
   c.programs[h] = p.release();
@@ -2580,27 +2613,79 @@ void mlp_backward(Context &c, Mlp &m, const float *x, const float *t, int batch,
   }
 }
 
-int choose_exhaustive(Context &c, TuneEntry &e, const std::vector<uint64_t> &in, uint64_t out) {
+// Median device time (ms) of `reps` runs of launch() on the context stream,
+// after one untimed run; with a flush buffer, a write twice the size of L2
+// precedes every timed run.
+float time_launches(Context &c, const std::function<void()> &launch, int reps, void *flush, size_t flush_bytes) {
+  if (reps < 1) reps = 1;
+  cudaStream_t s = c.stream;
+  std::vector<cudaEvent_t> ev(2 * (size_t)reps, nullptr);
+  auto destroy = [&]() {
+    for (auto &x : ev)
+      if (x) cudaEventDestroy(x);
+  };
+  std::vector<float> t(reps);
+  try {
+    for (auto &x : ev) check_cuda(cudaEventCreate(&x), "cudaEventCreate");
+    launch();
+    for (int r = 0; r < reps; ++r) {
+      if (flush) check_cuda(cudaMemsetAsync(flush, r & 0xff, flush_bytes, s), "cudaMemsetAsync");
+      check_cuda(cudaEventRecord(ev[2 * r], s), "cudaEventRecord");
+      launch();
+      check_cuda(cudaEventRecord(ev[2 * r + 1], s), "cudaEventRecord");
+    }
+    wait_event_bounded(ev[2 * reps - 1], 60ull * 1000000000ull, "timing a launch");
+    for (int r = 0; r < reps; ++r) check_cuda(cudaEventElapsedTime(&t[r], ev[2 * r], ev[2 * r + 1]), "cudaEventElapsedTime");
+  } catch (...) {
+    destroy();
+    throw;
+  }
+  destroy();
+  std::sort(t.begin(), t.end());
+  return t[reps / 2];
+}
+
+// The standard generated kernel of a tuned program, timed like a configuration.
+float time_standard(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, int reps, void *flush,
+                    size_t flush_bytes) {
+  return time_launches(
+      c,
+      [&]() {
+        end_pdl_chain(c);
+        launch_generated(c, p, in, out, c.stream);
+      },
+      reps, flush, flush_bytes);
+}
+
+// Every configuration of the tunable form and the standard kernel, timed
+// (3 runs each after an L2 flush); the fastest is kept, so a tuned program is
+// never slower than the standard kernel it would otherwise run.
+int choose_exhaustive(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out) {
+  TuneEntry &e = *p.tune;
   std::vector<int> configs(kTuneConfigs);
   for (int i = 0; i < kTuneConfigs; ++i) configs[i] = i;
-  std::vector<float> ms(kTuneConfigs);
+  std::vector<float> ms(kTuneConfigs + 1);
   size_t cls = 0;
   void *flush = c.pool.alloc(kFlushBytes, &cls);
   try {
     time_tune_entry(c, e, configs.data(), kTuneConfigs, in, out, 3, flush, kFlushBytes, ms.data());
+    ms[kStdConfig] = time_standard(c, p, in, out, 3, flush, kFlushBytes);
   } catch (...) {
     release_block(c, flush, cls);
     throw;
   }
   release_block(c, flush, cls);
-  int best = -1;
+  int best = kStdConfig;
   for (int i = 0; i < kTuneConfigs; ++i)
-    if (ms[i] >= 0.0f && (best < 0 || ms[i] < ms[best])) best = i;
-  if (best < 0) fail(CC_ERR_INVALID_OPERATION, "no configuration applies to these buffers");
+    if (ms[i] >= 0.0f && ms[i] < ms[best]) best = i;
   return best;
 }
 
-int choose_learned(Context &c, TuneEntry &e, const std::vector<uint64_t> &in, uint64_t out) {
+// The cost model ranks the configurations of the tunable form; its first
+// choice and the standard kernel are then timed (3 runs each after an L2
+// flush) and the faster is kept.
+int choose_learned(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out) {
+  TuneEntry &e = *p.tune;
   if (!c.cost_model) fail(CC_ERR_INVALID_OPERATION, "the learned tuner needs a cost model (cc_tuner_set_model)");
   Mlp &m = mlp_of(c, c.cost_model);
   std::vector<float> x((size_t)kTuneConfigs * kFeatures);
@@ -2624,11 +2709,21 @@ int choose_learned(Context &c, TuneEntry &e, const std::vector<uint64_t> &in, ui
     throw;
   }
   release_block(c, dx, cls);
-  int best = -1;
+  int pick = -1;
   for (int i = 0; i < kTuneConfigs; ++i)
-    if (tune_config_fits(e, i, in, out) && (best < 0 || y[i] < y[best])) best = i;
-  if (best < 0) fail(CC_ERR_INVALID_OPERATION, "no configuration applies to these buffers");
-  return best;
+    if (tune_config_fits(e, i, in, out) && (pick < 0 || y[i] < y[pick])) pick = i;
+  if (pick < 0) return kStdConfig;
+  float t_pick = 0.0f, t_std = 0.0f;
+  void *flush = c.pool.alloc(kFlushBytes, &cls);
+  try {
+    time_tune_entry(c, e, &pick, 1, in, out, 3, flush, kFlushBytes, &t_pick);
+    t_std = time_standard(c, p, in, out, 3, flush, kFlushBytes);
+  } catch (...) {
+    release_block(c, flush, cls);
+    throw;
+  }
+  release_block(c, flush, cls);
+  return (t_pick >= 0.0f && t_pick < t_std) ? pick : kStdConfig;
 }
 
 TuneSet &tune_set_of(Context &c, uint64_t h) {
@@ -2685,11 +2780,14 @@ void load_tune_entry(TuneEntry &e, const Ir &ir, std::shared_ptr<TuneModule> mod
 
 void launch_tuned_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
   TuneEntry &e = *p.tune;
-  if (p.tuned_config < 0 || !tune_config_fits(e, p.tuned_config, in, out)) {
+  if (p.tuned_config < 0 || (p.tuned_config < kTuneConfigs && !tune_config_fits(e, p.tuned_config, in, out))) {
     if (stream != c.stream) check_cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
-    p.tuned_config = c.tuner == 2 ? choose_learned(c, e, in, out) : choose_exhaustive(c, e, in, out);
+    p.tuned_config = c.tuner == 2 ? choose_learned(c, p, in, out) : choose_exhaustive(c, p, in, out);
   }
-  launch_tune_entry(c, e, p.tuned_config, in, out, stream);
+  if (p.tuned_config == kStdConfig)
+    launch_generated(c, p, in, out, stream);
+  else
+    launch_tune_entry(c, e, p.tuned_config, in, out, stream);
 }
 
 }  // namespace

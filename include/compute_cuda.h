@@ -320,16 +320,21 @@ int cc_batch_compile_check(const char *const *irs, const size_t *ir_lens, int n_
  *      Elementwise results are identical in every configuration; sums differ
  *      in the order of their compensated partials.
  *      With the "tuner" knob at 1 (exhaustive), cc_program_get compiles the
- *      tunable form and the first launch times all configurations on its own
- *      buffers (3 launches each after an L2 flush) and keeps the fastest; at 2
- *      (learned) the cost model installed by cc_tuner_set_model predicts each
- *      configuration's log-runtime and the least is kept. -------------------- */
+ *      tunable form beside the standard kernels, and the first launch times
+ *      all configurations and the standard kernel on its own buffers (3
+ *      launches each after an L2 flush) and keeps the fastest; at 2 (learned)
+ *      the cost model installed by cc_tuner_set_model predicts each
+ *      configuration's log-runtime, and its first choice and the standard
+ *      kernel are timed the same way; the faster is kept. -------------------- */
 #define CC_TUNE_CONFIGS 48
 #define CC_FEATURES 64
 int cc_tune_config(int index, int *block, int *vec, int *ept, int *split);
 /* The cost model's features of (program, configuration) for a GPU of sm_count SMs: CC_FEATURES floats. */
 int cc_program_features(const char *ir, size_t ir_len, int config, int sm_count, float *out);
-/* The configuration the tuner chose for a program (-1: not launched yet or not tuned). */
+/* The configuration the tuner chose for a program (-1: not launched yet or not tuned;
+ * CC_TUNE_STANDARD: the program's standard generated kernel, which the tuner times beside
+ * the tunable configurations, so a tuned program is never slower than it). */
+#define CC_TUNE_STANDARD CC_TUNE_CONFIGS
 int cc_tuner_choice(cc_handle program, int *config);
 /* Installs network `mlp` (CC_FEATURES inputs, one output) as the learned tuner's
  * model; inputs are normalised as (feature - mean) * inv_std.  mlp = 0 removes it. */

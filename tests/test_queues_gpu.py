@@ -46,8 +46,8 @@ def test_computational_graph_of_cpu_spec():
 
 def _two_chains(dev, n, depth):
     T = dev.Tensor
-    x = T.random([n, 64], seed=31)
-    y = T.randomNormal([n, 64], seed=32)
+    x = T.random([n, 64], seed=31)  # uniform: the oracle's random numbers are the device's bits
+    y = T.random([n, 64], seed=32) - T.fill(0.5, [n, 64])
     cx, cy = x, y
     for k in range(depth):
         cx = (T.abs(cx) * T.fill(-1.5, [n, 64]) + T.fill(0.25, [n, 64])).nonInline()
@@ -64,10 +64,13 @@ def test_independent_chains_joined_by_wait_lists_match_the_oracle():
     different queues; the kernel that joins them waits for both.  Elementwise
     results are the oracle's bits; the final sum (on a queue, with that queue's
     own partials) is within sqrt(n) * 2^-24 of the oracle's."""
+    from conftest import cuda_tensors
     got_t, got_s = _two_chains(_queued(), 4096, 9)
     want_t, want_s = _two_chains(_oracle(), 4096, 9)
     g, w = got_t.flatArray(), want_t.flatArray()
     assert np.array_equal(g.view(np.int32), w.view(np.int32))
+    one_stream = _two_chains(cuda_tensors(), 4096, 9)[0].flatArray()
+    assert np.array_equal(g.view(np.int32), one_stream.view(np.int32))
     s_dev, s_ref = got_s.readScalar(), want_s.readScalar()
     n = 4096 * 64
     assert abs(s_dev - s_ref) <= np.sqrt(n) * 2.0 ** -24 * max(1.0, abs(s_ref)) * 4
@@ -133,46 +136,52 @@ def test_invalid_wait_handle_is_rejected_before_anything_is_enqueued():
 
 
 def test_chains_on_different_queues_overlap():
-    """40 small launches per chain (latency-bound): two independent chains take
-    about as long as one, while the same launches forced into one order by
-    their wait lists take about twice as long."""
+    """Two chains of launches ordered by their events, each launch a kernel
+    that occupies under half of the SMs and runs long (an inner-axis fold of
+    1024 terms of tanh(tanh(tanh(x))) per output, 4864 outputs: 76 blocks):
+    independent, the chains take about as long as one; forced into one order
+    by their wait lists, about twice as long."""
     from compute.tensors import NonInlineTensor
     d = _queued()
     rt = d.runtime
     T = d.Tensor
-    n = 1 << 12
-    p = NonInlineTensor(d, (n,), 0.0, None)
-    prog = rt.program(d.serialize((T.tanh(p) * T.fill(0.999, [n])).closure, (n,)).text)
-    bufs = [rt.alloc(4 * n) for _ in range(4)]
-    for b in bufs:
-        rt.upload(b, np.zeros(n, np.float32))
+    rows, cols = 76 * 64, 1024
+    p = NonInlineTensor(d, (rows, cols), 0.0, None)
+    fold = T.tanh(T.tanh(T.tanh(p))).split(1).reduce(lambda u, v: u + v)
+    prog = rt.program(d.serialize(fold.closure, fold.shape).text)
+    assert "cc_rowfold" in prog.source()
+    x = rt.alloc(4 * rows * cols)
+    rt.upload(x, np.random.RandomState(4).uniform(-1, 1, rows * cols).astype(np.float32))
+    outs = [rt.alloc(4 * rows) for _ in range(2)]
 
-    def run(independent):
+    def run(independent, launches=8):
         rt.synchronize()
         t0 = time.perf_counter()
         ea = eb = None
         evs = []
-        for k in range(40):
-            ea = rt.launch_ev(prog, [bufs[k % 2]], bufs[1 - k % 2], [ea] if ea else [])
+        for k in range(launches):
+            ea = rt.launch_ev(prog, [x], outs[0], [ea] if ea else [])
             wait_b = [eb] if eb else []
             if not independent:
                 wait_b.append(ea)
-            eb = rt.launch_ev(prog, [bufs[2 + k % 2]], bufs[3 - k % 2], wait_b)
+            eb = rt.launch_ev(prog, [x], outs[1], wait_b)
             evs += [ea, eb]
         rt.event_wait(ea, 60 * 10 ** 9)
         rt.event_wait(eb, 60 * 10 ** 9)
         dt = time.perf_counter() - t0
-        for e in evs:
-            rt.event_release(e)
+        for ev in evs:
+            rt.event_release(ev)
         return dt
 
     run(True)
     together = min(run(True) for _ in range(3))
     ordered = min(run(False) for _ in range(3))
     print("two independent chains %.3f ms, forced into one order %.3f ms" % (together * 1e3, ordered * 1e3))
-    assert together < ordered
-    for b in bufs:
-        b.release()
+    assert together < 0.8 * ordered
+    a, b = rt.download(outs[0], rows), rt.download(outs[1], rows)
+    assert np.array_equal(a.view(np.int32), b.view(np.int32))
+    for buf in outs + [x]:
+        buf.release()
 
 
 def test_released_buffers_wait_for_every_stream_that_used_them():

@@ -173,7 +173,7 @@ def test_runtime_tuner_modes(cuda_device):
                 rt.launch(prog, bufs, out)
                 got = rt.download(out, n_out)
                 choice = rt.tuner_choice(prog)
-                assert 0 <= choice < 48
+                assert 0 <= choice <= 48  # 48: the standard generated kernel won
                 if p["kind"] == "sum":
                     assert np.allclose(got, want, rtol=1e-5, equal_nan=True)
                 else:
@@ -200,7 +200,7 @@ def test_shipped_model_drives_the_learned_tuner(cuda_device):
             out = rt.alloc(max(1, n_out) * 4)
             prog = rt.program(p["ir"])
             rt.launch(prog, bufs, out)
-            assert 0 <= rt.tuner_choice(prog) < 48
+            assert 0 <= rt.tuner_choice(prog) <= 48
             rt.config_set("tuner", 0)
             ref = rt.alloc(max(1, n_out) * 4)
             rt.launch(rt.program(p["ir"]), bufs, ref)
@@ -215,3 +215,44 @@ def test_shipped_model_drives_the_learned_tuner(cuda_device):
     finally:
         rt.config_set("tuner", 0)
         model.close()
+
+
+def test_the_tuned_choice_is_never_slower_than_the_standard_kernel(cuda_device):
+    """The tuner times the standard generated kernel beside the tunable form's
+    configurations (exhaustive: all 48; learned: the model's first choice), so
+    the kernel a tuned program runs is at most as slow as the standard one, up
+    to timing noise."""
+    rt = cuda_device.runtime
+    progs = tuner.random_programs(6, seed=23, max_points=1 << 22)
+    try:
+        for k, p in enumerate(progs):
+            _, bufs = _inputs(rt, p, k)
+            n_out = 1 if p["kind"] == "sum" else p["points"]
+            out = rt.alloc(max(1, n_out) * 4)
+            std = rt.program(p["ir"])
+            rt.config_set("tuner", 1)
+            tuned = rt.program(p["ir"])
+            rt.launch(tuned, bufs, out)
+            choice = rt.tuner_choice(tuned)
+            rt.config_set("tuner", 0)
+            assert 0 <= choice <= 48
+
+            def median_ms(prog):
+                times = []
+                for _ in range(7):
+                    rt.synchronize()
+                    e0 = rt.event()
+                    rt.launch(prog, bufs, out)
+                    e1 = rt.event()
+                    rt.event_wait(e1)
+                    times.append(rt.event_elapsed_ms(e0, e1))
+                    rt.event_release(e0)
+                    rt.event_release(e1)
+                return sorted(times)[3]
+
+            t_std, t_tuned = median_ms(std), median_ms(tuned)
+            assert t_tuned <= 1.25 * t_std + 0.003, (k, choice, t_tuned, t_std)
+            for b in bufs + [out]:
+                b.release()
+    finally:
+        rt.config_set("tuner", 0)
