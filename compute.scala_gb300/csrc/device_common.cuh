@@ -120,27 +120,23 @@ __device__ __forceinline__ void cc_pdl_gate(int &early) {
   }
 }
 
-// The grid sum's finish in generated kernels launched with programmatic
-// dependent launch.  The partials and the completion counter are the launch's
-// own (the runtime alternates two scratch blocks between consecutive sums on
-// its stream), so only the last block, before it writes `out`, waits for the
-// previous kernel (`early` = 1; with early = 0 the kernel waited at entry):
-// the other blocks publish their partials and leave without waiting, and
-// consecutive sums overlap everything but their final stores.  One block needs
-// no partials at all.  Thread 0's partial store is ordered before its ticket
-// by the atomic's release; the last block's thread 0 acquires every partial
-// through its own ticket and the barrier passes that on to the block.
+// The grid sum's finish in generated kernels (launched with programmatic
+// dependent launch): every block first waits for the previous kernel when it
+// started early (cc_pdl_gate: the partials, the counter and `out` may still be
+// the previous sum's), then publishes its partial.  Thread 0 orders its
+// partial before its ticket with the atomic's release semantics, and the last
+// block's thread 0 acquires every partial through its own ticket; the barrier
+// passes that on to the block (no separate fences).  One block needs no
+// partials at all.
 __device__ __forceinline__ void cc_grid_finish_pdl(float s, float c, float2 *__restrict__ partials,
                                                    unsigned int *__restrict__ counter, float *__restrict__ out,
                                                    int early) {
   __shared__ float2 ws[32];
   __shared__ int last;
+  cc_pdl_gate(early);
   cc_block_merge(s, c, ws);
   if (gridDim.x == 1) {
-    if (threadIdx.x == 0) {
-      if (early) cc_pdl_wait_then_release();
-      out[0] = isfinite(s) ? __fadd_rn(s, c) : s;
-    }
+    if (threadIdx.x == 0) out[0] = isfinite(s) ? __fadd_rn(s, c) : s;
     return;
   }
   if (threadIdx.x == 0) {
@@ -159,7 +155,6 @@ __device__ __forceinline__ void cc_grid_finish_pdl(float s, float c, float2 *__r
   }
   cc_block_merge(s, c, ws);
   if (threadIdx.x == 0) {
-    if (early) cc_pdl_wait_then_release();
     out[0] = isfinite(s) ? __fadd_rn(s, c) : s;
     *counter = 0u;
   }

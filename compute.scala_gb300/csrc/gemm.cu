@@ -165,12 +165,15 @@ __global__ void __launch_bounds__(256) split_planes_kernel(const float *__restri
 
 // Transposing split through shared memory: a 64 (k) x 64 (n) tile of src
 // (rows = K, cols = N, row-major) becomes a 64 x 64 tile of the planes (rows =
-// N, cols = K).  Loads are 16-byte reads along n (when src allows), stores
-// two 16-byte words per plane, 16 consecutive k of one n per thread.
+// N, cols = K).  Loads are 16-byte reads along n (when src allows); in the
+// store phase eight threads share one n, each splitting eight consecutive k
+// into one 16-byte word per plane, so a warp writes four whole 128-byte plane
+// rows per store.  The odd row pitch keeps the column reads at most two-way
+// bank conflicted.
 __global__ void __launch_bounds__(256) split_planes_t_kernel(const float *__restrict__ src, long long ld, int krows,
                                                              int ncols, int vec, __nv_bfloat16 *__restrict__ dst,
                                                              int prows, int pcols) {
-  __shared__ __align__(16) float tile[64][68];
+  __shared__ float tile[64][65];
   const long long plane = (long long)prows * pcols;
   const int k0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
   const int t = threadIdx.x;
@@ -189,28 +192,28 @@ __global__ void __launch_bounds__(256) split_planes_t_kernel(const float *__rest
       v.z = (k < krows && n + 2 < ncols) ? __ldg(p + n + 2) : 0.0f;
       v.w = (k < krows && n + 3 < ncols) ? __ldg(p + n + 3) : 0.0f;
     }
-    *reinterpret_cast<float4 *>(&tile[kr][lc]) = v;
+    tile[kr][lc + 0] = v.x;
+    tile[kr][lc + 1] = v.y;
+    tile[kr][lc + 2] = v.z;
+    tile[kr][lc + 3] = v.w;
   }
   __syncthreads();
-  const int nl = t & 63, kc = (t >> 6) * 16;  // a warp: 32 consecutive n, one run of 16 k
-  const int n = n0 + nl, k = k0 + kc;
-  if (n >= prows || k >= pcols) return;
-  float x[8], y[8];
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    x[e] = tile[kc + e][nl];
-    y[e] = tile[kc + 8 + e][nl];
+  for (int r = 0; r < 2; ++r) {
+    const int u = t + 256 * r;
+    const int nl = u >> 3, kc = (u & 7) * 8;
+    const int n = n0 + nl, k = k0 + kc;
+    if (n >= prows || k >= pcols) continue;
+    float x[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) x[e] = tile[kc + e][nl];
+    uint4 h, m, l;
+    split8(x, h, m, l);
+    const long long o = (long long)n * pcols + k;
+    *reinterpret_cast<uint4 *>(dst + o) = h;
+    *reinterpret_cast<uint4 *>(dst + plane + o) = m;
+    *reinterpret_cast<uint4 *>(dst + 2 * plane + o) = l;
   }
-  uint4 h0, m0, l0, h1, m1, l1;
-  split8(x, h0, m0, l0);
-  split8(y, h1, m1, l1);
-  const long long o = (long long)n * pcols + k;
-  uint4 *d0 = reinterpret_cast<uint4 *>(dst + o);
-  uint4 *d1 = reinterpret_cast<uint4 *>(dst + plane + o);
-  uint4 *d2 = reinterpret_cast<uint4 *>(dst + 2 * plane + o);
-  d0[0] = h0; d0[1] = h1;
-  d1[0] = m0; d1[1] = m1;
-  d2[0] = l0; d2[1] = l1;
 }
 
 }  // namespace

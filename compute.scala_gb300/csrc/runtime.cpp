@@ -421,12 +421,7 @@ struct Context {
   // Scratch of the grid sums: kMaxSumBlocks float2 partials, then the counter.
   void *sum_scratch = nullptr;
   size_t sum_scratch_cls = 0;
-  // A second block that consecutive sums on the context stream alternate with:
-  // a generated sum's blocks publish their partials without waiting for the
-  // previous kernel, which may be the previous sum.
-  void *sum_scratch_alt = nullptr;
-  size_t sum_scratch_alt_cls = 0;
-  int sum_parity = 0;
+
 
   uint64_t make_handle(uint64_t tag) { return (tag << 56) | (next_id++); }
   // Device error flag of the kernels with bounded waits (in the same scratch block).
@@ -537,10 +532,7 @@ void release_block(Context &c, void *p, size_t cls) {
 // then set and the caller releases it after synchronising the stream.
 void *sum_scratch_for(Context &c, cudaStream_t s, size_t *temporary_cls) {
   *temporary_cls = 0;
-  if (s == c.stream) {
-    c.sum_parity ^= 1;
-    return c.sum_parity ? c.sum_scratch_alt : c.sum_scratch;
-  }
+  if (s == c.stream) return c.sum_scratch;
   const int q = queue_index(c, s);
   if (q >= 0) return c.queue_scratch[q];
   size_t cls = 0;
@@ -975,9 +967,6 @@ int cc_init(int device_ordinal, uint32_t flags) {
   c->stream = c->own_stream;
   c->sum_scratch = c->pool.alloc(sizeof(float2) * kMaxSumBlocks + 256, &c->sum_scratch_cls);
   check_cuda(cudaMemsetAsync(c->sum_scratch, 0, sizeof(float2) * kMaxSumBlocks + 256, c->stream), "cudaMemsetAsync");
-  c->sum_scratch_alt = c->pool.alloc(sizeof(float2) * kMaxSumBlocks + 256, &c->sum_scratch_alt_cls);
-  check_cuda(cudaMemsetAsync(c->sum_scratch_alt, 0, sizeof(float2) * kMaxSumBlocks + 256, c->stream),
-             "cudaMemsetAsync");
   check_cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
   g_ctx = c.release();
   CC_API_END
@@ -1027,7 +1016,6 @@ int cc_shutdown(void) {
   }
   c->events.clear();
   release_block(*c, c->sum_scratch, c->sum_scratch_cls);
-  release_block(*c, c->sum_scratch_alt, c->sum_scratch_alt_cls);
   for (int i = 0; i < kQueues; ++i)
     if (c->queue_scratch[i]) release_block(*c, c->queue_scratch[i], c->queue_scratch_cls[i]);
   c->pool.trim();

@@ -136,31 +136,33 @@ def test_invalid_wait_handle_is_rejected_before_anything_is_enqueued():
 
 
 def test_chains_on_different_queues_overlap():
-    """Two chains of launches ordered by their events, each launch a kernel
-    that occupies under half of the SMs and runs long (an inner-axis fold of
-    1024 terms of tanh(tanh(tanh(x))) per output, 4864 outputs: 76 blocks):
-    independent, the chains take about as long as one; forced into one order
-    by their wait lists, about twice as long."""
+    """Two chains of launches ordered by their events, each launch a kernel of
+    one block that runs long (an inner-axis fold of 4096 terms of tanh(x) per
+    output, 64 outputs): independent, the chains take about as long as one;
+    forced into one order by their wait lists, about twice as long."""
     from compute.tensors import NonInlineTensor
     d = _queued()
     rt = d.runtime
     T = d.Tensor
-    rows, cols = 76 * 64, 1024
+    rows, cols = 64, 4096
     p = NonInlineTensor(d, (rows, cols), 0.0, None)
-    fold = T.tanh(T.tanh(T.tanh(p))).split(1).reduce(lambda u, v: u + v)
+    fold = T.tanh(p).split(1).reduce(lambda u, v: u + v)
     prog = rt.program(d.serialize(fold.closure, fold.shape).text)
     assert "cc_rowfold" in prog.source()
     x = rt.alloc(4 * rows * cols)
     rt.upload(x, np.random.RandomState(4).uniform(-1, 1, rows * cols).astype(np.float32))
     outs = [rt.alloc(4 * rows) for _ in range(2)]
 
-    def run(independent, launches=8):
+    def run(independent, launches=6):
         rt.synchronize()
         t0 = time.perf_counter()
         ea = eb = None
         evs = []
         for k in range(launches):
-            ea = rt.launch_ev(prog, [x], outs[0], [ea] if ea else [])
+            wait_a = [ea] if ea else []
+            if not independent and eb:
+                wait_a.append(eb)  # one order: a0, b0, a1, b1, ...
+            ea = rt.launch_ev(prog, [x], outs[0], wait_a)
             wait_b = [eb] if eb else []
             if not independent:
                 wait_b.append(ea)

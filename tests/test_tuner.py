@@ -125,3 +125,36 @@ def test_shipped_cost_model_file():
     n = sum(k * m + m for k, m in zip(tuner.MODEL_DIMS[:-1], tuner.MODEL_DIMS[1:]))
     assert z["params"].shape == (n,) and np.all(np.isfinite(z["params"]))
     assert z["mean"].shape == (64,) and z["inv_std"].shape == (64,)
+
+
+def test_evaluation_against_the_standard_kernel():
+    """With the standard generated kernel's time in each record, the learned
+    tuner's result is the faster of the model's first choice and that kernel
+    (what the runtime keeps), compared with the standard kernel and with the
+    fastest of the 48 configurations and the standard kernel."""
+    progs = tuner.random_programs(4, seed=9)
+    recs = []
+    for k, p in enumerate(progs):
+        rec = dict(p)
+        ms = np.full(48, 2.0)
+        ms[5] = 1.0           # the fastest configuration
+        rec["ms"] = list(ms)
+        rec["std_ms"] = [1.5, 0.5, 2.0, 4.0][k]  # the standard kernel: slower, faster, equal, slower
+        recs.append(rec)
+
+    class PicksConfigZero:
+        def predict(self, x):
+            out = np.ones(x.shape[0], dtype=np.float32)
+            out[::48] = 0.0  # configuration 0 of every program (2.0 ms)
+            return out
+
+    res = tuner.evaluate(PicksConfigZero(), recs, 152)
+    v = res["vs_standard_kernel"]
+    tuned = np.array([1.5, 0.5, 2.0, 2.0])
+    std = np.array([1.5, 0.5, 2.0, 4.0])
+    best = np.array([1.0, 0.5, 1.0, 1.0])
+    assert v["learned_speedup_total"] == pytest.approx(std.sum() / tuned.sum())
+    assert v["learned_speedup_geomean"] == pytest.approx(np.exp(np.mean(np.log(std / tuned))))
+    assert v["exhaustive_speedup_total"] == pytest.approx(std.sum() / best.sum())
+    assert v["learned_regret_vs_exhaustive_geomean"] == pytest.approx(np.exp(np.mean(np.log(tuned / best))) - 1)
+    assert v["standard_wins"] == 3
