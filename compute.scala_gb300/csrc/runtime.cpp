@@ -727,9 +727,24 @@ void launch_row_fold(Context &c, Program &p, const std::vector<uint64_t> &in, ui
   args.push_back(&cols);
   args.push_back(&err);
   const unsigned grid = (unsigned)((rf.rows + kRowFoldRows - 1) / kRowFoldRows);
-  check_cu(g_drv.LaunchKernel(aligned ? p.rf_tma : p.rf_plain, grid, 1, 1, kRowFoldRows, 1, 1,
-                              aligned ? (unsigned)row_fold_smem_bytes(nin) : 0u, (CUstream)stream, args.data(), nullptr),
-           "cuLaunchKernel");
+  // With programmatic dependent launch the block set-up (barrier
+  // initialisation) overlaps the previous kernel's tail; every block waits
+  // (griddepcontrol.wait) before its first load.
+  CUlaunchAttribute attr;
+  memset(&attr, 0, sizeof attr);
+  attr.id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
+  attr.value.programmaticStreamSerializationAllowed = 1;
+  CUlaunchConfig cfg;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.gridDimX = grid;
+  cfg.gridDimY = cfg.gridDimZ = 1;
+  cfg.blockDimX = (unsigned)kRowFoldRows;
+  cfg.blockDimY = cfg.blockDimZ = 1;
+  cfg.sharedMemBytes = aligned ? (unsigned)row_fold_smem_bytes(nin) : 0u;
+  cfg.hStream = (CUstream)stream;
+  cfg.attrs = &attr;
+  cfg.numAttrs = c.pdl ? 1 : 0;
+  check_cu(g_drv.LaunchKernelEx(&cfg, aligned ? p.rf_tma : p.rf_plain, args.data(), nullptr), "cuLaunchKernelEx");
 }
 
 void launch_generated(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream);
