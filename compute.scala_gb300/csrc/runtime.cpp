@@ -385,8 +385,8 @@ struct Context {
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
   int row_fold = 1;     // inner-axis folds of at least kRowFoldMinTerms terms: 1 = TMA-staged skeleton
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
-  int batch_max_registers = 128;  // two 256-thread blocks per SM for the persistent kernel
-  int batch_run_tiles = 16;       // tiles a persistent block claims at once
+  int batch_max_registers = 64;   // four 256-thread blocks per SM for the persistent kernel
+  int batch_run_tiles = 4;        // tiles a persistent block claims at once
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int ew_points = 1;     // generic elementwise kernels: consecutive points per thread

@@ -123,10 +123,10 @@ int cc_synchronize(void);
  *   "tuner"             0 = generated kernels with the fixed launch shape (default), 1 = exhaustive
  *                       tuner, 2 = learned tuner (see the tuner section)
  *   "batch_max_registers" batch modules: register cap per thread of every compiled part (0 = none;
- *                       default 128: the indirect calls of the persistent kernel otherwise take the
- *                       largest part's registers and one block per SM)
+ *                       default 64: four blocks per SM; the indirect calls of the persistent kernel
+ *                       otherwise take the largest part's registers and one block per SM)
  *   "batch_run_tiles"   consecutive 4096-float tiles a block of the persistent batch kernel claims at once
- *                       (default 16)
+ *                       (default 4)
  *   "batch_inline"      batch modules: 0 = expressions and exp/log/tanh are called functions,
  *                       1 = expressions inlined, exp/log/tanh called (default), 2 = all inlined
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
