@@ -1015,13 +1015,14 @@ bool match_row_fold(const Ir &ir, RowFold *out, std::string *why) {
   return true;
 }
 
-int row_fold_stages(int row_inputs) {
+int row_fold_stages(int row_inputs, int requested) {
   const int per_stage = row_inputs * kRowFoldRows * 128;
+  if (requested >= 2 && requested <= 16 && requested * per_stage + 1024 <= 200 * 1024) return requested;
   int s = (96 * 1024) / (per_stage > 0 ? per_stage : 1);
   return s < 2 ? 2 : s > 8 ? 8 : s;
 }
 
-int row_fold_smem_bytes(int row_inputs) { return row_fold_stages(row_inputs) * row_inputs * kRowFoldRows * 128 + 1024; }
+int row_fold_smem_bytes(int row_inputs, int stages) { return stages * row_inputs * kRowFoldRows * 128 + 1024; }
 
 std::string row_fold_source(const Ir &ir, const RowFold &rf) {
   Generator gen(ir, true, false, -1, false);
@@ -1029,7 +1030,7 @@ std::string row_fold_source(const Ir &ir, const RowFold &rf) {
   Frame f0{0, {}, rf.term_frame};
   const std::string r = gen.gen(rf.term, f0);
   gen.emit(body, 2, 0);
-  const int n = ir.n_params, nin = (int)rf.row_inputs.size(), S = row_fold_stages(nin);
+  const int n = ir.n_params, nin = (int)rf.row_inputs.size(), S = row_fold_stages(nin, rf.stages);
   std::vector<int> slot(n, -1);  // parameter -> row-input slot
   for (int i = 0; i < nin; ++i) slot[rf.row_inputs[i]] = i;
   std::ostringstream o;
@@ -1666,6 +1667,9 @@ std::string tunable_source(const Ir &ir, const std::string &suffix) {
         << (sum ? "float2 *__restrict__ partials, unsigned int *__restrict__ counter, float *__restrict__ out"
                 : "float *__restrict__ out")
         << ", cc_i64 n) {\n";
+      // launched with programmatic dependent launch: wait for the previous kernel
+      // before any memory access (a no-op without the launch attribute)
+      o << "  cc_pdl_wait_then_release();\n";
       if (sum) o << "  float s_ = 0.0f, c_ = 0.0f;\n";
       o << "  const cc_i64 stride = (cc_i64)gridDim.x * blockDim.x;\n"
         << "  const cc_i64 tid = (cc_i64)blockIdx.x * blockDim.x + threadIdx.x;\n";

@@ -171,6 +171,7 @@ struct RowFold {
   int64_t rows = 0, cols = 0;     // outputs, and J
   std::vector<int> row_inputs;    // parameter indices read as rows, in order
   std::vector<bool> is_row;       // per parameter: a row input (else a column input)
+  int stages = 0;                 // shared-memory ring stages (row_fold_stages)
 };
 // Terms below this count stay on the generic fold (a short fold is cheap to unroll).
 constexpr int64_t kRowFoldMinTerms = 32;
@@ -178,10 +179,11 @@ constexpr int kRowFoldRows = 64;       // outputs (threads) per block
 constexpr int kRowFoldMaxInputs = 4;   // row inputs staged per tile
 constexpr int kRowFoldWaitCode = 31;   // device error code: a tile's barrier wait ran out
 bool match_row_fold(const Ir &ir, RowFold *out, std::string *why = nullptr);
-// Stages of the shared-memory ring for `row_inputs` staged inputs.
-int row_fold_stages(int row_inputs);
+// Stages of the shared-memory ring for `row_inputs` staged inputs: `requested`
+// (1..16) if it fits, else as many 8 KiB tiles as fit in 96 KiB, 2 to 8.
+int row_fold_stages(int row_inputs, int requested = 0);
 // Dynamic shared memory of cc_rowfold (ring + alignment slack).
-int row_fold_smem_bytes(int row_inputs);
+int row_fold_smem_bytes(int row_inputs, int stages);
 // Kernels cc_rowfold (TMA-staged tiles) and cc_rowfold_plain (direct loads,
 // for row inputs that are not 16-byte aligned), with the prelude.
 std::string row_fold_source(const Ir &ir, const RowFold &rf);

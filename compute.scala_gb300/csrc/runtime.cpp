@@ -384,6 +384,7 @@ struct Context {
   int tc_variant = 5;  // 128x256 tiles, hi*hi restarted every 256 of K
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
   int row_fold = 1;     // inner-axis folds of at least kRowFoldMinTerms terms: 1 = TMA-staged skeleton
+  int row_fold_stages = 0;  // its ring stages (0 = as many 8 KiB tiles as fit 96 KiB, at most 8)
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
   int batch_max_registers = 64;   // four 256-thread blocks per SM for the persistent kernel
   int batch_run_tiles = 4;        // tiles a persistent block claims at once
@@ -740,7 +741,7 @@ void launch_row_fold(Context &c, Program &p, const std::vector<uint64_t> &in, ui
   cfg.gridDimY = cfg.gridDimZ = 1;
   cfg.blockDimX = (unsigned)kRowFoldRows;
   cfg.blockDimY = cfg.blockDimZ = 1;
-  cfg.sharedMemBytes = aligned ? (unsigned)row_fold_smem_bytes(nin) : 0u;
+  cfg.sharedMemBytes = aligned ? (unsigned)row_fold_smem_bytes(nin, row_fold_stages(nin, rf.stages)) : 0u;
   cfg.hStream = (CUstream)stream;
   cfg.attrs = &attr;
   cfg.numAttrs = c.pdl ? 1 : 0;
@@ -750,7 +751,7 @@ void launch_row_fold(Context &c, Program &p, const std::vector<uint64_t> &in, ui
 void launch_generated(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream);
 
 void launch_program(Context &c, Program &p, const std::vector<uint64_t> &in, uint64_t out, cudaStream_t stream) {
-  if (p.tune || p.is_contraction || p.is_row_fold) end_pdl_chain(c);
+  if (p.is_contraction || p.is_row_fold) end_pdl_chain(c);
   if (p.is_row_fold) {
     launch_row_fold(c, p, in, out, stream);
     return;
@@ -1136,6 +1137,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "batch_inline") {
     if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "batch_inline must be 0, 1 or 2");
     c.batch_inline = (int)value;
+  } else if (k == "row_fold_stages") {
+    if (value != 0 && (value < 2 || value > 16)) fail(CC_ERR_INVALID_VALUE, "row_fold_stages must be 0 or in [2, 16]");
+    c.row_fold_stages = (int)value;
   } else if (k == "row_fold") {
     if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "row_fold must be 0 or 1");
     c.row_fold = (int)value;
@@ -1175,6 +1179,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "tc_variant") *value = c.tc_variant;
   else if (k == "contraction") *value = c.contraction;
   else if (k == "row_fold") *value = c.row_fold;
+  else if (k == "row_fold_stages") *value = c.row_fold_stages;
   else if (k == "batch_inline") *value = c.batch_inline;
   else if (k == "tuner") *value = c.tuner;
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
@@ -1475,7 +1480,7 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
          " blocks " + std::to_string(-opt.min_blocks) + " block " + std::to_string(opt.block) + " unroll " + std::to_string(opt.vec_unroll) +
          " prefetch " + std::to_string(opt.prefetch_min_bytes) + " ring " + std::to_string(opt.smem_ring) + " points " + std::to_string(opt.points_per_thread) + " vl " + std::to_string((int)opt.vector_loads) + " bl " + std::to_string((int)opt.batch_loads) +
          " sumblock " + std::to_string(c.sum_block) +
-         " contraction " + std::to_string(c.contraction) + " rowfold " + std::to_string(c.row_fold) +
+         " contraction " + std::to_string(c.contraction) + " rowfold " + std::to_string(c.row_fold) + "/" + std::to_string(c.row_fold_stages) +
          " tc " + std::to_string(c.tc_variant) + " tuner " +
          std::to_string(c.tuner) + " flags " + std::to_string(c.flags) + "\n";
   {
@@ -1532,6 +1537,10 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
   }
   RowFold rf;
   if (row_fold_knob && match_row_fold(ir, &rf)) {
+    {
+      std::lock_guard<std::recursive_mutex> g(c.mu);
+      rf.stages = c.row_fold_stages;
+    }
     auto p = std::make_unique<Program>();
     p->kind = ProgramKind::Elementwise;
     p->gen = describe_program(ir);
@@ -1544,7 +1553,8 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     check_cu(g_drv.ModuleGetFunction(&p->rf_tma, mod->module, "cc_rowfold"), "cuModuleGetFunction");
     check_cu(g_drv.ModuleGetFunction(&p->rf_plain, mod->module, "cc_rowfold_plain"), "cuModuleGetFunction");
     check_cu(g_drv.FuncSetAttribute(p->rf_tma, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
-                                    row_fold_smem_bytes((int)rf.row_inputs.size())),
+                                    row_fold_smem_bytes((int)rf.row_inputs.size(),
+                                                        row_fold_stages((int)rf.row_inputs.size(), rf.stages))),
              "cuFuncSetAttribute");
     p->mod = mod;
     std::lock_guard<std::recursive_mutex> g(c.mu);
@@ -2494,7 +2504,21 @@ void launch_tune_entry(Context &c, TuneEntry &e, int config, const std::vector<u
   }
   args.push_back(&o);
   args.push_back(&n);
-  CUresult r = g_drv.LaunchKernel(e.fn[k], (unsigned)grid, 1, 1, t.block, 1, 1, 0, (CUstream)s, args.data(), nullptr);
+  // programmatic dependent launch (the tunable kernels wait at entry)
+  CUlaunchAttribute attr;
+  memset(&attr, 0, sizeof attr);
+  attr.id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
+  attr.value.programmaticStreamSerializationAllowed = 1;
+  CUlaunchConfig cfg;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.gridDimX = (unsigned)grid;
+  cfg.gridDimY = cfg.gridDimZ = 1;
+  cfg.blockDimX = (unsigned)t.block;
+  cfg.blockDimY = cfg.blockDimZ = 1;
+  cfg.hStream = (CUstream)s;
+  cfg.attrs = &attr;
+  cfg.numAttrs = c.pdl ? 1 : 0;
+  CUresult r = g_drv.LaunchKernelEx(&cfg, e.fn[k], args.data(), nullptr);
   if (temporary) {
     cudaError_t se = r == CUDA_SUCCESS ? cudaStreamSynchronize(s) : cudaSuccess;
     c.pool.release(scratch, temporary);
@@ -2785,12 +2809,16 @@ void launch_tuned_program(Context &c, Program &p, const std::vector<uint64_t> &i
   TuneEntry &e = *p.tune;
   if (p.tuned_config < 0 || (p.tuned_config < kTuneConfigs && !tune_config_fits(e, p.tuned_config, in, out))) {
     if (stream != c.stream) check_cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    end_pdl_chain(c);
     p.tuned_config = c.tuner == 2 ? choose_learned(c, p, in, out) : choose_exhaustive(c, p, in, out);
+    end_pdl_chain(c);
   }
-  if (p.tuned_config == kStdConfig)
-    launch_generated(c, p, in, out, stream);
-  else
+  if (p.tuned_config == kStdConfig) {
+    launch_generated(c, p, in, out, stream);  // keeps the early-start chain going
+  } else {
+    end_pdl_chain(c);
     launch_tune_entry(c, e, p.tuned_config, in, out, stream);
+  }
 }
 
 }  // namespace

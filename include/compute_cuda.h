@@ -91,6 +91,8 @@ int cc_synchronize(void);
  *                       inputs at j and literals, runs as a skeleton that stages tiles of those inputs in
  *                       shared memory by TMA and folds each output's terms in order (bit-identical to the
  *                       generated fold); 0 = the generated fold
+ *   "row_fold_stages"   that skeleton's ring of 8 KiB tiles per staged input (2..16; 0 = as many as fit
+ *                       96 KiB, at most 8; default 0)
  *   "contraction"       how a program that is the library's matmul idiom runs (a left fold over j
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
