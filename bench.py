@@ -639,10 +639,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-clocks", action="store_true", help="skip the clock sampling (and its untimed busy loop)")
-    ap.add_argument("--tuner", default="off", choices=["off", "exhaustive", "learned"],
-                    help="launch configurations: the standard kernels (off), every configuration timed at the "
-                         "first launch (exhaustive), or the shipped cost model's choice timed against the "
-                         "standard kernel (learned)")
+    ap.add_argument("--tuner", default="learned", choices=["off", "exhaustive", "learned"],
+                    help="launch configurations (the device object's setting): the shipped cost model's choice "
+                         "timed against the standard kernel at a program's first launch (learned, the default), "
+                         "every configuration timed (exhaustive), or the standard kernels (off)")
     ap.add_argument("--no-workloads", action="store_true",
                     help="default workload only: skip the records of the other configurations")
     ap.add_argument("--c5-eval-programs", type=int, default=400,
@@ -683,10 +683,9 @@ def main():
         dist = dist_mod
 
     from compute import Tensors
-    d = Tensors(device=local_rank)
+    d = Tensors(device=local_rank, tuner=args.tuner)
     rt = d.runtime
     apply_knobs(rt, args.knob)
-    model = use_tuner(rt, args.tuner)
     if args.workload == "c1":
         C1["n"] = C1["m"] = args.c1_side
     if args.workload == "c2":
@@ -696,26 +695,11 @@ def main():
                          clocks_on=not args.no_clocks)
     if rank == 0 and world == 1 and args.workload == "c2" and not args.no_workloads:
         line["workloads"] = measure_all_configs(d, args, warmup, local_rank)
-    if args.tuner != "off":
-        line["config"]["tuner"] = args.tuner
+    line["config"]["tuner"] = args.tuner
     if rank == 0:
         emit(line)
-    if model is not None:
-        model.close()
     if dist:
         dist.destroy_process_group()
-
-
-def use_tuner(rt, mode):
-    """Turns the runtime's tuner on ("exhaustive", "learned": the shipped cost
-    model) or leaves the standard kernels ("off"); returns the model to keep."""
-    if mode == "off":
-        return None
-    if mode == "exhaustive":
-        rt.config_set("tuner", 1)
-        return None
-    from compute import tuner
-    return tuner.use_learned_tuner(rt)
 
 
 def measure_fused(d, workload, steps, warmup, rank=0, world=1, local_rank=0, dist=None, e2e_on=True, cpu_on=True,
@@ -1033,7 +1017,7 @@ def measure_batch(d, programs, max_len, steps, warmup, local_rank=0, e2e_on=True
 
 def main_batch(args, warmup, rank, world, local_rank):
     from compute import Tensors
-    d = Tensors(device=local_rank)
+    d = Tensors(device=local_rank, tuner=args.tuner)
     apply_knobs(d.runtime, args.knob)
     line = measure_batch(d, args.programs, args.max_len, args.steps, warmup, local_rank=local_rank,
                          e2e_on=not args.no_e2e, cpu_on=not args.no_cpu_baseline, clocks_on=not args.no_clocks,
@@ -1118,7 +1102,7 @@ def main_contraction(args, warmup, rank, world, local_rank):
         emit(line)
         return
     from compute import Tensors
-    d = Tensors(device=local_rank)
+    d = Tensors(device=local_rank, tuner=args.tuner)
     apply_knobs(d.runtime, args.knob)
     line = measure_contraction(d, args.workload, args.steps, warmup, local_rank=local_rank, e2e_on=not args.no_e2e,
                                cpu_on=not args.no_cpu_baseline, clocks_on=not args.no_clocks, world=world)

@@ -30,6 +30,7 @@ order, and intermediate buffers go back to the pool when the action ends.
 from __future__ import annotations
 
 import functools
+import os
 from typing import Dict, List, Optional, Sequence
 
 import numpy as np
@@ -605,9 +606,17 @@ class Tensors:
     """
 
     def __init__(self, device: int = 0, flags: int = 0, planner: Optional[trees.Planner] = None, runtime=None,
-                 queues: bool = False):
+                 queues: bool = False, tuner: str = "learned"):
         self.device_ordinal = device
         self.flags = flags
+        # launch configurations of the native runtime's programs: "learned" (the shipped
+        # cost model's choice, timed against the standard kernel at a program's first
+        # launch; the faster is kept), "exhaustive" (every configuration timed) or "off"
+        # (the standard kernels); programs of more than 64 nodes are never tuned
+        if tuner not in ("learned", "exhaustive", "off"):
+            raise IllegalArgumentException("tuner must be 'learned', 'exhaustive' or 'off'")
+        self.tuner = tuner
+        self._cost_model = None
         # queues=True: every kernel of an action goes to the runtime's queue pool and
         # waits only for the events of the buffers it reads, as the reference's
         # CompiledKernel.run enqueues with its inputs' events (Tensors.scala:1331-1381);
@@ -621,7 +630,16 @@ class Tensors:
     def runtime(self):
         if self._runtime is None:
             from .runtime import NativeRuntime
-            self._runtime = NativeRuntime(self.device_ordinal, self.flags)
+            rt = NativeRuntime(self.device_ordinal, self.flags)
+            if self.tuner == "learned":
+                from . import tuner as tuner_mod
+                if os.path.exists(tuner_mod.DEFAULT_MODEL):
+                    self._cost_model = tuner_mod.use_learned_tuner(rt)
+                else:
+                    rt.config_set("tuner", 0)
+            else:
+                rt.config_set("tuner", 1 if self.tuner == "exhaustive" else 0)
+            self._runtime = rt
         return self._runtime
 
     @staticmethod

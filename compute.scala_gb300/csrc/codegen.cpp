@@ -1019,7 +1019,7 @@ int row_fold_stages(int row_inputs, int requested) {
   const int per_stage = row_inputs * kRowFoldRows * 128;
   if (requested >= 2 && requested <= 16 && requested * per_stage + 1024 <= 200 * 1024) return requested;
   int s = (96 * 1024) / (per_stage > 0 ? per_stage : 1);
-  return s < 2 ? 2 : s > 8 ? 8 : s;
+  return s < 2 ? 2 : s > 12 ? 12 : s;
 }
 
 int row_fold_smem_bytes(int row_inputs, int stages) { return stages * row_inputs * kRowFoldRows * 128 + 1024; }
@@ -1605,6 +1605,10 @@ bool is_tunable(const Ir &ir, std::string *why) {
   int64_t domain = 1;
   for (int64_t d : ir.out_shape) domain *= d;
   if (domain <= 0) return no("a tuned program has at least one point");
+  // The cost model knows programs of up to 47 nodes (its training workloads);
+  // larger ones run their standard kernel (their six-kernel tunable form also
+  // compiles slowly: over a minute for the 262-node view-heavy op).
+  if ((int)ir.nodes.size() > kTuneMaxNodes) return no("a tuned program has at most 64 nodes");
   return true;
 }
 

@@ -180,7 +180,8 @@ constexpr int kRowFoldMaxInputs = 4;   // row inputs staged per tile
 constexpr int kRowFoldWaitCode = 31;   // device error code: a tile's barrier wait ran out
 bool match_row_fold(const Ir &ir, RowFold *out, std::string *why = nullptr);
 // Stages of the shared-memory ring for `row_inputs` staged inputs: `requested`
-// (1..16) if it fits, else as many 8 KiB tiles as fit in 96 KiB, 2 to 8.
+// (2..16) if it fits, else as many 8 KiB tiles per input as fit in 96 KiB
+// (two blocks per SM), 2 to 12.
 int row_fold_stages(int row_inputs, int requested = 0);
 // Dynamic shared memory of cc_rowfold (ring + alignment slack).
 int row_fold_smem_bytes(int row_inputs, int stages);
@@ -211,6 +212,7 @@ struct TuneConfig {
   int block = 256, vec = 1, ept = 1, split = 1;
 };
 constexpr int kTuneConfigs = 48;
+constexpr int kTuneMaxNodes = 64;  // larger programs are not tuned
 // The tuner's choice "the program's standard generated kernel" (no tunable configuration).
 constexpr int kStdConfig = kTuneConfigs;
 constexpr int kTuneKernels = 6;  // (vec, ept) pairs compiled per program

@@ -92,7 +92,7 @@ int cc_synchronize(void);
  *                       shared memory by TMA and folds each output's terms in order (bit-identical to the
  *                       generated fold); 0 = the generated fold
  *   "row_fold_stages"   that skeleton's ring of 8 KiB tiles per staged input (2..16; 0 = as many as fit
- *                       96 KiB, at most 8; default 0)
+ *                       96 KiB, at most 12; default 0)
  *   "contraction"       how a program that is the library's matmul idiom runs (a left fold over j
  *                       of split(1) views of A.broadcast * B.reshape.broadcast): 0 = the generated
  *                       fold kernel, 1 = CC_GEMM_EXACT (bit-identical to 0, default), 2 = CC_GEMM_FP32,
@@ -321,6 +321,9 @@ int cc_batch_compile_check(const char *const *irs, const size_t *ir_lens, int n_
  *      of work items per thread; for a sum, the number of partial sums).
  *      Elementwise results are identical in every configuration; sums differ
  *      in the order of their compensated partials.
+ *      Programs of more than 64 IR nodes (beyond the cost model's training
+ *      workloads) and tuple-valued programs are not tuned: they run their
+ *      standard kernel whatever the knob.
  *      With the "tuner" knob at 1 (exhaustive), cc_program_get compiles the
  *      tunable form beside the standard kernels, and the first launch times
  *      all configurations and the standard kernel on its own buffers (3

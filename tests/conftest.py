@@ -17,8 +17,11 @@ _cuda = {}
 
 
 def cuda_tensors(**kw):
-    """One native device object per flag set for the whole session (compiled programs are cached)."""
+    """One native device object per flag set for the whole session (compiled programs are cached).
+    The parity tests pin the standard kernels, so the tuner is off unless asked for; the
+    tuner's own tests check that every configuration computes the standard kernel's bits."""
     from compute import Tensors
+    kw.setdefault("tuner", "off")
     key = tuple(sorted(kw.items()))
     if key not in _cuda:
         _cuda[key] = Tensors(device=0, **kw)

@@ -29,7 +29,7 @@ _CHILD = textwrap.dedent("""
     from compute.batch import Batch
     from oracle import interp
 
-    d = Tensors(device=0, flags=1)  # CC_FLAG_FMA_CONTRACT
+    d = Tensors(device=0, flags=1, tuner="off")  # CC_FLAG_FMA_CONTRACT; the standard kernels
     T = d.Tensor
 
     def check(expr, kind="ew"):
