@@ -388,6 +388,7 @@ struct Context {
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
   int batch_max_registers = 64;   // four 256-thread blocks per SM for the persistent kernel
   int batch_run_tiles = 4;        // tiles a persistent block claims at once
+  int batch_max_loads = 16;       // float4 loads a tile function keeps in flight per thread
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int ew_points = 1;     // generic elementwise kernels: consecutive points per thread
@@ -1131,6 +1132,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "batch_run_tiles") {
     if (value < 1 || value > 4096) fail(CC_ERR_INVALID_VALUE, "batch_run_tiles must be in [1, 4096]");
     c.batch_run_tiles = (int)value;
+  } else if (k == "batch_max_loads") {
+    if (value != 4 && value != 8 && value != 16) fail(CC_ERR_INVALID_VALUE, "batch_max_loads must be 4, 8 or 16");
+    c.batch_max_loads = (int)value;
   } else if (k == "batch_max_registers") {
     if (value < 0 || value > 255) fail(CC_ERR_INVALID_VALUE, "batch_max_registers must be in [0, 255]");
     c.batch_max_registers = (int)value;
@@ -1190,6 +1194,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "tc_group_m") *value = c.tc_group_m;
   else if (k == "copy_kernel") *value = c.copy_kernel;
   else if (k == "batch_max_registers") *value = c.batch_max_registers;
+  else if (k == "batch_max_loads") *value = c.batch_max_loads;
   else if (k == "batch_run_tiles") *value = c.batch_run_tiles;
   else fail(CC_ERR_INVALID_VALUE, "unknown config key '" + k + "'");
   CC_API_END
@@ -2039,7 +2044,7 @@ const char *kTileParams =
 // 1 = the expression is inlined into its tile function, exp/log/tanh called;
 // 2 = everything inlined.  Higher levels run faster and compile slower.
 std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs, size_t first,
-                               size_t last, int inline_level) {
+                               size_t last, int inline_level, int max_loads) {
   std::ostringstream o;
   o << "// generated batch part for sm_103a\n"
     << "static __device__ __noinline__ float cc_expf(float x) { return expf(x); }\n"
@@ -2057,25 +2062,32 @@ std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector
         c += (i ? ", " : "") + (i < nin ? "v" + std::to_string(i) + suffix : std::string("0.0f"));
       return c + ")";
     };
-    // A full tile loads all its float4s before computing any, so every thread
-    // has kBatchUnroll loads per input in flight; the ragged last tile of a
-    // program takes the plain loops.
+    // A full tile loads its float4s before computing any: all kBatchUnroll
+    // positions per input at once, or, when that is more than max_loads float4
+    // loads, in groups of positions (fewer registers held by loads in flight);
+    // the ragged last tile of a program takes the plain loops.
+    int group = kBatchUnroll;
+    while (group > 1 && nin * group > max_loads) group /= 2;
     o << "extern \"C\" __device__ __noinline__ void cc_tile_" << S << kTileParams << " {\n"
       << "  for (; count > 0; --count, base += " << kBatchTile << "LL) {\n"
       << "  if (base + " << kBatchTile << "LL <= n) {\n"
       << "    const long long q0 = (base >> 2) + threadIdx.x;\n";
-    for (int i = 0; i < nin; ++i)
-      for (int u = 0; u < kBatchUnroll; ++u)
-        o << "    const float4 v" << i << "_" << u << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q0 + "
-          << u * kBatchBlock << ");\n";
-    for (int u = 0; u < kBatchUnroll; ++u) {
-      const std::string U = "_" + std::to_string(u);
-      o << "    float4 r" << U << ";\n";
-      for (const char *lane : {".x", ".y", ".z", ".w"})
-        o << "    r" << U << lane << " = " << call(U + lane) << ";\n";
+    for (int g0 = 0; g0 < kBatchUnroll; g0 += group) {
+      o << "    {\n";
+      for (int i = 0; i < nin; ++i)
+        for (int u = g0; u < g0 + group; ++u)
+          o << "    const float4 v" << i << "_" << u << " = __ldg(reinterpret_cast<const float4 *>(in" << i
+            << ") + q0 + " << u * kBatchBlock << ");\n";
+      for (int u = g0; u < g0 + group; ++u) {
+        const std::string U = "_" + std::to_string(u);
+        o << "    float4 r" << U << ";\n";
+        for (const char *lane : {".x", ".y", ".z", ".w"})
+          o << "    r" << U << lane << " = " << call(U + lane) << ";\n";
+      }
+      for (int u = g0; u < g0 + group; ++u)
+        o << "    reinterpret_cast<float4 *>(out)[q0 + " << u * kBatchBlock << "] = r_" << u << ";\n";
+      o << "    }\n";
     }
-    for (int u = 0; u < kBatchUnroll; ++u)
-      o << "    reinterpret_cast<float4 *>(out)[q0 + " << u * kBatchBlock << "] = r_" << u << ";\n";
     o << "    continue;\n  }\n"
       << "  const long long end = base + " << kBatchTile << "LL < n ? base + " << kBatchTile << "LL : n;\n"
       << "  const long long end4 = end & ~3LL;\n"
@@ -2171,12 +2183,13 @@ std::vector<std::vector<char>> compile_parallel(const std::vector<std::string> &
 // Compiles the parts in parallel and links them into one loadable image.
 std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs,
                                     int cc_major, int cc_minor, uint32_t flags, bool link, int inline_level,
-                                    int max_registers) {
+                                    int max_registers, int max_loads = 16) {
   std::vector<std::string> sources;
   FmaScope fma_scope((flags & CC_FLAG_FMA_CONTRACT) != 0);
   for (size_t first = 0; first < structs.size(); first += kBatchChunk)
     sources.push_back(batch_chunk_source(structs, struct_inputs, first,
-                                         std::min(structs.size(), first + (size_t)kBatchChunk), inline_level));
+                                         std::min(structs.size(), first + (size_t)kBatchChunk), inline_level,
+                                         max_loads));
   sources.push_back(batch_main_source(structs.size()));
   std::vector<std::vector<char>> parts = compile_parallel(sources, cc_major, cc_minor, flags, true, max_registers);
   if (!link) return {};
@@ -2272,7 +2285,7 @@ int cc_batch_create(const char *const *irs, const size_t *lens, int n_programs, 
   {
     std::lock_guard<std::mutex> cg(c.compile_mu);
     cubin = build_batch_image(structs, struct_inputs, c.cc_major, c.cc_minor, c.flags, true, c.batch_inline,
-                              c.batch_max_registers);
+                              c.batch_max_registers, c.batch_max_loads);
   }
   check_cu(g_drv.ModuleLoadData(&b->module, cubin.data()), "cuModuleLoadData");
   check_cu(g_drv.ModuleGetFunction(&b->persistent, b->module, "cc_batch"), "cuModuleGetFunction");
