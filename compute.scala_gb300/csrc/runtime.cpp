@@ -362,6 +362,7 @@ struct Context {
   std::unordered_map<uint64_t, Program *> programs;   // by handle
   std::unordered_map<std::string, uint64_t> cache;    // IR text -> program handle
   std::unordered_map<std::string, std::shared_ptr<Module>> modules;  // structure key -> module
+  std::unordered_map<std::string, std::shared_ptr<TuneModule>> tune_modules;  // structure key -> tunable form
   std::unordered_map<uint64_t, Event *> events;
   std::unordered_map<uint64_t, Batch *> batches;
   std::unordered_map<uint64_t, TuneSet *> tune_sets;
@@ -388,7 +389,7 @@ struct Context {
   int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
   int batch_max_registers = 64;   // four 256-thread blocks per SM for the persistent kernel
   int batch_run_tiles = 4;        // tiles a persistent block claims at once
-  int batch_max_loads = 16;       // float4 loads a tile function keeps in flight per thread
+  int batch_max_loads = 8;        // float4 loads a tile function keeps in flight per thread
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int ew_points = 1;     // generic elementwise kernels: consecutive points per thread
@@ -1002,6 +1003,7 @@ int cc_shutdown(void) {
   c->multi_queue = false;  // every stream is idle: blocks go straight back to the pool
   for (auto &kv : c->programs) delete kv.second;
   c->modules.clear();
+  c->tune_modules.clear();
   for (auto &kv : c->batches) {
     Batch *b = kv.second;
     if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
@@ -1580,11 +1582,26 @@ int cc_program_get(const char *ir_text, size_t ir_len, cc_handle *out) {
     // tunable configurations and the standard kernel at the first launch.
     auto p = std::make_unique<Program>();
     p->kind = ir.kind;
-    const std::string tunable = std::string("// generated by compute.scala_gb300 for sm_103a (tunable form)\n") +
-                                kPrelude + "\n" + tunable_source(ir, "");
-    std::vector<char> cubin = compile_cubin(tunable, c.cc_major, c.cc_minor, c.flags);
+    // contiguous programs share one tunable module per structure (the length is an argument)
+    std::string tkey = contiguous_structure_key(ir);
+    std::shared_ptr<TuneModule> tmod;
+    if (!tkey.empty()) {
+      tkey += "#tunable flags " + std::to_string(c.flags);
+      std::lock_guard<std::recursive_mutex> g(c.mu);
+      auto it = c.tune_modules.find(tkey);
+      if (it != c.tune_modules.end()) tmod = it->second;
+    }
+    if (!tmod) {
+      const std::string tunable = std::string("// generated by compute.scala_gb300 for sm_103a (tunable form)\n") +
+                                  kPrelude + "\n" + tunable_source(ir, "");
+      tmod = load_tune_module(compile_cubin(tunable, c.cc_major, c.cc_minor, c.flags));
+      if (!tkey.empty()) {
+        std::lock_guard<std::recursive_mutex> g(c.mu);
+        c.tune_modules[tkey] = tmod;
+      }
+    }
     p->tune = std::make_unique<TuneEntry>();
-    load_tune_entry(*p->tune, ir, load_tune_module(cubin), "");
+    load_tune_entry(*p->tune, ir, tmod, "");
     p->mod = standard_module(c, ir, opt, key, &p->gen);
     std::lock_guard<std::recursive_mutex> g(c.mu);
     uint64_t h = c.make_handle(kTagProgram);

@@ -130,7 +130,7 @@ int cc_synchronize(void);
  *   "batch_run_tiles"   consecutive 4096-float tiles a block of the persistent batch kernel claims at once
  *                       (default 4)
  *   "batch_max_loads"   float4 loads a batch tile function keeps in flight per thread (4, 8 or 16; default
- *                       16: every input's four positions at once); fewer load the positions in groups
+ *                       8); programs with more inputs load their four positions per input in groups
  *   "batch_inline"      batch modules: 0 = expressions and exp/log/tanh are called functions,
  *                       1 = expressions inlined, exp/log/tanh called (default), 2 = all inlined
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in
