@@ -309,7 +309,7 @@ class Generator {
       case NodeKind::Literal:
         v = fresh();
         if (reuse("K " + lit_code(node.bits), v)) break;
-        add(Cat::Compute, "const float " + v + " = " + lit_code(node.bits) + ";");
+        add(Cat::Compute, "const " + ty() + " " + v + " = " + lit_code(node.bits) + ";");
         break;
       case NodeKind::Unary: {
         std::string a = gen(node.a, f);
@@ -317,11 +317,12 @@ class Generator {
         if (reuse("U " + std::to_string(node.op) + " " + a, v)) break;
         static const char *fn[] = {"-", "expf", "logf", "tanhf", "fabsf", "sqrtf"};
         static const char *shared_fn[] = {"-", "cc_expf", "cc_logf", "cc_tanhf", "fabsf", "sqrtf"};
+        static const char *lane_fn[] = {"-", "cc_exp", "cc_log", "cc_tanh", "cc_abs", "cc_sqrt"};
         if (node.op == (uint8_t)UnOp::Neg)
-          add(Cat::Compute, "const float " + v + " = -" + a + ";");
+          add(Cat::Compute, "const " + ty() + " " + v + " = -" + a + ";");
         else
-          add(Cat::Compute, "const float " + v + " = " + (shared_transcendentals_ ? shared_fn : fn)[node.op] + "(" +
-                                a + ");");
+          add(Cat::Compute, "const " + ty() + " " + v + " = " +
+                                (lanes_ ? lane_fn : shared_transcendentals_ ? shared_fn : fn)[node.op] + "(" + a + ");");
         break;
       }
       case NodeKind::Binary: {
@@ -339,14 +340,15 @@ class Generator {
             std::string c = gen(a_mul ? node.b : node.a, f);
             v = fresh();
             std::string e;
+            const std::string fma = lanes_ ? "cc_fma(" : "__fmaf_rn(";
             if (node.op == (uint8_t)BinOp::Add)
-              e = "__fmaf_rn(" + p + ", " + q + ", " + c + ")";
+              e = fma + p + ", " + q + ", " + c + ")";
             else if (a_mul)
-              e = "__fmaf_rn(" + p + ", " + q + ", -" + c + ")";
+              e = fma + p + ", " + q + ", -" + c + ")";
             else
-              e = "__fmaf_rn(-" + p + ", " + q + ", " + c + ")";
+              e = fma + "-" + p + ", " + q + ", " + c + ")";
             if (reuse("B " + e, v)) break;
-            add(Cat::Compute, "const float " + v + " = " + e + ";");
+            add(Cat::Compute, "const " + ty() + " " + v + " = " + e + ";");
             break;
           }
         }
@@ -359,12 +361,12 @@ class Generator {
           case BinOp::Sub: e = a + " - " + b; break;
           case BinOp::Mul: e = a + " * " + b; break;
           case BinOp::Div: e = a + " / " + b; break;
-          case BinOp::Mod: e = "fmodf(" + a + ", " + b + ")"; break;
-          case BinOp::Min: e = "fminf(" + a + ", " + b + ")"; break;
-          case BinOp::Max: e = "fmaxf(" + a + ", " + b + ")"; break;
+          case BinOp::Mod: e = (lanes_ ? "cc_mod(" : "fmodf(") + a + ", " + b + ")"; break;
+          case BinOp::Min: e = (lanes_ ? "cc_min(" : "fminf(") + a + ", " + b + ")"; break;
+          case BinOp::Max: e = (lanes_ ? "cc_max(" : "fmaxf(") + a + ", " + b + ")"; break;
         }
         if (reuse("B " + e, v)) break;
-        add(Cat::Compute, "const float " + v + " = " + e + ";");
+        add(Cat::Compute, "const " + ty() + " " + v + " = " + e + ";");
         break;
       }
       case NodeKind::Extract: {
@@ -373,7 +375,7 @@ class Generator {
           fail(CC_ERR_INVALID_PROGRAM, "IR: view matrix columns do not match the frame rank");
         v = fresh();
         if (contig_) {
-          add(Cat::Compute, "const float " + v + " = a" + std::to_string(p.param_index) + ";");
+          add(Cat::Compute, "const " + ty() + " " + v + " = a" + std::to_string(p.param_index) + ";");
           break;
         }
         std::vector<std::string> idx, row_ok;
@@ -602,6 +604,7 @@ class Generator {
   // Emit scalar predicated loads of one condition in groups of kLoadBatch,
   // one predicate per group.
   void set_batch_loads(bool on) { batch_loads_ = on; }
+  void set_lanes(bool on) { lanes_ = on; }
   // Group reads of the same 16 bytes into float4 loads (needs merging on).
   void set_vector_loads(bool on) { vec_loads_ = on; }
   // Parameters with shared-memory copies (cc_sp<k>, 16-byte aligned).
@@ -793,6 +796,12 @@ class Generator {
   bool asm_loads_;
   int64_t prefetch_min_bytes_;
   bool shared_transcendentals_;
+  // Lane-generic contiguous code: every value has the template type T and
+  // every operation other than + - * / and negation goes through an
+  // overloaded cc_ helper (cc_exp, cc_fma, cc_min, ...), so one body serves a
+  // scalar and a several-lane evaluation with the same per-lane arithmetic.
+  bool lanes_ = false;
+  std::string ty() const { return lanes_ ? "T" : "float"; }
   bool fp64_ = false;
   int next_var_ = 0;
   int next_frame_ = 1;
@@ -1166,15 +1175,19 @@ bool is_batchable(const Ir &ir, std::string *why) {
   return true;
 }
 
-std::string point_function(const Ir &ir, const std::string &name, bool inline_it, bool shared_transcendentals) {
+std::string point_function(const Ir &ir, const std::string &name, bool inline_it, bool shared_transcendentals,
+                           bool lanes) {
   Generator gen(ir, true, false, -1, shared_transcendentals);
+  gen.set_lanes(lanes);
   std::ostringstream body;
   Frame f0{0, {}, ir.out_shape};
   std::string r = gen.gen(ir.root, f0);
   gen.emit(body, 2, 0);
   std::ostringstream o;
-  o << "__device__ " << (inline_it ? "__forceinline__" : "__noinline__") << " float " << name << "(";
-  for (int i = 0; i < kBatchMaxInputs; ++i) o << (i ? ", " : "") << "float a" << i;
+  const char *ty = lanes ? "T" : "float";
+  if (lanes) o << "template <class T> ";
+  o << "__device__ " << (inline_it ? "__forceinline__" : "__noinline__") << " " << ty << " " << name << "(";
+  for (int i = 0; i < kBatchMaxInputs; ++i) o << (i ? ", " : "") << ty << " a" << i;
   o << ") {\n" << body.str() << "  return " << r << ";\n}\n";
   return o.str();
 }

@@ -198,9 +198,13 @@ bool is_batchable(const Ir &ir, std::string *why);
 // program's value at one point from its inputs' values there (unused
 // arguments are ignored).  With shared_transcendentals, exp/log/tanh go through
 // the module's cc_expf/cc_logf/cc_tanhf (the same functions, called, which keeps
-// the code of thousands of structures small).
+// the code of thousands of structures small).  With lanes, the function is a
+// template over the value type T (`template <class T> T <name>(T a0, ...)`):
+// its operations are + - * / and negation on T and the overloaded helpers
+// cc_exp, cc_log, cc_tanh, cc_abs, cc_sqrt, cc_fma, cc_mod, cc_min and cc_max,
+// which the including module defines for each T it evaluates.
 std::string point_function(const Ir &ir, const std::string &name, bool inline_it = true,
-                           bool shared_transcendentals = false);
+                           bool shared_transcendentals = false, bool lanes = false);
 
 // ---- tuning
 // A launch configuration of a program's tunable form: threads per block,

@@ -344,6 +344,14 @@ struct Batch {
 
 enum : uint64_t { kTagBuffer = 1, kTagProgram = 2, kTagEvent = 3, kTagBatch = 4, kTagTuneSet = 5, kTagMlp = 6 };
 
+// Defaults of the batch code-generation knobs (also what the CPU-side
+// compile check builds).
+constexpr int kBatchInlineDefault = 1;
+constexpr int kBatchRegistersDefault = 64;
+constexpr int kBatchLoadsDefault = 4;
+constexpr int kBatchLanesDefault = 4;
+constexpr int kBatchRolledDefault = 1;
+
 struct Context {
   int device = 0;
   CUcontext cuctx = nullptr;
@@ -386,10 +394,12 @@ struct Context {
   int contraction = 1;  // 0: generated fold kernel; else CC_GEMM_* mode + 1
   int row_fold = 1;     // inner-axis folds of at least kRowFoldMinTerms terms: 1 = TMA-staged skeleton
   int row_fold_stages = 0;  // its ring stages (0 = as many 8 KiB tiles as fit 96 KiB, at most 8)
-  int batch_inline = 1;           // expressions inlined into tile functions, exp/log/tanh called
-  int batch_max_registers = 64;   // four 256-thread blocks per SM for the persistent kernel
-  int batch_run_tiles = 4;        // tiles a persistent block claims at once
-  int batch_max_loads = 8;        // float4 loads a tile function keeps in flight per thread
+  int batch_inline = kBatchInlineDefault;          // expressions inlined into tile functions, exp/log/tanh called
+  int batch_max_registers = kBatchRegistersDefault;  // four 256-thread blocks per SM for the persistent kernel
+  int batch_run_tiles = 4;                          // tiles a persistent block claims at once
+  int batch_max_loads = kBatchLoadsDefault;         // float4 loads a tile function keeps in flight per thread
+  int batch_lanes = kBatchLanesDefault;             // points a tile function evaluates together (0: one)
+  int batch_rolled = kBatchRolledDefault;           // a tile's load groups in a loop (1) or unrolled (0)
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int ew_points = 1;     // generic elementwise kernels: consecutive points per thread
@@ -1135,7 +1145,8 @@ int cc_config_set(const char *key, int64_t value) {
     if (value < 1 || value > 4096) fail(CC_ERR_INVALID_VALUE, "batch_run_tiles must be in [1, 4096]");
     c.batch_run_tiles = (int)value;
   } else if (k == "batch_max_loads") {
-    if (value != 4 && value != 8 && value != 16) fail(CC_ERR_INVALID_VALUE, "batch_max_loads must be 4, 8 or 16");
+    if (value != 1 && value != 2 && value != 4 && value != 8 && value != 16)
+      fail(CC_ERR_INVALID_VALUE, "batch_max_loads must be 1, 2, 4, 8 or 16");
     c.batch_max_loads = (int)value;
   } else if (k == "batch_max_registers") {
     if (value < 0 || value > 255) fail(CC_ERR_INVALID_VALUE, "batch_max_registers must be in [0, 255]");
@@ -1143,6 +1154,12 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "batch_inline") {
     if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "batch_inline must be 0, 1 or 2");
     c.batch_inline = (int)value;
+  } else if (k == "batch_rolled") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "batch_rolled must be 0 or 1");
+    c.batch_rolled = (int)value;
+  } else if (k == "batch_lanes") {
+    if (value != 0 && value != 4 && value != 8) fail(CC_ERR_INVALID_VALUE, "batch_lanes must be 0, 4 or 8");
+    c.batch_lanes = (int)value;
   } else if (k == "row_fold_stages") {
     if (value != 0 && (value < 2 || value > 16)) fail(CC_ERR_INVALID_VALUE, "row_fold_stages must be 0 or in [2, 16]");
     c.row_fold_stages = (int)value;
@@ -1187,6 +1204,8 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "row_fold") *value = c.row_fold;
   else if (k == "row_fold_stages") *value = c.row_fold_stages;
   else if (k == "batch_inline") *value = c.batch_inline;
+  else if (k == "batch_lanes") *value = c.batch_lanes;
+  else if (k == "batch_rolled") *value = c.batch_rolled;
   else if (k == "tuner") *value = c.tuner;
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
   else if (k == "ew_points") *value = c.ew_points;
@@ -2060,59 +2079,175 @@ const char *kTileParams =
 // inline_level: 0 = the expression is a called function and so are exp/log/tanh;
 // 1 = the expression is inlined into its tile function, exp/log/tanh called;
 // 2 = everything inlined.  Higher levels run faster and compile slower.
+//
+// lanes (0, 4 or 8): the expression is evaluated on several points at once,
+// a float4 (4) or two float4 positions (8), as a template over the value type
+// (cc_f4, cc_f8; float for the ragged end), so a called exp/log/tanh computes
+// 4 or 8 independent values per call.  Each lane runs the same scalar
+// operation as the one-lane form (same functions, same rounding), so the
+// results are identical bit for bit.
+const char *kBatchLanePrelude = R"(namespace {
+struct cc_f4 {
+  float x, y, z, w;
+  __device__ __forceinline__ cc_f4() {}
+  __device__ __forceinline__ cc_f4(float s) : x(s), y(s), z(s), w(s) {}
+  __device__ __forceinline__ cc_f4(float4 v) : x(v.x), y(v.y), z(v.z), w(v.w) {}
+  __device__ __forceinline__ float4 f4() const { return make_float4(x, y, z, w); }
+};
+__device__ __forceinline__ cc_f4 operator+(cc_f4 a, cc_f4 b) { cc_f4 r; r.x = a.x + b.x; r.y = a.y + b.y; r.z = a.z + b.z; r.w = a.w + b.w; return r; }
+__device__ __forceinline__ cc_f4 operator-(cc_f4 a, cc_f4 b) { cc_f4 r; r.x = a.x - b.x; r.y = a.y - b.y; r.z = a.z - b.z; r.w = a.w - b.w; return r; }
+__device__ __forceinline__ cc_f4 operator*(cc_f4 a, cc_f4 b) { cc_f4 r; r.x = a.x * b.x; r.y = a.y * b.y; r.z = a.z * b.z; r.w = a.w * b.w; return r; }
+__device__ __forceinline__ cc_f4 operator/(cc_f4 a, cc_f4 b) { cc_f4 r; r.x = a.x / b.x; r.y = a.y / b.y; r.z = a.z / b.z; r.w = a.w / b.w; return r; }
+__device__ __forceinline__ cc_f4 operator-(cc_f4 a) { cc_f4 r; r.x = -a.x; r.y = -a.y; r.z = -a.z; r.w = -a.w; return r; }
+__device__ __forceinline__ float cc_abs(float a) { return fabsf(a); }
+__device__ __forceinline__ float cc_sqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ float cc_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float cc_mod(float a, float b) { return fmodf(a, b); }
+__device__ __forceinline__ float cc_min(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ float cc_max(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ cc_f4 cc_abs(cc_f4 a) { cc_f4 r; r.x = fabsf(a.x); r.y = fabsf(a.y); r.z = fabsf(a.z); r.w = fabsf(a.w); return r; }
+__device__ __forceinline__ cc_f4 cc_sqrt(cc_f4 a) { cc_f4 r; r.x = sqrtf(a.x); r.y = sqrtf(a.y); r.z = sqrtf(a.z); r.w = sqrtf(a.w); return r; }
+__device__ __forceinline__ cc_f4 cc_fma(cc_f4 a, cc_f4 b, cc_f4 c) {
+  cc_f4 r; r.x = __fmaf_rn(a.x, b.x, c.x); r.y = __fmaf_rn(a.y, b.y, c.y); r.z = __fmaf_rn(a.z, b.z, c.z); r.w = __fmaf_rn(a.w, b.w, c.w); return r;
+}
+__device__ __forceinline__ cc_f4 cc_mod(cc_f4 a, cc_f4 b) { cc_f4 r; r.x = fmodf(a.x, b.x); r.y = fmodf(a.y, b.y); r.z = fmodf(a.z, b.z); r.w = fmodf(a.w, b.w); return r; }
+__device__ __forceinline__ cc_f4 cc_min(cc_f4 a, cc_f4 b) { cc_f4 r; r.x = fminf(a.x, b.x); r.y = fminf(a.y, b.y); r.z = fminf(a.z, b.z); r.w = fminf(a.w, b.w); return r; }
+__device__ __forceinline__ cc_f4 cc_max(cc_f4 a, cc_f4 b) { cc_f4 r; r.x = fmaxf(a.x, b.x); r.y = fmaxf(a.y, b.y); r.z = fmaxf(a.z, b.z); r.w = fmaxf(a.w, b.w); return r; }
+struct cc_f8 {
+  cc_f4 lo, hi;
+  __device__ __forceinline__ cc_f8() {}
+  __device__ __forceinline__ cc_f8(float s) : lo(s), hi(s) {}
+  __device__ __forceinline__ cc_f8(float4 a, float4 b) : lo(a), hi(b) {}
+};
+__device__ __forceinline__ cc_f8 cc_pair(cc_f4 lo, cc_f4 hi) { cc_f8 r; r.lo = lo; r.hi = hi; return r; }
+__device__ __forceinline__ cc_f8 operator+(cc_f8 a, cc_f8 b) { return cc_pair(a.lo + b.lo, a.hi + b.hi); }
+__device__ __forceinline__ cc_f8 operator-(cc_f8 a, cc_f8 b) { return cc_pair(a.lo - b.lo, a.hi - b.hi); }
+__device__ __forceinline__ cc_f8 operator*(cc_f8 a, cc_f8 b) { return cc_pair(a.lo * b.lo, a.hi * b.hi); }
+__device__ __forceinline__ cc_f8 operator/(cc_f8 a, cc_f8 b) { return cc_pair(a.lo / b.lo, a.hi / b.hi); }
+__device__ __forceinline__ cc_f8 operator-(cc_f8 a) { return cc_pair(-a.lo, -a.hi); }
+__device__ __forceinline__ cc_f8 cc_abs(cc_f8 a) { return cc_pair(cc_abs(a.lo), cc_abs(a.hi)); }
+__device__ __forceinline__ cc_f8 cc_sqrt(cc_f8 a) { return cc_pair(cc_sqrt(a.lo), cc_sqrt(a.hi)); }
+__device__ __forceinline__ cc_f8 cc_fma(cc_f8 a, cc_f8 b, cc_f8 c) { return cc_pair(cc_fma(a.lo, b.lo, c.lo), cc_fma(a.hi, b.hi, c.hi)); }
+__device__ __forceinline__ cc_f8 cc_mod(cc_f8 a, cc_f8 b) { return cc_pair(cc_mod(a.lo, b.lo), cc_mod(a.hi, b.hi)); }
+__device__ __forceinline__ cc_f8 cc_min(cc_f8 a, cc_f8 b) { return cc_pair(cc_min(a.lo, b.lo), cc_min(a.hi, b.hi)); }
+__device__ __forceinline__ cc_f8 cc_max(cc_f8 a, cc_f8 b) { return cc_pair(cc_max(a.lo, b.lo), cc_max(a.hi, b.hi)); }
+)";
+
+// exp, log and tanh over one lane and over four: called functions (shared by
+// every structure of the part) below inline level 2, else inlined.
+std::string batch_lane_transcendentals(int inline_level) {
+  std::ostringstream o;
+  const char *fq = inline_level >= 2 ? "__forceinline__" : "__noinline__";
+  for (const char *f : {"exp", "log", "tanh"}) {
+    const std::string F = std::string(f) + "f(";
+    o << "__device__ " << fq << " float cc_" << f << "(float a) { return " << F << "a); }\n"
+      << "__device__ " << fq << " cc_f4 cc_" << f << "(cc_f4 a) { cc_f4 r; r.x = " << F << "a.x); r.y = " << F
+      << "a.y); r.z = " << F << "a.z); r.w = " << F << "a.w); return r; }\n"
+      << "__device__ " << fq << " cc_f8 cc_" << f << "(cc_f8 a) { cc_f8 r; r.lo.x = " << F << "a.lo.x); r.lo.y = "
+      << F << "a.lo.y); r.lo.z = " << F << "a.lo.z); r.lo.w = " << F << "a.lo.w); r.hi.x = " << F
+      << "a.hi.x); r.hi.y = " << F << "a.hi.y); r.hi.z = " << F << "a.hi.z); r.hi.w = " << F
+      << "a.hi.w); return r; }\n";
+  }
+  return o.str();
+}
+
 std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs, size_t first,
-                               size_t last, int inline_level, int max_loads) {
+                               size_t last, int inline_level, int max_loads, int lane_width, bool rolled) {
+  const bool lanes = lane_width > 0;
   std::ostringstream o;
   o << "// generated batch part for sm_103a\n"
     << "static __device__ __noinline__ float cc_expf(float x) { return expf(x); }\n"
        "static __device__ __noinline__ float cc_logf(float x) { return logf(x); }\n"
        "static __device__ __noinline__ float cc_tanhf(float x) { return tanhf(x); }\n";
+  if (lanes) o << kBatchLanePrelude << batch_lane_transcendentals(inline_level) << "}  // namespace\n";
   const std::string B = std::to_string(kBatchBlock);
   for (size_t s = first; s < last; ++s) {
     const int nin = struct_inputs[s];
     const std::string S = std::to_string(s);
-    std::string pf = point_function(structs[s], "cc_point_" + S, inline_level >= 1, inline_level <= 1);
-    o << "static " << pf;
-    auto call = [&](const std::string &suffix) {
-      std::string c = "cc_point_" + S + "(";
-      for (int i = 0; i < kBatchMaxInputs; ++i)
-        c += (i ? ", " : "") + (i < nin ? "v" + std::to_string(i) + suffix : std::string("0.0f"));
+    std::string pf = point_function(structs[s], "cc_point_" + S, inline_level >= 1, inline_level <= 1, lanes);
+    o << (lanes ? "namespace {\n" + pf + "}  // namespace\n" : "static " + pf);
+    // one lane (`suffix` names a float: ".x", "_0.y", ...) or, with lanes, a
+    // whole float4 (`suffix` names the float4 itself and `four` is set)
+    auto call = [&](const std::string &suffix, bool four = false) {
+      std::string c = "cc_point_" + S + (lanes ? (four ? "<cc_f4>(" : "<float>(") : "(");
+      for (int i = 0; i < kBatchMaxInputs; ++i) {
+        std::string v = i < nin ? "v" + std::to_string(i) + suffix : std::string("0.0f");
+        if (four) v = "cc_f4(" + v + ")";
+        c += (i ? ", " : "") + v;
+      }
+      return c + ")" + (four ? ".f4()" : "");
+    };
+    // eight lanes: the float4s at positions u and u + 1 of every input
+    auto call8 = [&](int u) {
+      std::string c = "cc_point_" + S + "<cc_f8>(";
+      for (int i = 0; i < kBatchMaxInputs; ++i) {
+        const std::string I = std::to_string(i);
+        c += (i ? ", " : "") + (i < nin ? "cc_f8(v" + I + "_" + std::to_string(u) + ", v" + I + "_" +
+                                              std::to_string(u + 1) + ")"
+                                        : std::string("cc_f8(0.0f)"));
+      }
       return c + ")";
     };
     // A full tile loads its float4s before computing any: all kBatchUnroll
     // positions per input at once, or, when that is more than max_loads float4
-    // loads, in groups of positions (fewer registers held by loads in flight);
-    // the ragged last tile of a program takes the plain loops.
+    // loads, in groups of positions (fewer registers held by loads in flight;
+    // eight lanes take positions in pairs); the ragged last tile of a program
+    // takes the plain loops.
+    const int min_group = lane_width == 8 ? 2 : 1;
     int group = kBatchUnroll;
-    while (group > 1 && nin * group > max_loads) group /= 2;
+    while (group > min_group && nin * group > max_loads) group /= 2;
     o << "extern \"C\" __device__ __noinline__ void cc_tile_" << S << kTileParams << " {\n"
       << "  for (; count > 0; --count, base += " << kBatchTile << "LL) {\n"
       << "  if (base + " << kBatchTile << "LL <= n) {\n"
       << "    const long long q0 = (base >> 2) + threadIdx.x;\n";
-    for (int g0 = 0; g0 < kBatchUnroll; g0 += group) {
+    // rolled: one copy of the group's code in a loop over the groups (a
+    // smaller tile function) instead of one copy per group
+    const int copies = rolled ? group : kBatchUnroll;
+    if (rolled && group < kBatchUnroll)
+      o << "    #pragma unroll 1\n"
+        << "    for (int k_ = 0; k_ < " << kBatchUnroll << "; k_ += " << group << ") {\n"
+        << "    const long long qk = q0 + (long long)k_ * " << kBatchBlock << ";\n";
+    else
+      o << "    {\n    const long long qk = q0;\n";
+    for (int g0 = 0; g0 < copies; g0 += group) {
       o << "    {\n";
       for (int i = 0; i < nin; ++i)
         for (int u = g0; u < g0 + group; ++u)
           o << "    const float4 v" << i << "_" << u << " = __ldg(reinterpret_cast<const float4 *>(in" << i
-            << ") + q0 + " << u * kBatchBlock << ");\n";
-      for (int u = g0; u < g0 + group; ++u) {
+            << ") + qk + " << u * kBatchBlock << ");\n";
+      if (lane_width == 8) {
+        for (int u = g0; u < g0 + group; u += 2)
+          o << "    const cc_f8 r8_" << u << " = " << call8(u) << ";\n"
+            << "    const float4 r_" << u << " = r8_" << u << ".lo.f4(), r_" << u + 1 << " = r8_" << u
+            << ".hi.f4();\n";
+      }
+      for (int u = g0; u < g0 + group && lane_width != 8; ++u) {
         const std::string U = "_" + std::to_string(u);
+        if (lanes) {
+          o << "    const float4 r" << U << " = " << call(U, true) << ";\n";
+          continue;
+        }
         o << "    float4 r" << U << ";\n";
         for (const char *lane : {".x", ".y", ".z", ".w"})
           o << "    r" << U << lane << " = " << call(U + lane) << ";\n";
       }
       for (int u = g0; u < g0 + group; ++u)
-        o << "    reinterpret_cast<float4 *>(out)[q0 + " << u * kBatchBlock << "] = r_" << u << ";\n";
+        o << "    reinterpret_cast<float4 *>(out)[qk + " << u * kBatchBlock << "] = r_" << u << ";\n";
       o << "    }\n";
     }
+    o << "    }\n";
     o << "    continue;\n  }\n"
       << "  const long long end = base + " << kBatchTile << "LL < n ? base + " << kBatchTile << "LL : n;\n"
       << "  const long long end4 = end & ~3LL;\n"
       << "  for (long long q = (base >> 2) + threadIdx.x; (q << 2) < end4; q += " << B << ") {\n";
     for (int i = 0; i < nin; ++i)
       o << "    const float4 v" << i << " = __ldg(reinterpret_cast<const float4 *>(in" << i << ") + q);\n";
-    o << "    float4 r;\n";
-    for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    r" << lane << " = " << call(lane) << ";\n";
+    if (lanes) {
+      o << "    const float4 r = " << call("", true) << ";\n";
+    } else {
+      o << "    float4 r;\n";
+      for (const char *lane : {".x", ".y", ".z", ".w"}) o << "    r" << lane << " = " << call(lane) << ";\n";
+    }
     o << "    reinterpret_cast<float4 *>(out)[q] = r;\n  }\n"
       << "  for (long long i = end4 + threadIdx.x; i < end; i += " << B << ") {\n";
     for (int i = 0; i < nin; ++i) o << "    const float v" << i << " = __ldg(in" << i << " + i);\n";
@@ -2200,13 +2335,13 @@ std::vector<std::vector<char>> compile_parallel(const std::vector<std::string> &
 // Compiles the parts in parallel and links them into one loadable image.
 std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs,
                                     int cc_major, int cc_minor, uint32_t flags, bool link, int inline_level,
-                                    int max_registers, int max_loads = 16) {
+                                    int max_registers, int max_loads, int lane_width, bool rolled) {
   std::vector<std::string> sources;
   FmaScope fma_scope((flags & CC_FLAG_FMA_CONTRACT) != 0);
   for (size_t first = 0; first < structs.size(); first += kBatchChunk)
     sources.push_back(batch_chunk_source(structs, struct_inputs, first,
                                          std::min(structs.size(), first + (size_t)kBatchChunk), inline_level,
-                                         max_loads));
+                                         max_loads, lane_width, rolled));
   sources.push_back(batch_main_source(structs.size()));
   std::vector<std::vector<char>> parts = compile_parallel(sources, cc_major, cc_minor, flags, true, max_registers);
   if (!link) return {};
@@ -2302,7 +2437,7 @@ int cc_batch_create(const char *const *irs, const size_t *lens, int n_programs, 
   {
     std::lock_guard<std::mutex> cg(c.compile_mu);
     cubin = build_batch_image(structs, struct_inputs, c.cc_major, c.cc_minor, c.flags, true, c.batch_inline,
-                              c.batch_max_registers, c.batch_max_loads);
+                              c.batch_max_registers, c.batch_max_loads, c.batch_lanes, c.batch_rolled != 0);
   }
   check_cu(g_drv.ModuleLoadData(&b->module, cubin.data()), "cuModuleLoadData");
   check_cu(g_drv.ModuleGetFunction(&b->persistent, b->module, "cc_batch"), "cuModuleGetFunction");
@@ -2343,7 +2478,9 @@ int cc_batch_compile_check(const char *const *irs, const size_t *lens, int n_pro
     }
   }
   auto t0 = std::chrono::steady_clock::now();
-  build_batch_image(structs, struct_inputs, cc_major, cc_minor, 0, false, 0, 0);  // linking needs a driver
+  // a context's default settings; linking needs a driver
+  build_batch_image(structs, struct_inputs, cc_major, cc_minor, 0, false, kBatchInlineDefault, kBatchRegistersDefault,
+                    kBatchLoadsDefault, kBatchLanesDefault, kBatchRolledDefault != 0);
   if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (n_structures) *n_structures = (int)structs.size();
   CC_API_END

@@ -129,8 +129,13 @@ int cc_synchronize(void);
  *                       otherwise take the largest part's registers and one block per SM)
  *   "batch_run_tiles"   consecutive 4096-float tiles a block of the persistent batch kernel claims at once
  *                       (default 4)
- *   "batch_max_loads"   float4 loads a batch tile function keeps in flight per thread (4, 8 or 16; default
- *                       8); programs with more inputs load their four positions per input in groups
+ *   "batch_max_loads"   float4 loads a batch tile function keeps in flight per thread (1, 2, 4, 8 or 16;
+ *                       default 4); programs with more inputs load their four positions per input in groups
+ *   "batch_rolled"      batch tile functions: 1 = the load groups of a tile run in a loop over one copy of
+ *                       the group's code (default), 0 = one copy per group
+ *   "batch_lanes"       points a batch tile function evaluates per expression call: 4 = a float4's four
+ *                       (default; a called exp/log/tanh computes four values), 8 = two float4s, 0 = one
+ *                       point per call.  Every setting gives the same bits.
  *   "batch_inline"      batch modules: 0 = expressions and exp/log/tanh are called functions,
  *                       1 = expressions inlined, exp/log/tanh called (default), 2 = all inlined
  *   "tc_variant"        tensor-core contraction: 0 = 128x128 tiles, K in chunks of 128 summed in

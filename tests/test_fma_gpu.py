@@ -76,15 +76,21 @@ _CHILD = textwrap.dedent("""
     n = T.randomNormal([200, 256], seed=0x40000006)
     contracted += check((m * n - m).split(1).reduce(lambda u, v: u + v))
     # a batch: every program's bits are its single launch's
-    progs = [(T.random([5000 + 7 * k], seed=k) * T.fill(1.25, [5000 + 7 * k]) + T.fill(0.5, [5000 + 7 * k]))
-             for k in range(6)]
+    def contractible(k):
+        n = 5000 + 7 * k
+        u, w = T.random([n], seed=k), T.random([n], seed=100 + k)
+        return [u * T.fill(1.25, [n]) + T.fill(0.5, [n]), T.fill(0.5, [n]) - u * w, u * w - T.exp(u),
+                T.tanh(u * w + u * u)][k % 4]
+    progs = [contractible(k) for k in range(8)]
     single = [p.flatArray() for p in progs]
-    bt = Batch(d, progs).bind()
-    bt.run(Batch.PERSISTENT)
-    for k, want in enumerate(single):
-        got = d.runtime.download(bt.outputs[k], want.size)
-        assert np.array_equal(got.view(np.int32), want.view(np.int32))
-    bt.close()
+    for lanes in (0, 4, 8):  # one, four and eight points per tile-function call
+        d.runtime.config_set("batch_lanes", lanes)
+        bt = Batch(d, progs).bind()
+        bt.run(Batch.PERSISTENT)
+        for k, want in enumerate(single):
+            got = d.runtime.download(bt.outputs[k], want.size)
+            assert np.array_equal(got.view(np.int32), want.view(np.int32)), (lanes, k)
+        bt.close()
     assert contracted > 0
     print("fma mode bit-exact; %d points differ from the uncontracted oracle" % contracted)
 """)
