@@ -438,9 +438,16 @@ def keep_busy(rt, st, seconds):
         rt.synchronize()
 
 
-def time_e2e(d, st, steps):
-    """Host buffers in, result out, through the C ABI: upload inputs (non-blocking
-    writes ordered on the runtime's stream), launch, download (blocking)."""
+def time_e2e(d, st, steps, pipelined=True):
+    """Host buffers in, result out, through the C ABI, every step: upload the
+    inputs from pinned host memory, launch, read the result back.
+
+    pipelined: two steps in flight through the event API (cc_buf_upload_ev,
+    cc_launch_ev, cc_buf_download_ev: the reference's enqueue with wait lists),
+    each on its own device buffers, the host waiting for a step's result before
+    issuing the step two later; else one step at a time (non-blocking uploads,
+    launch, blocking read).  Returns (seconds per step, H2D bytes, D2H bytes,
+    whether every result read back has the bits of a launch on the inputs)."""
     import ctypes
     import numpy as np
     from compute._native import call
@@ -458,78 +465,201 @@ def time_e2e(d, st, steps):
     out = st["out"]
     out_elems = st["prog"].out_elems
     d2h = 4 * max(1, out_elems)
-    res = ctypes.c_void_p()  # the result lands in pinned host memory too
-    call("cc_host_alloc", ctypes.c_size_t(d2h), ctypes.byref(res))
+    depth = 2 if pipelined else 1
+    results = []  # the results land in pinned host memory too
+    for _ in range(depth):
+        res = ctypes.c_void_p()
+        call("cc_host_alloc", ctypes.c_size_t(d2h), ctypes.byref(res))
+        results.append(res)
+    owned = []
 
-    def step():
+    def blocking_step():
         for (ptr, arr), b in zip(hosts, inputs):
             call("cc_buf_upload_async", ctypes.c_uint64(b.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(b.nbytes))
         rt.launch(st["prog"], inputs, out)
-        call("cc_buf_download", ctypes.c_uint64(out.handle), ctypes.c_size_t(0), res, ctypes.c_size_t(d2h))
+        call("cc_buf_download", ctypes.c_uint64(out.handle), ctypes.c_size_t(0), results[0], ctypes.c_size_t(d2h))
+
+    if pipelined:
+        slots = []
+        for _ in range(depth):
+            ins = [rt.alloc(b.nbytes) for b in inputs]
+            o = rt.alloc(max(d2h, out.nbytes))
+            owned.extend(ins + [o])
+            slots.append((ins, o))
+        launched = [None] * depth
+        pending = []
+
+        def run(n_steps):
+            for k in range(n_steps):
+                s = k % depth
+                ins, o = slots[s]
+                # the slot's buffers are free once its previous launch has read them
+                wait = [launched[s]] if launched[s] else []
+                ups = [rt.upload_ev(b, ptr.value, b.nbytes, wait=wait) for (ptr, _), b in zip(hosts, ins)]
+                if launched[s]:
+                    rt.event_release(launched[s])
+                launched[s] = rt.launch_ev(st["prog"], ins, o, wait=ups)
+                for e in ups:
+                    rt.event_release(e)
+                pending.append(rt.download_ev(o, results[s].value, d2h, wait=[launched[s]]))
+                if len(pending) >= depth:  # this step's slot comes round again next: its result must be read
+                    e = pending.pop(0)
+                    rt.event_wait(e, 60 * 10 ** 9)
+                    rt.event_release(e)
+            while pending:
+                e = pending.pop(0)
+                rt.event_wait(e, 60 * 10 ** 9)
+                rt.event_release(e)
+    else:
+        def run(n_steps):
+            for _ in range(n_steps):
+                blocking_step()
 
     try:
-        for _ in range(2):
-            step()
+        run(2)
         t0 = time.perf_counter()
-        for _ in range(steps):
-            step()
+        run(steps)
         dt = (time.perf_counter() - t0) / steps
+        # every slot's last result against one launch on the original inputs
+        rt.launch(st["prog"], inputs, out)
+        want = rt.download(out, d2h // 4)
+        match = all(np.array_equal(np.ctypeslib.as_array((ctypes.c_float * (d2h // 4)).from_address(r.value)).view(
+            np.int32), want.view(np.int32)) for r in results)
     finally:
+        if pipelined:
+            for e in launched:
+                if e:
+                    rt.event_release(e)
+            rt.synchronize()
+        for b in owned:
+            b.release()
         for ptr, _ in hosts:
             call("cc_host_free", ptr)
-        call("cc_host_free", res)
-    return dt, h2d, d2h
+        for r in results:
+            call("cc_host_free", r)
+    return dt, h2d, d2h, match
+
+
+def e2e_record(d, st, steps, work, unit):
+    """The e2e record: the step timed both ways (two steps in flight through
+    the event API, and one step at a time), `work` units per step; the value is
+    the faster way's, and the record names it and carries both."""
+    dt_p, h2d, d2h, match_p = time_e2e(d, st, steps=steps)
+    dt_b, _, _, match_b = time_e2e(d, st, steps=steps, pipelined=False)
+    modes = {"two_in_flight": {"value": work / dt_p, "unit": unit, "ms_per_step": dt_p * 1e3,
+                               "how": "cc_buf_upload_ev, cc_launch_ev, cc_buf_download_ev with wait lists, two "
+                                      "steps in flight on their own device buffers"},
+             "one_at_a_time": {"value": work / dt_b, "unit": unit, "ms_per_step": dt_b * 1e3,
+                               "how": "cc_buf_upload_async, cc_launch, blocking cc_buf_download"}}
+    best = min(modes, key=lambda k: modes[k]["ms_per_step"])
+    return {"value": modes[best]["value"], "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_step": modes[best]["ms_per_step"], "mode": best, "modes": modes,
+            "note": "every step uploads its inputs from pinned host memory and reads its result back inside the "
+                    "timed region",
+            "results_match": bool(match_p and match_b)}
 
 
 def time_e2e_batch(d, b, progs, nbytes, steps):
-    """The batch through the C ABI with host buffers: every input uploaded from
-    pinned memory, one persistent launch, every output downloaded (non-blocking
-    reads, then one synchronisation), per step."""
+    """The batch through the C ABI with host buffers, every step: every input
+    uploaded from pinned memory, one persistent launch, every output read back.
+    Timed both ways, the value being the faster's:
+      two_in_flight: cc_batch_upload_ev / cc_batch_run_ev / cc_batch_download_ev
+        with wait lists (uploads after the previous run, the run after them and
+        the previous step's reads), a step's reads overlapping the next step's
+        uploads, each step reading into its own host buffers;
+      one_at_a_time: a non-blocking upload per input, the run, a non-blocking
+        read per output, one synchronisation."""
     import ctypes
     import numpy as np
     from compute._native import call
     rt = d.runtime
-    bufs = []
-    for _, inputs in progs:
-        for t in inputs:
-            bufs.append(t._cached)
+    # bound inputs: per program its parameters in the program's order
+    bufs = [prm._cached for ser in b.serialized for prm in ser.params]
+    pinned = []
+
+    def host(nb):
+        ptr = ctypes.c_void_p()
+        call("cc_host_alloc", ctypes.c_size_t(max(16, nb)), ctypes.byref(ptr))
+        pinned.append(ptr)
+        return ptr
+
     hosts = []
     h2d = 0
     for buf in bufs:
-        ptr = ctypes.c_void_p()
-        call("cc_host_alloc", ctypes.c_size_t(buf.nbytes), ctypes.byref(ptr))
+        ptr = host(buf.nbytes)
         ctypes.memmove(ptr, rt.download(buf, buf.nbytes // 4).ctypes.data, buf.nbytes)
         hosts.append(ptr)
         h2d += buf.nbytes
-    outs = []
-    d2h = 0
-    for out in b.outputs:
-        ptr = ctypes.c_void_p()
-        call("cc_host_alloc", ctypes.c_size_t(out.nbytes), ctypes.byref(ptr))
-        outs.append(ptr)
-        d2h += out.nbytes
+    outs = [[host(out.nbytes) for out in b.outputs] for _ in range(2)]
+    d2h = sum(out.nbytes for out in b.outputs)
 
-    def step():
+    def one_at_a_time():
         for ptr, buf in zip(hosts, bufs):
             call("cc_buf_upload_async", ctypes.c_uint64(buf.handle), ctypes.c_size_t(0), ptr,
                  ctypes.c_size_t(buf.nbytes))
         b.run(0)
-        for ptr, out in zip(outs, b.outputs):
+        for ptr, out in zip(outs[0], b.outputs):
             call("cc_buf_download_async", ctypes.c_uint64(out.handle), ctypes.c_size_t(0), ptr,
                  ctypes.c_size_t(out.nbytes))
         call("cc_synchronize")
 
-    try:
-        step()
+    host_in = [p.value for p in hosts]
+    host_out = [[p.value for p in o] for o in outs]
+
+    def two_in_flight(n_steps):
+        prev_run = prev_read = None
+        pending = []
+        for k in range(n_steps):
+            up = b.upload_ev(host_in, wait=[prev_run] if prev_run else [])
+            run = b.run_ev(0, wait=[up] + ([prev_read] if prev_read else []))
+            read = b.download_ev(host_out[k % 2], wait=[run])
+            rt.event_release(up)
+            if prev_run:
+                rt.event_release(prev_run)
+            prev_run, prev_read = run, read
+            pending.append(read)
+            if len(pending) >= 2:  # the step whose host buffers come round next: its results are read
+                e = pending.pop(0)
+                rt.event_wait(e, 600 * 10 ** 9)
+                rt.event_release(e)
+        for e in pending:
+            rt.event_wait(e, 600 * 10 ** 9)
+            rt.event_release(e)
+        if prev_run:
+            rt.event_release(prev_run)
+
+    def timed(fn):
+        fn(2)  # both host output sets seen once (the copy tables are built on first use)
         t0 = time.perf_counter()
-        for _ in range(steps):
-            step()
-        dt = (time.perf_counter() - t0) / steps
+        fn(steps)
+        return (time.perf_counter() - t0) / steps
+
+    try:
+        dt_b = timed(lambda n: [one_at_a_time() for _ in range(n)])
+        want = [np.ctypeslib.as_array((ctypes.c_float * (o.nbytes // 4)).from_address(p.value)).copy()
+                for p, o in zip(outs[0], b.outputs)]
+        dt_p = timed(two_in_flight)
+        match = all(np.array_equal(np.ctypeslib.as_array((ctypes.c_float * (o.nbytes // 4)).from_address(p.value))
+                                   .view(np.int32), w.view(np.int32))
+                    for slot in outs for p, o, w in zip(slot, b.outputs, want))
     finally:
-        for ptr in hosts + outs:
+        rt.synchronize()
+        for ptr in pinned:
             call("cc_host_free", ptr)
-    return {"value": nbytes / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "ms_per_step": dt * 1e3}
+    copier = "one SM copy kernel over a table of the copies" if rt.config_get("batch_copy_kernel") else \
+        "the DMA engines, one copy per buffer over four streams"
+    modes = {"two_in_flight": {"value": nbytes / dt_p / 1e9, "unit": "GB/s", "ms_per_step": dt_p * 1e3,
+                               "how": "cc_batch_upload_ev, cc_batch_run_ev, cc_batch_download_ev with wait lists; "
+                                      "copies by " + copier},
+             "one_at_a_time": {"value": nbytes / dt_b / 1e9, "unit": "GB/s", "ms_per_step": dt_b * 1e3,
+                               "how": "cc_buf_upload_async per input, cc_batch_run, cc_buf_download_async per "
+                                      "output, cc_synchronize"}}
+    best = min(modes, key=lambda k: modes[k]["ms_per_step"])
+    return {"value": modes[best]["value"], "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_step": modes[best]["ms_per_step"], "mode": best, "modes": modes,
+            "note": "every step uploads its inputs from pinned host memory and reads every output back inside "
+                    "the timed region",
+            "results_match": bool(match)}
 
 
 _KNOBS = []
@@ -735,9 +865,8 @@ def measure_fused(d, workload, steps, warmup, rank=0, world=1, local_rank=0, dis
                                    "ms": iso_ms, "note": "one launch between two synchronisations, median of 50"}}
     e2e = None
     if e2e_on:
-        dt, h2d, d2h = time_e2e(d, st, steps=max(3, min(steps, 20)))
-        e2e = {"value": st["bytes"] / dt / 1e9 * world, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
+        n_e2e = max(3, min(steps, 20))
+        e2e = e2e_record(d, st, n_e2e, st["bytes"] / 1e9 * world, "GB/s")
     peak, peak_kind = _peaks()
     roofline = {"bound": "hbm", "achieved": gbs_step, "peak": peak, "unit": "GB/s", "frac": gbs_step / peak,
                 "traffic": _traffic(workload), "peak_source": peak_kind,
@@ -1047,9 +1176,7 @@ def measure_contraction(d, workload, steps, warmup, local_rank=0, e2e_on=True, c
         extras = contraction_extras(d, st)
         e2e = None
         if e2e_on:
-            dt, h2d, d2h = time_e2e(d, st, steps=3)
-            e2e = {"value": st["flops"] / dt / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-                   "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3}
+            e2e = e2e_record(d, st, 3, st["flops"] / 1e12, "TFLOP/s")
     finally:
         release(st)
         rt.config_set("contraction", saved)

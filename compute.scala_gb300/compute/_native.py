@@ -190,6 +190,11 @@ _SIGNATURES = {
                       ctypes.POINTER(ctypes.c_int)],
     "cc_batch_bind": [c_handle, ctypes.POINTER(ctypes.c_uint64), c_size],
     "cc_batch_run": [c_handle, ctypes.c_int, ctypes.c_uint64],
+    "cc_batch_run_ev": [c_handle, ctypes.c_int, ctypes.POINTER(c_handle), ctypes.c_int, ctypes.POINTER(c_handle)],
+    "cc_batch_upload_ev": [c_handle, ctypes.POINTER(ctypes.c_void_p), c_size, ctypes.POINTER(c_handle), ctypes.c_int,
+                           ctypes.POINTER(c_handle)],
+    "cc_batch_download_ev": [c_handle, ctypes.POINTER(ctypes.c_void_p), c_size, ctypes.POINTER(c_handle),
+                             ctypes.c_int, ctypes.POINTER(c_handle)],
     "cc_batch_release": [c_handle],
     "cc_batch_compile_check": [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(c_size), ctypes.c_int, ctypes.c_int,
                                ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],

@@ -52,6 +52,18 @@ class Batch:
         self.device.runtime.batch_run(self.handle, mode)
         return self
 
+    # host transfers in the event model: each returns an event for the next wait list
+    def upload_ev(self, host_ptrs, wait=()):
+        """Every input from pinned host memory: per program, its inputs in parameter order."""
+        return self.device.runtime.batch_upload_ev(self.handle, host_ptrs, wait)
+
+    def run_ev(self, mode: int = 0, wait=()):
+        return self.device.runtime.batch_run_ev(self.handle, mode, wait)
+
+    def download_ev(self, host_ptrs, wait=()):
+        """Every output into pinned host memory (one pointer per program)."""
+        return self.device.runtime.batch_download_ev(self.handle, host_ptrs, wait)
+
     def results(self):
         """The outputs, as cached tensors that stay valid until closed."""
         res = []

@@ -244,6 +244,28 @@ class NativeRuntime:
     def batch_run(self, batch: int, mode: int = 0, stream: int = 0):
         call("cc_batch_run", c_handle(batch), int(mode), ctypes.c_uint64(stream))
 
+    def batch_run_ev(self, batch: int, mode: int = 0, wait=()) -> int:
+        w, nw = self._wait_list(wait)
+        ev = c_handle()
+        call("cc_batch_run_ev", c_handle(batch), int(mode), w, nw, ctypes.byref(ev))
+        return ev.value
+
+    def batch_upload_ev(self, batch: int, host_ptrs: Sequence[int], wait=()) -> int:
+        """Every bound input from pinned host memory (per program, its inputs in order)."""
+        arr = (ctypes.c_void_p * max(1, len(host_ptrs)))(*host_ptrs)
+        w, nw = self._wait_list(wait)
+        ev = c_handle()
+        call("cc_batch_upload_ev", c_handle(batch), arr, ctypes.c_size_t(len(host_ptrs)), w, nw, ctypes.byref(ev))
+        return ev.value
+
+    def batch_download_ev(self, batch: int, host_ptrs: Sequence[int], wait=()) -> int:
+        """Every program's output into pinned host memory."""
+        arr = (ctypes.c_void_p * max(1, len(host_ptrs)))(*host_ptrs)
+        w, nw = self._wait_list(wait)
+        ev = c_handle()
+        call("cc_batch_download_ev", c_handle(batch), arr, ctypes.c_size_t(len(host_ptrs)), w, nw, ctypes.byref(ev))
+        return ev.value
+
     def batch_release(self, batch: int):
         call("cc_batch_release", c_handle(batch))
 

@@ -134,6 +134,52 @@ cudaError_t launch_flag_wait(const int *flag, unsigned long long limit_ns, int *
   return cudaGetLastError();
 }
 
+// Many copies in one launch: the copies are cut into kCopyChunk-byte chunks,
+// numbered in table order (entry e owns chunks [chunk_begin(e), chunk_begin(e+1))),
+// and each block takes chunks grid-stride, finds the chunk's entry by binary
+// search and copies it 16 bytes per thread-step (4 bytes when an end of the
+// copy is not 16-byte aligned).
+__global__ void __launch_bounds__(256) copy_table_kernel(const CopyEntry *__restrict__ table, int n,
+                                                         long long chunks) {
+  for (long long c = blockIdx.x; c < chunks; c += gridDim.x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (table[mid].chunk_begin <= c) lo = mid; else hi = mid - 1;
+    }
+    const CopyEntry e = table[lo];
+    const unsigned long long off = (unsigned long long)(c - e.chunk_begin) * kCopyChunk;
+    if (off >= e.bytes) continue;
+    const unsigned long long len = e.bytes - off < kCopyChunk ? e.bytes - off : kCopyChunk;
+    const char *src = reinterpret_cast<const char *>(e.src) + off;
+    char *dst = reinterpret_cast<char *>(e.dst) + off;
+    if (((e.src | e.dst) & 15ull) == 0) {
+      const long long n16 = (long long)(len >> 4);
+      const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+      uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+      long long i = threadIdx.x;
+      for (; i + 3 * 256 < n16; i += 4 * 256) {
+        const uint4 a = s4[i], b = s4[i + 256], cc = s4[i + 512], d = s4[i + 768];
+        d4[i] = a;
+        d4[i + 256] = b;
+        d4[i + 512] = cc;
+        d4[i + 768] = d;
+      }
+      for (; i < n16; i += 256) d4[i] = s4[i];
+      for (long long j = (n16 << 4) + threadIdx.x; j < (long long)len; j += 256) dst[j] = src[j];
+    } else {
+      for (long long j = threadIdx.x; j < (long long)len; j += 256) dst[j] = src[j];
+    }
+  }
+}
+
+cudaError_t launch_copy_table(const CopyEntry *table, int n, long long chunks, int blocks, cudaStream_t stream) {
+  if (n <= 0 || chunks <= 0) return cudaSuccess;
+  const long long grid = chunks < blocks ? chunks : blocks;
+  copy_table_kernel<<<(unsigned)grid, 256, 0, stream>>>(table, n, chunks);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_copy16(void *dst, const void *src, size_t bytes, int sm_count, cudaStream_t stream) {
   const long long n16 = (long long)(bytes / 16);
   if (n16 <= 0) return cudaSuccess;

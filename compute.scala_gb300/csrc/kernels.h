@@ -15,6 +15,16 @@ int sum_grid(long long work, int sm_count);
 // Copies bytes / 16 sixteen-byte words with a kernel (both pointers 16-byte aligned,
 // device-accessible: device memory or pinned host memory); the remainder is the caller's.
 cudaError_t launch_copy16(void *dst, const void *src, size_t bytes, int sm_count, cudaStream_t stream);
+// One copy of a copy table (device-accessible addresses: device memory or
+// pinned host memory); chunk_begin = the copies before it, in kCopyChunk-byte chunks.
+constexpr unsigned long long kCopyChunk = 65536;
+struct CopyEntry {
+  unsigned long long dst, src, bytes;
+  long long chunk_begin;
+};
+// Every copy of a table of n entries (device memory), `chunks` chunks in all,
+// with at most `blocks` blocks of 256 threads.
+cudaError_t launch_copy_table(const CopyEntry *table, int n, long long chunks, int blocks, cudaStream_t stream);
 // One thread waits until *flag is nonzero, at most limit_ns; on expiry *err = code
 // (if it was 0).
 cudaError_t launch_flag_wait(const int *flag, unsigned long long limit_ns, int *err, int code, cudaStream_t stream);

@@ -340,6 +340,17 @@ struct Batch {
   int64_t total_tiles = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
+  // device copy tables of recent cc_batch_upload_ev / cc_batch_download_ev
+  // calls (most recent last), keyed by direction and host pointers
+  struct CopyTable {
+    std::vector<uint64_t> key;
+    uint64_t pinned_gen = 0;
+    void *dev = nullptr;
+    size_t cls = 0;
+    int n = 0;
+    long long chunks = 0;
+  };
+  std::vector<CopyTable> copy_tables;
 };
 
 enum : uint64_t { kTagBuffer = 1, kTagProgram = 2, kTagEvent = 3, kTagBatch = 4, kTagTuneSet = 5, kTagMlp = 6 };
@@ -407,6 +418,10 @@ struct Context {
   int ew_batch_loads = 0;   // those kernels: one predicate per group of 8 scalar loads
   int pdl = 1;           // launch generated kernels with programmatic dependent launch
   int copy_kernel = 0;   // copies between pinned host memory and the device by the SMs
+  int batch_copy_kernel = 1;  // batch transfers: one SM copy kernel over a table of the copies
+  // live cc_host_alloc allocations (start -> bytes); the generation changes at every free
+  std::map<uintptr_t, size_t> pinned;
+  uint64_t pinned_gen = 0;
   // The output range of the last generated kernel launched, and its stream: a
   // kernel that reads none of it may start its loads before that kernel ends,
   // provided nothing else was enqueued on the stream since.  Every entry point
@@ -427,6 +442,9 @@ struct Context {
   bool multi_queue = false;
   cudaStream_t queues[kQueues] = {};
   bool queue_dirty[kQueues] = {};  // work enqueued since the last cc_synchronize
+  // copy streams with batch transfers not joined into the context stream
+  // (cc_batch_*_ev) since the last cc_synchronize
+  bool copy_dirty[8] = {};
   int next_queue = 0;
   void *queue_scratch[kQueues] = {};  // each queue's sum partials and counter
   size_t queue_scratch_cls[kQueues] = {};
@@ -527,14 +545,18 @@ int queue_index(const Context &c, cudaStream_t s) {
 // context stream and on every queue that has work pending may still use the
 // block, so it is deferred behind a fence on each of them.
 void release_block(Context &c, void *p, size_t cls) {
-  if (!c.multi_queue) {
+  bool copies = false;
+  for (bool d : c.copy_dirty) copies = copies || d;
+  if (!c.multi_queue && !copies) {
     c.pool.release(p, cls);
     return;
   }
   std::vector<FencePtr> fences;
   fences.push_back(record_fence(c, c.stream));
   for (int i = 0; i < kQueues; ++i)
-    if (c.queue_dirty[i]) fences.push_back(record_fence(c, c.queues[i]));
+    if (c.multi_queue && c.queue_dirty[i]) fences.push_back(record_fence(c, c.queues[i]));
+  for (int i = 0; i < 8; ++i)
+    if (c.copy_dirty[i]) fences.push_back(record_fence(c, c.copy_streams[i]));
   c.pool.release(p, cls, std::move(fences));
 }
 
@@ -1154,6 +1176,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "batch_inline") {
     if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "batch_inline must be 0, 1 or 2");
     c.batch_inline = (int)value;
+  } else if (k == "batch_copy_kernel") {
+    if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "batch_copy_kernel must be 0 or 1");
+    c.batch_copy_kernel = (int)value;
   } else if (k == "batch_rolled") {
     if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "batch_rolled must be 0 or 1");
     c.batch_rolled = (int)value;
@@ -1206,6 +1231,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "batch_inline") *value = c.batch_inline;
   else if (k == "batch_lanes") *value = c.batch_lanes;
   else if (k == "batch_rolled") *value = c.batch_rolled;
+  else if (k == "batch_copy_kernel") *value = c.batch_copy_kernel;
   else if (k == "tuner") *value = c.tuner;
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
   else if (k == "ew_points") *value = c.ew_points;
@@ -1232,14 +1258,22 @@ int cc_synchronize(void) {
     multi = c.multi_queue;
   }
   check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  bool deferred = false;
   if (multi) {
-    std::lock_guard<std::recursive_mutex> g(c.mu);
     for (int i = 0; i < kQueues; ++i) {
       check_cuda(cudaStreamSynchronize(c.queues[i]), "cudaStreamSynchronize");
       c.queue_dirty[i] = false;
     }
-    c.pool.reclaim();
+    deferred = true;
   }
+  for (int i = 0; i < 8; ++i)
+    if (c.copy_dirty[i]) {
+      check_cuda(cudaStreamSynchronize(c.copy_streams[i]), "cudaStreamSynchronize");
+      c.copy_dirty[i] = false;
+      deferred = true;
+    }
+  if (deferred) c.pool.reclaim();
   CC_API_END
 }
 
@@ -1373,15 +1407,23 @@ int cc_buf_download_async(cc_handle h, size_t offset, void *host, size_t bytes) 
 int cc_host_alloc(size_t bytes, void **host) {
   CC_API_BEGIN
   if (!host) fail(CC_ERR_INVALID_VALUE, "null pointer");
-  ctx();
+  Context &c = ctx();
   check_cuda(cudaMallocHost(host, bytes ? bytes : 1), "cudaMallocHost");
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  c.pinned[reinterpret_cast<uintptr_t>(*host)] = bytes ? bytes : 1;
   CC_API_END
 }
 
 int cc_host_free(void *host) {
   CC_API_BEGIN
-  ctx();
-  if (host) check_cuda(cudaFreeHost(host), "cudaFreeHost");
+  Context &c = ctx();
+  if (!host) return CC_OK;
+  {
+    std::lock_guard<std::recursive_mutex> g(c.mu);
+    c.pinned.erase(reinterpret_cast<uintptr_t>(host));
+    ++c.pinned_gen;
+  }
+  check_cuda(cudaFreeHost(host), "cudaFreeHost");
   CC_API_END
 }
 
@@ -2379,6 +2421,125 @@ void batch_drop_graph(Batch &b) {
   b.graph = nullptr;
 }
 
+struct BatchCopy {
+  void *dst;
+  const void *src;
+  size_t bytes;
+};
+
+// Copies between pinned host memory and a batch's buffers, host to device on
+// copy streams 0-3 and device to host on copy streams 4-7 (so one step's reads
+// and the next step's uploads overlap on the link), each stream taking the
+// next copy when it holds the fewest bytes.  Every stream first waits for the
+// wait list; the returned event completes when every copy has.  The streams are
+// not joined into the context stream: the caller orders later work by the event.
+// Whether [p, p + bytes) lies inside one live cc_host_alloc allocation.
+bool in_pinned(const Context &c, const void *p, size_t bytes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  auto it = c.pinned.upper_bound(a);
+  if (it == c.pinned.begin()) return false;
+  --it;
+  return a - it->first <= it->second && bytes <= it->second - (a - it->first);
+}
+
+// The device copy table of these copies (built and cached on first use), or
+// nullptr when a host end is not memory of cc_host_alloc (then the DMA engines copy).
+const Batch::CopyTable *batch_copy_table(Context &c, Batch &b, const std::vector<BatchCopy> &copies, bool to_device) {
+  std::vector<uint64_t> key;
+  key.reserve(1 + 3 * copies.size());
+  key.push_back(to_device ? 1 : 0);
+  for (const BatchCopy &cp : copies) {
+    key.push_back(reinterpret_cast<uint64_t>(cp.dst));
+    key.push_back(reinterpret_cast<uint64_t>(cp.src));
+    key.push_back(cp.bytes);
+  }
+  for (auto it = b.copy_tables.begin(); it != b.copy_tables.end(); ++it)
+    if (it->pinned_gen == c.pinned_gen && it->key == key) {
+      if (it + 1 != b.copy_tables.end()) std::rotate(it, it + 1, b.copy_tables.end());  // most recent last
+      return &b.copy_tables.back();
+    }
+  std::vector<CopyEntry> table;
+  long long chunks = 0;
+  for (const BatchCopy &cp : copies) {
+    const void *host = to_device ? cp.src : cp.dst;
+    if (cp.bytes == 0) continue;
+    if (!in_pinned(c, host, cp.bytes)) return nullptr;
+    const void *alias = pinned_device_alias(host);
+    if (!alias) return nullptr;
+    CopyEntry e;
+    e.dst = reinterpret_cast<uint64_t>(to_device ? cp.dst : alias);
+    e.src = reinterpret_cast<uint64_t>(to_device ? alias : cp.src);
+    e.bytes = cp.bytes;
+    e.chunk_begin = chunks;
+    chunks += (long long)((cp.bytes + kCopyChunk - 1) / kCopyChunk);
+    table.push_back(e);
+  }
+  if (table.empty()) return nullptr;
+  Batch::CopyTable t;
+  t.key = std::move(key);
+  t.pinned_gen = c.pinned_gen;
+  t.n = (int)table.size();
+  t.chunks = chunks;
+  t.dev = c.pool.alloc(sizeof(CopyEntry) * table.size(), &t.cls);
+  // ordered after the context stream's work (the block may have served it) and
+  // complete before the host's table goes away: built once per pointer list
+  cudaError_t e = cudaMemcpyAsync(t.dev, table.data(), sizeof(CopyEntry) * table.size(), cudaMemcpyHostToDevice,
+                                  c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) {
+    release_block(c, t.dev, t.cls);
+    check_cuda(e, "cudaMemcpy copy table");
+  }
+  constexpr size_t kKeep = 4;
+  if (b.copy_tables.size() >= kKeep) {
+    release_block(c, b.copy_tables.front().dev, b.copy_tables.front().cls);
+    b.copy_tables.erase(b.copy_tables.begin());
+  }
+  b.copy_tables.push_back(std::move(t));
+  return &b.copy_tables.back();
+}
+
+void batch_drop_copy_tables(Context &c, Batch &b) {
+  for (auto &t : b.copy_tables) release_block(c, t.dev, t.cls);
+  b.copy_tables.clear();
+}
+
+cc_handle batch_copies(Context &c, Batch &b, const std::vector<BatchCopy> &copies, bool to_device,
+                       const cc_handle *wait, int n_wait) {
+  const int first = to_device ? 0 : 4, n = 4;
+  if (c.batch_copy_kernel) {
+    // one kernel over the whole table on the direction's first copy stream
+    const Batch::CopyTable *t = batch_copy_table(c, b, copies, to_device);
+    if (t) {
+      cudaStream_t s = c.copy_streams[first];
+      wait_events(c, s, wait, n_wait);
+      check_cuda(launch_copy_table(static_cast<const CopyEntry *>(t->dev), t->n, t->chunks, c.sm_count * 2, s),
+                 "copy table kernel");
+      c.copy_dirty[first] = true;
+      return fence_handle(c, record_fence(c, s));
+    }
+  }
+  for (int i = 0; i < n; ++i) wait_events(c, c.copy_streams[first + i], wait, n_wait);
+  size_t load[4] = {0, 0, 0, 0};
+  for (const BatchCopy &cp : copies) {
+    if (!cp.bytes) continue;
+    int s = 0;
+    for (int i = 1; i < n; ++i)
+      if (load[i] < load[s]) s = i;
+    load[s] += cp.bytes;
+    check_cuda(cudaMemcpyAsync(cp.dst, cp.src, cp.bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
+                               c.copy_streams[first + s]),
+               to_device ? "cudaMemcpyAsync H2D" : "cudaMemcpyAsync D2H");
+  }
+  cudaStream_t lead = c.copy_streams[first];
+  for (int i = 1; i < n; ++i) {
+    FencePtr f = record_fence(c, c.copy_streams[first + i]);
+    check_cuda(cudaStreamWaitEvent(lead, f->ev, 0), "cudaStreamWaitEvent");
+  }
+  for (int i = 0; i < n; ++i) c.copy_dirty[first + i] = true;
+  return fence_handle(c, record_fence(c, lead));
+}
+
 void batch_launch_each(Context &c, Batch &b, cudaStream_t s) {
   for (size_t p = 0; p < b.sid.size(); ++p) {
     if (b.length[p] == 0) continue;
@@ -2535,6 +2696,7 @@ int cc_batch_bind(cc_handle batch, const uint64_t *ptrs, size_t n_ptrs) {
   b.total_tiles = tiles;
   b.bound = true;
   batch_drop_graph(b);
+  batch_drop_copy_tables(c, b);
   CC_API_END
 }
 
@@ -2590,6 +2752,67 @@ int cc_batch_run(cc_handle batch, int mode, uint64_t stream) {
   CC_API_END
 }
 
+int cc_batch_run_ev(cc_handle batch, int mode, const cc_handle *wait, int n_wait, cc_handle *event) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  batch_of(c, batch);
+  for (int i = 0; i < n_wait; ++i) event_of(c, wait[i]);  // every handle valid before anything is enqueued
+  end_pdl_chain(c);
+  wait_events(c, c.stream, wait, n_wait);
+  const int r = cc_batch_run(batch, mode, 0);
+  if (r != CC_OK) return r;
+  if (event) *event = fence_handle(c, record_fence(c, c.stream));
+  CC_API_END
+}
+
+int cc_batch_upload_ev(cc_handle batch, const void *const *hosts, size_t n_hosts, const cc_handle *wait, int n_wait,
+                       cc_handle *event) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Batch &b = batch_of(c, batch);
+  if (!b.bound) fail(CC_ERR_INVALID_OPERATION, "bind the batch's buffers first");
+  size_t need = 0;
+  for (size_t p = 0; p < b.sid.size(); ++p) need += b.n_inputs[p];
+  if (!hosts || n_hosts != need)
+    fail(CC_ERR_INVALID_VALUE, "the batch has " + std::to_string(need) + " inputs, got " + std::to_string(n_hosts) +
+                                   " host pointers");
+  for (int i = 0; i < n_wait; ++i) event_of(c, wait[i]);
+  std::vector<BatchCopy> copies;
+  size_t k = 0;
+  for (size_t p = 0; p < b.sid.size(); ++p)
+    for (int i = 0; i < b.n_inputs[p]; ++i, ++k) {
+      const size_t bytes = (size_t)b.length[p] * sizeof(float);
+      if (bytes && !hosts[k]) fail(CC_ERR_INVALID_VALUE, "null host pointer");
+      copies.push_back({reinterpret_cast<void *>(b.ptrs[p][i]), hosts[k], bytes});
+    }
+  end_pdl_chain(c);  // the context stream's generated kernels do not see these writes as their own
+  *event = batch_copies(c, b, copies, true, wait, n_wait);
+  CC_API_END
+}
+
+int cc_batch_download_ev(cc_handle batch, void *const *hosts, size_t n_hosts, const cc_handle *wait, int n_wait,
+                         cc_handle *event) {
+  CC_API_BEGIN
+  Context &c = ctx();
+  std::lock_guard<std::recursive_mutex> g(c.mu);
+  Batch &b = batch_of(c, batch);
+  if (!b.bound) fail(CC_ERR_INVALID_OPERATION, "bind the batch's buffers first");
+  if (!hosts || n_hosts != b.sid.size())
+    fail(CC_ERR_INVALID_VALUE, "the batch has " + std::to_string(b.sid.size()) + " outputs, got " +
+                                   std::to_string(n_hosts) + " host pointers");
+  for (int i = 0; i < n_wait; ++i) event_of(c, wait[i]);
+  std::vector<BatchCopy> copies;
+  for (size_t p = 0; p < b.sid.size(); ++p) {
+    const size_t bytes = (size_t)b.length[p] * sizeof(float);
+    if (bytes && !hosts[p]) fail(CC_ERR_INVALID_VALUE, "null host pointer");
+    copies.push_back({hosts[p], reinterpret_cast<const void *>(b.ptrs[p][b.n_inputs[p]]), bytes});
+  }
+  *event = batch_copies(c, b, copies, false, wait, n_wait);
+  CC_API_END
+}
+
 int cc_batch_release(cc_handle batch) {
   CC_API_BEGIN
   Context &c = ctx();
@@ -2597,6 +2820,7 @@ int cc_batch_release(cc_handle batch) {
   Batch &b = batch_of(c, batch);
   check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize");
   batch_drop_graph(b);
+  batch_drop_copy_tables(c, b);
   if (b.table) release_block(c, b.table, b.table_cls);
   g_drv.ModuleUnload(b.module);
   delete &b;

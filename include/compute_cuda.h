@@ -313,6 +313,27 @@ int cc_batch_info(cc_handle batch, int *n_programs, int *n_structures, int *regi
 /* ptrs: for each program, its inputs in parameter order, then its output (16-byte aligned). */
 int cc_batch_bind(cc_handle batch, const uint64_t *ptrs, size_t n_ptrs);
 int cc_batch_run(cc_handle batch, int mode, uint64_t stream);
+/* The batch with host transfers in the event model of the launch API
+ * (Kernel.enqueue with waitingEvents, OpenCL.scala:787-844; enqueueWriteBuffer /
+ * enqueueReadBuffer with wait lists, OpenCL.scala:1206-1244, 1415-1431): each
+ * call waits for exactly its wait list and returns an event (release it with
+ * cc_event_release).
+ *   cc_batch_upload_ev: every bound input from pinned host memory; hosts: for
+ *     each program its inputs in parameter order (length of the program floats
+ *     each); copies spread over four copy streams.
+ *   cc_batch_run_ev: cc_batch_run on the context stream after the wait list.
+ *   cc_batch_download_ev: every program's output into hosts[p] (pinned), on four
+ *     other copy streams, so the reads of one step overlap the uploads of the
+ *     next when their wait lists allow it (uploads after the previous run; the
+ *     next run after these reads and the new uploads).
+ * The copies are ordered by their wait lists only: a caller that writes a bound
+ * buffer otherwise must wait for the events itself.  cc_synchronize waits for
+ * them too, and a buffer released meanwhile returns to the pool after them. */
+int cc_batch_upload_ev(cc_handle batch, const void *const *hosts, size_t n_hosts, const cc_handle *wait, int n_wait,
+                       cc_handle *event);
+int cc_batch_run_ev(cc_handle batch, int mode, const cc_handle *wait, int n_wait, cc_handle *event);
+int cc_batch_download_ev(cc_handle batch, void *const *hosts, size_t n_hosts, const cc_handle *wait, int n_wait,
+                         cc_handle *event);
 int cc_batch_release(cc_handle batch);
 /* GPU-free: generates and NVRTC-compiles a batch module for sm_<cc_major><cc_minor>a. */
 int cc_batch_compile_check(const char *const *irs, const size_t *ir_lens, int n_programs, int cc_major, int cc_minor,

@@ -78,3 +78,88 @@ def test_batch_rejects_programs_with_views(cuda_device):
     with pytest.raises(InvalidProgram):
         Batch(cuda_device, [a.transpose() * T.fill(2.0, [8, 64])])
     a.close()
+
+
+@pytest.mark.parametrize("copy_kernel", [1, 0])
+def test_batch_transfers_in_the_event_model(cuda_device, copy_kernel):
+    """Three steps in flight: each uploads its own inputs, runs after them and
+    the previous step's reads, and reads into its own host buffers; every step's
+    outputs are the bits of the same step run one call at a time.  The copies
+    go through one SM kernel over a copy table (copy_kernel 1) or the DMA engines."""
+    import ctypes
+    import bench
+    from compute._native import call
+    from compute.batch import Batch
+    rt = cuda_device.runtime
+    T = cuda_device.Tensor
+    saved = rt.config_get("batch_copy_kernel")
+    rt.config_set("batch_copy_kernel", copy_kernel)
+    progs = bench.c4_programs(T, seed=21, count=20, lo=1, hi=60000)
+    b = Batch(cuda_device, [t for t, _ in progs]).bind()
+    lengths = [int(np.prod(t.shape)) for t, _ in progs]
+    # the bound inputs: per program, its parameters in the order the program numbers them
+    in_lengths = [n for ser, n in zip(b.serialized, lengths) for _ in ser.params]
+    in_bufs = [prm._cached for ser in b.serialized for prm in ser.params]
+    pinned = []
+
+    def host(n):
+        p = ctypes.c_void_p()
+        call("cc_host_alloc", ctypes.c_size_t(max(1, 4 * n)), ctypes.byref(p))
+        pinned.append(p)
+        return p.value, np.ctypeslib.as_array((ctypes.c_float * max(1, n)).from_address(p.value))[:n]
+
+    r = np.random.RandomState(5)
+    steps = 3
+    hin = [[host(n) for n in in_lengths] for _ in range(steps)]
+    hout = [[host(n) for n in lengths] for _ in range(steps)]
+    for k in range(steps):
+        for _, arr in hin[k]:
+            arr[:] = r.uniform(0.1, 2.0, arr.size).astype(np.float32)
+    try:
+        # one call at a time: blocking uploads, a run, blocking reads
+        want = []
+        for k in range(steps):
+            for (_, arr), buf in zip(hin[k], in_bufs):
+                rt.upload(buf, arr)
+            b.run()
+            want.append([rt.download(o, n) for o, n in zip(b.outputs, lengths)])
+        for k in range(steps):  # the outputs are overwritten before the pipelined run reads them
+            for _, arr in hout[k]:
+                arr[:] = np.nan
+        events, prev_run, prev_read = [], None, None
+        for k in range(steps):
+            up = b.upload_ev([p for p, _ in hin[k]], wait=[prev_run] if prev_run else [])
+            run = b.run_ev(0, wait=[up] + ([prev_read] if prev_read else []))
+            read = b.download_ev([p for p, _ in hout[k]], wait=[run])
+            events += [up, run, read]
+            prev_run, prev_read = run, read
+        rt.event_wait(prev_read, 60 * 10 ** 9)
+        rt.synchronize()
+        for e in events:
+            rt.event_release(e)
+        for k in range(steps):
+            for p, ((_, got), exp) in enumerate(zip(hout[k], want[k])):
+                assert np.array_equal(got.view(np.int32), exp.view(np.int32)), (k, p)
+    finally:
+        rt.synchronize()
+        rt.config_set("batch_copy_kernel", saved)
+        for p in pinned:
+            call("cc_host_free", p)
+        b.close()
+        for _, inputs in progs:
+            for i in inputs:
+                i.close()
+
+
+def test_batch_event_calls_check_their_arguments(cuda_device):
+    from compute._native import InvalidValue
+    from compute.batch import Batch
+    T = cuda_device.Tensor
+    a = T.random([64], seed=1).doCache()
+    b = Batch(cuda_device, [a * a, a + a]).bind()
+    with pytest.raises(InvalidValue):
+        b.upload_ev([0])  # two inputs (one per program), one pointer
+    with pytest.raises(InvalidValue):
+        b.download_ev([0, 0, 0])
+    b.close()
+    a.close()
