@@ -438,16 +438,16 @@ def keep_busy(rt, st, seconds):
         rt.synchronize()
 
 
-def time_e2e(d, st, steps, pipelined=True):
+def time_e2e(d, st, steps, pipelined=True, depth=2):
     """Host buffers in, result out, through the C ABI, every step: upload the
     inputs from pinned host memory, launch, read the result back.
 
-    pipelined: two steps in flight through the event API (cc_buf_upload_ev,
+    pipelined: `depth` steps in flight through the event API (cc_buf_upload_ev,
     cc_launch_ev, cc_buf_download_ev: the reference's enqueue with wait lists),
     each on its own device buffers, the host waiting for a step's result before
-    issuing the step two later; else one step at a time (non-blocking uploads,
-    launch, blocking read).  Returns (seconds per step, H2D bytes, D2H bytes,
-    whether every result read back has the bits of a launch on the inputs)."""
+    issuing the step `depth` later; else one step at a time (non-blocking
+    uploads, launch, blocking read).  Returns (seconds per step, H2D bytes, D2H
+    bytes, whether every result read back has the bits of a launch on the inputs)."""
     import ctypes
     import numpy as np
     from compute._native import call
@@ -465,7 +465,7 @@ def time_e2e(d, st, steps, pipelined=True):
     out = st["out"]
     out_elems = st["prog"].out_elems
     d2h = 4 * max(1, out_elems)
-    depth = 2 if pipelined else 1
+    depth = depth if pipelined else 1
     results = []  # the results land in pinned host memory too
     for _ in range(depth):
         res = ctypes.c_void_p()
@@ -540,23 +540,77 @@ def time_e2e(d, st, steps, pipelined=True):
     return dt, h2d, d2h, match
 
 
+_LINK = {}
+
+
+def link_rates(d, nbytes=64 << 20, reps=8):
+    """The host link's copy rates through the C ABI (pinned host memory of
+    cc_host_alloc, cc_buf_upload_async / cc_buf_download_async of nbytes, reps
+    back to back, one cc_synchronize), in GB/s; measured once per process."""
+    if _LINK:
+        return _LINK
+    import ctypes
+    from compute._native import call
+    rt = d.runtime
+    buf = rt.alloc(nbytes)
+    ptr = ctypes.c_void_p()
+    call("cc_host_alloc", ctypes.c_size_t(nbytes), ctypes.byref(ptr))
+    try:
+        ctypes.memset(ptr, 0, nbytes)
+        for name, fn in (("h2d_gbs", "cc_buf_upload_async"), ("d2h_gbs", "cc_buf_download_async")):
+            best = None
+            for _ in range(3):
+                call(fn, ctypes.c_uint64(buf.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(nbytes))
+                call("cc_synchronize")
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    call(fn, ctypes.c_uint64(buf.handle), ctypes.c_size_t(0), ptr, ctypes.c_size_t(nbytes))
+                call("cc_synchronize")
+                dt = time.perf_counter() - t0
+                best = dt if best is None else min(best, dt)
+            _LINK[name] = nbytes * reps / best / 1e9
+    finally:
+        call("cc_host_free", ptr)
+        buf.release()
+    _LINK["how"] = "%d MB copies from/to pinned host memory, %d back to back, best of 3" % (nbytes >> 20, reps)
+    return _LINK
+
+
+def with_link_bound(d, e2e):
+    """Adds the host link's bound to an e2e record: the time the step's copies
+    take at the link's measured rates (each direction alone, the two overlapping),
+    and the step's fraction of it."""
+    if not e2e or not e2e.get("ms_per_step"):
+        return e2e
+    rates = link_rates(d)
+    t_h2d = e2e["h2d_bytes_per_step"] / (rates["h2d_gbs"] * 1e9)
+    t_d2h = e2e["d2h_bytes_per_step"] / (rates["d2h_gbs"] * 1e9)
+    bound_ms = max(t_h2d, t_d2h) * 1e3
+    e2e["link"] = {"h2d_gbs": rates["h2d_gbs"], "d2h_gbs": rates["d2h_gbs"], "how": rates["how"],
+                   "bound_ms_per_step": bound_ms, "frac": bound_ms / e2e["ms_per_step"],
+                   "note": "bound = the step's host->device bytes at the measured H2D rate, or its device->host "
+                           "bytes at the D2H rate, whichever is longer (the two directions overlapping)"}
+    return e2e
+
+
 def e2e_record(d, st, steps, work, unit):
-    """The e2e record: the step timed both ways (two steps in flight through
+    """The e2e record: the step timed both ways (three steps in flight through
     the event API, and one step at a time), `work` units per step; the value is
     the faster way's, and the record names it and carries both."""
-    dt_p, h2d, d2h, match_p = time_e2e(d, st, steps=steps)
+    dt_p, h2d, d2h, match_p = time_e2e(d, st, steps=steps, depth=3)
     dt_b, _, _, match_b = time_e2e(d, st, steps=steps, pipelined=False)
-    modes = {"two_in_flight": {"value": work / dt_p, "unit": unit, "ms_per_step": dt_p * 1e3,
-                               "how": "cc_buf_upload_ev, cc_launch_ev, cc_buf_download_ev with wait lists, two "
-                                      "steps in flight on their own device buffers"},
+    modes = {"three_in_flight": {"value": work / dt_p, "unit": unit, "ms_per_step": dt_p * 1e3,
+                                 "how": "cc_buf_upload_ev, cc_launch_ev, cc_buf_download_ev with wait lists, three "
+                                        "steps in flight on their own device buffers"},
              "one_at_a_time": {"value": work / dt_b, "unit": unit, "ms_per_step": dt_b * 1e3,
                                "how": "cc_buf_upload_async, cc_launch, blocking cc_buf_download"}}
     best = min(modes, key=lambda k: modes[k]["ms_per_step"])
-    return {"value": modes[best]["value"], "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "ms_per_step": modes[best]["ms_per_step"], "mode": best, "modes": modes,
-            "note": "every step uploads its inputs from pinned host memory and reads its result back inside the "
-                    "timed region",
-            "results_match": bool(match_p and match_b)}
+    return with_link_bound(d, {
+        "value": modes[best]["value"], "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+        "ms_per_step": modes[best]["ms_per_step"], "mode": best, "modes": modes,
+        "note": "every step uploads its inputs from pinned host memory and reads its result back inside the "
+                "timed region",
+        "results_match": bool(match_p and match_b)})
 
 
 def time_e2e_batch(d, b, progs, nbytes, steps):
@@ -655,11 +709,12 @@ def time_e2e_batch(d, b, progs, nbytes, steps):
                                "how": "cc_buf_upload_async per input, cc_batch_run, cc_buf_download_async per "
                                       "output, cc_synchronize"}}
     best = min(modes, key=lambda k: modes[k]["ms_per_step"])
-    return {"value": modes[best]["value"], "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "ms_per_step": modes[best]["ms_per_step"], "mode": best, "modes": modes,
-            "note": "every step uploads its inputs from pinned host memory and reads every output back inside "
-                    "the timed region",
-            "results_match": bool(match)}
+    return with_link_bound(d, {
+        "value": modes[best]["value"], "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+        "ms_per_step": modes[best]["ms_per_step"], "mode": best, "modes": modes,
+        "note": "every step uploads its inputs from pinned host memory and reads every output back inside "
+                "the timed region",
+        "results_match": bool(match)})
 
 
 _KNOBS = []
@@ -1176,7 +1231,7 @@ def measure_contraction(d, workload, steps, warmup, local_rank=0, e2e_on=True, c
         extras = contraction_extras(d, st)
         e2e = None
         if e2e_on:
-            e2e = e2e_record(d, st, 3, st["flops"] / 1e12, "TFLOP/s")
+            e2e = e2e_record(d, st, max(3, min(steps, 12)), st["flops"] / 1e12, "TFLOP/s")
     finally:
         release(st)
         rt.config_set("contraction", saved)

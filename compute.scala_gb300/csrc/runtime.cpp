@@ -362,6 +362,7 @@ constexpr int kBatchRegistersDefault = 64;
 constexpr int kBatchLoadsDefault = 4;
 constexpr int kBatchLanesDefault = 4;
 constexpr int kBatchRolledDefault = 1;
+constexpr int kBatchPrefetchDefault = 0;
 
 struct Context {
   int device = 0;
@@ -411,6 +412,7 @@ struct Context {
   int batch_max_loads = kBatchLoadsDefault;         // float4 loads a tile function keeps in flight per thread
   int batch_lanes = kBatchLanesDefault;             // points a tile function evaluates together (0: one)
   int batch_rolled = kBatchRolledDefault;           // a tile's load groups in a loop (1) or unrolled (0)
+  int batch_prefetch = kBatchPrefetchDefault;       // L2 bulk prefetch of a run's later tiles (1), and of the next run (2)
   int tuner = 0;  // 0 off, 1 exhaustive, 2 learned
   int ew_smem_ring = 0;  // generic kernels: shared-memory ring slots per thread for staged loads
   int ew_points = 1;     // generic elementwise kernels: consecutive points per thread
@@ -1182,6 +1184,9 @@ int cc_config_set(const char *key, int64_t value) {
   } else if (k == "batch_rolled") {
     if (value != 0 && value != 1) fail(CC_ERR_INVALID_VALUE, "batch_rolled must be 0 or 1");
     c.batch_rolled = (int)value;
+  } else if (k == "batch_prefetch") {
+    if (value < 0 || value > 2) fail(CC_ERR_INVALID_VALUE, "batch_prefetch must be 0, 1 or 2");
+    c.batch_prefetch = (int)value;
   } else if (k == "batch_lanes") {
     if (value != 0 && value != 4 && value != 8) fail(CC_ERR_INVALID_VALUE, "batch_lanes must be 0, 4 or 8");
     c.batch_lanes = (int)value;
@@ -1231,6 +1236,7 @@ int cc_config_get(const char *key, int64_t *value) {
   else if (k == "batch_inline") *value = c.batch_inline;
   else if (k == "batch_lanes") *value = c.batch_lanes;
   else if (k == "batch_rolled") *value = c.batch_rolled;
+  else if (k == "batch_prefetch") *value = c.batch_prefetch;
   else if (k == "batch_copy_kernel") *value = c.batch_copy_kernel;
   else if (k == "tuner") *value = c.tuner;
   else if (k == "ew_smem_ring") *value = c.ew_smem_ring;
@@ -2175,6 +2181,12 @@ __device__ __forceinline__ cc_f8 cc_min(cc_f8 a, cc_f8 b) { return cc_pair(cc_mi
 __device__ __forceinline__ cc_f8 cc_max(cc_f8 a, cc_f8 b) { return cc_pair(cc_max(a.lo, b.lo), cc_max(a.hi, b.hi)); }
 )";
 
+// L2 bulk prefetch of [p, p + bytes): p 16-byte aligned, bytes a multiple of 16.
+const char *kBatchPrefetchPrelude =
+    "static __device__ __forceinline__ void cc_l2_prefetch(const float *p, unsigned bytes) {\n"
+    "  asm volatile(\"cp.async.bulk.prefetch.L2.global [%0], %1;\" ::\"l\"(p), \"r\"(bytes) : \"memory\");\n"
+    "}\n";
+
 // exp, log and tanh over one lane and over four: called functions (shared by
 // every structure of the part) below inline level 2, else inlined.
 std::string batch_lane_transcendentals(int inline_level) {
@@ -2194,10 +2206,12 @@ std::string batch_lane_transcendentals(int inline_level) {
 }
 
 std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs, size_t first,
-                               size_t last, int inline_level, int max_loads, int lane_width, bool rolled) {
+                               size_t last, int inline_level, int max_loads, int lane_width, bool rolled,
+                               int prefetch) {
   const bool lanes = lane_width > 0;
   std::ostringstream o;
   o << "// generated batch part for sm_103a\n"
+    << kBatchPrefetchPrelude
     << "static __device__ __noinline__ float cc_expf(float x) { return expf(x); }\n"
        "static __device__ __noinline__ float cc_logf(float x) { return logf(x); }\n"
        "static __device__ __noinline__ float cc_tanhf(float x) { return tanhf(x); }\n";
@@ -2238,8 +2252,21 @@ std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector
     const int min_group = lane_width == 8 ? 2 : 1;
     int group = kBatchUnroll;
     while (group > min_group && nin * group > max_loads) group /= 2;
-    o << "extern \"C\" __device__ __noinline__ void cc_tile_" << S << kTileParams << " {\n"
-      << "  for (; count > 0; --count, base += " << kBatchTile << "LL) {\n"
+    o << "extern \"C\" __device__ __noinline__ void cc_tile_" << S << kTileParams << " {\n";
+    // prefetch: one thread asks L2 for the run's later tiles of every input
+    // (one bulk prefetch per input) before the first tile's loads, so only
+    // the first tile of a run waits for DRAM
+    if (prefetch >= 1 && nin > 0) {
+      o << "  if (threadIdx.x == 0 && count > 1) {\n"
+        << "    const long long ps = base + " << kBatchTile << "LL;\n"
+        << "    long long pe = base + (long long)count * " << kBatchTile << "LL;\n"
+        << "    if (pe > n) pe = n;\n"
+        << "    if (pe - ps >= 4) {\n"
+        << "      const unsigned bytes = (unsigned)(((pe - ps) & ~3LL) * 4);\n";
+      for (int i = 0; i < nin; ++i) o << "      cc_l2_prefetch(in" << i << " + ps, bytes);\n";
+      o << "    }\n  }\n";
+    }
+    o << "  for (; count > 0; --count, base += " << kBatchTile << "LL) {\n"
       << "  if (base + " << kBatchTile << "LL <= n) {\n"
       << "    const long long q0 = (base >> 2) + threadIdx.x;\n";
     // rolled: one copy of the group's code in a loop over the groups (a
@@ -2304,9 +2331,10 @@ std::string batch_chunk_source(const std::vector<Ir> &structs, const std::vector
   return o.str();
 }
 
-std::string batch_main_source(size_t n_structs) {
+std::string batch_main_source(size_t n_structs, int prefetch) {
   std::ostringstream o;
   o << "// generated batch main part for sm_103a\n"
+    << kBatchPrefetchPrelude
     << "struct cc_entry { const float *in[4]; float *out; long long n; long long tile_begin; int sid; int pad; };\n"
     << "typedef void (*cc_tile_fn)" << kTileParams << ";\n";
   for (size_t s = 0; s < n_structs; ++s) o << "extern \"C\" __device__ void cc_tile_" << s << kTileParams << ";\n";
@@ -2321,11 +2349,42 @@ std::string batch_main_source(size_t n_structs) {
     << "                unsigned long long *__restrict__ work, int run) {\n"
     << "  extern __shared__ long long s_begin[];\n"
     << "  __shared__ long long s_run;\n"
-    << "  for (int i = threadIdx.x; i < nprog; i += blockDim.x) s_begin[i] = table[i].tile_begin;\n"
-    << "  for (;;) {\n"
-    << "    __syncthreads();\n"
-    << "    if (threadIdx.x == 0) s_run = (long long)atomicAdd(work, (unsigned long long)run);\n"
-    << "    __syncthreads();\n"
+    << "  for (int i = threadIdx.x; i < nprog; i += blockDim.x) s_begin[i] = table[i].tile_begin;\n";
+  if (prefetch >= 2) {
+    // The block claims its next run one run ahead and, while it works on the
+    // current one, L2 prefetches the next run's first tile (the tile
+    // functions prefetch the later tiles of a run themselves).
+    o << "  __shared__ long long s_next;\n"
+      << "  if (threadIdx.x == 0) s_next = (long long)atomicAdd(work, (unsigned long long)run);\n"
+      << "  for (;;) {\n"
+      << "    __syncthreads();\n"
+      << "    if (threadIdx.x == 0) {\n"
+      << "      s_run = s_next;\n"
+      << "      const long long tn = s_run < total_tiles ? (long long)atomicAdd(work, (unsigned long long)run) : total_tiles;\n"
+      << "      s_next = tn;\n"
+      << "      if (tn < total_tiles) {\n"
+      << "        int a = 0, z = nprog - 1;\n"
+      << "        while (a < z) {\n          const int m = (a + z + 1) >> 1;\n"
+      << "          if (s_begin[m] <= tn) a = m; else z = m - 1;\n        }\n"
+      << "        const cc_entry &f = table[a];\n"
+      << "        const long long b0 = (tn - f.tile_begin) * " << kBatchTile << "LL;\n"
+      << "        long long b1 = b0 + " << kBatchTile << "LL;\n"
+      << "        if (b1 > f.n) b1 = f.n;\n"
+      << "        if (b1 - b0 >= 4) {\n"
+      << "          const unsigned bytes = (unsigned)(((b1 - b0) & ~3LL) * 4);\n"
+      << "          for (int k = 0; k < 4; ++k)\n"
+      << "            if (f.in[k]) cc_l2_prefetch(f.in[k] + b0, bytes);\n"
+      << "        }\n"
+      << "      }\n"
+      << "    }\n"
+      << "    __syncthreads();\n";
+  } else {
+    o << "  for (;;) {\n"
+      << "    __syncthreads();\n"
+      << "    if (threadIdx.x == 0) s_run = (long long)atomicAdd(work, (unsigned long long)run);\n"
+      << "    __syncthreads();\n";
+  }
+  o
     << "    const long long t0 = s_run;\n"
     << "    if (t0 >= total_tiles) break;\n"
     << "    const long long t1 = t0 + run < total_tiles ? t0 + run : total_tiles;\n"
@@ -2377,14 +2436,15 @@ std::vector<std::vector<char>> compile_parallel(const std::vector<std::string> &
 // Compiles the parts in parallel and links them into one loadable image.
 std::vector<char> build_batch_image(const std::vector<Ir> &structs, const std::vector<int> &struct_inputs,
                                     int cc_major, int cc_minor, uint32_t flags, bool link, int inline_level,
-                                    int max_registers, int max_loads, int lane_width, bool rolled) {
+                                    int max_registers, int max_loads, int lane_width, bool rolled,
+                                    int prefetch) {
   std::vector<std::string> sources;
   FmaScope fma_scope((flags & CC_FLAG_FMA_CONTRACT) != 0);
   for (size_t first = 0; first < structs.size(); first += kBatchChunk)
     sources.push_back(batch_chunk_source(structs, struct_inputs, first,
                                          std::min(structs.size(), first + (size_t)kBatchChunk), inline_level,
-                                         max_loads, lane_width, rolled));
-  sources.push_back(batch_main_source(structs.size()));
+                                         max_loads, lane_width, rolled, prefetch));
+  sources.push_back(batch_main_source(structs.size(), prefetch));
   std::vector<std::vector<char>> parts = compile_parallel(sources, cc_major, cc_minor, flags, true, max_registers);
   if (!link) return {};
   CUlinkState state;
@@ -2598,7 +2658,8 @@ int cc_batch_create(const char *const *irs, const size_t *lens, int n_programs, 
   {
     std::lock_guard<std::mutex> cg(c.compile_mu);
     cubin = build_batch_image(structs, struct_inputs, c.cc_major, c.cc_minor, c.flags, true, c.batch_inline,
-                              c.batch_max_registers, c.batch_max_loads, c.batch_lanes, c.batch_rolled != 0);
+                              c.batch_max_registers, c.batch_max_loads, c.batch_lanes, c.batch_rolled != 0,
+                              c.batch_prefetch);
   }
   check_cu(g_drv.ModuleLoadData(&b->module, cubin.data()), "cuModuleLoadData");
   check_cu(g_drv.ModuleGetFunction(&b->persistent, b->module, "cc_batch"), "cuModuleGetFunction");
@@ -2641,7 +2702,7 @@ int cc_batch_compile_check(const char *const *irs, const size_t *lens, int n_pro
   auto t0 = std::chrono::steady_clock::now();
   // a context's default settings; linking needs a driver
   build_batch_image(structs, struct_inputs, cc_major, cc_minor, 0, false, kBatchInlineDefault, kBatchRegistersDefault,
-                    kBatchLoadsDefault, kBatchLanesDefault, kBatchRolledDefault != 0);
+                    kBatchLoadsDefault, kBatchLanesDefault, kBatchRolledDefault != 0, kBatchPrefetchDefault);
   if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (n_structures) *n_structures = (int)structs.size();
   CC_API_END

@@ -133,6 +133,9 @@ int cc_synchronize(void);
  *                       default 4); programs with more inputs load their four positions per input in groups
  *   "batch_rolled"      batch tile functions: 1 = the load groups of a tile run in a loop over one copy of
  *                       the group's code (default), 0 = one copy per group
+ *   "batch_prefetch"    persistent batch kernel: 1 = a tile function asks L2 for the later tiles of its run
+ *                       (one bulk prefetch per input) before loading the first; 2 = also, a block claims
+ *                       its next run one run ahead and prefetches that run's first tile (default 0)
  *   "batch_lanes"       points a batch tile function evaluates per expression call: 4 = a float4's four
  *                       (default; a called exp/log/tanh computes four values), 8 = two float4s, 0 = one
  *                       point per call.  Every setting gives the same bits.

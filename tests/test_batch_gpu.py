@@ -70,6 +70,39 @@ def test_batch_lane_widths_give_the_single_launch_bits(cuda_device, lanes, inlin
                 i.close()
 
 
+@pytest.mark.parametrize("prefetch,run", [(1, 4), (2, 4), (2, 3), (1, 16)])
+def test_batch_l2_prefetch_keeps_the_bits(cuda_device, prefetch, run):
+    """The L2 bulk prefetches of a run's later tiles and of a block's next run
+    (whose tiles may start in another program, or past the last one) change no
+    result: every program's output is the single launch's, bit for bit."""
+    import bench
+    from compute.batch import Batch
+    rt = cuda_device.runtime
+    T = cuda_device.Tensor
+    saved = {k: rt.config_get(k) for k in ("batch_prefetch", "batch_run_tiles")}
+    progs = bench.c4_programs(T, seed=17, count=32, lo=1, hi=60000)
+    tensors = [t for t, _ in progs]
+    single = [t.flatArray() for t in tensors]
+    try:
+        rt.config_set("batch_prefetch", prefetch)
+        rt.config_set("batch_run_tiles", run)
+        b = Batch(cuda_device, tensors).bind()
+        for _ in range(2):
+            for out in b.outputs:
+                rt.upload(out, np.full(out.nbytes // 4, np.nan, np.float32))
+            b.run(Batch.PERSISTENT)
+            for k, want in enumerate(single):
+                got = rt.download(b.outputs[k], want.size)
+                assert np.array_equal(got.view(np.int32), want.view(np.int32)), k
+        b.close()
+    finally:
+        for k, v in saved.items():
+            rt.config_set(k, v)
+        for _, inputs in progs:
+            for i in inputs:
+                i.close()
+
+
 def test_batch_rejects_programs_with_views(cuda_device):
     from compute._native import InvalidProgram
     from compute.batch import Batch
