@@ -320,8 +320,10 @@ struct Event {
 
 // The queue pool: streams that the *_ev entry points spread independent work
 // over, as the reference's CommandQueuePool spreads it over command queues
-// (OpenCL.scala:423-448, 5 per device).
-constexpr int kQueues = 5;
+// (OpenCL.scala:423-448, 5 per device).  Streams are cheap, and every queue
+// is in order, so a larger pool puts fewer unrelated operations behind one
+// another: eight.
+constexpr int kQueues = 8;
 
 // Many independent programs evaluated together (cc_batch_*).
 struct Batch {
@@ -529,10 +531,25 @@ void enter_multi_queue(Context &c) {
   c.multi_queue = true;
 }
 
-// The next queue, round robin (the reference's dispatch takes one from its pool).
+// A queue for the next operation (the reference's dispatch takes one from its
+// pool): the first idle one from the round-robin position on, so that an
+// operation whose wait list is already satisfied does not queue behind
+// unrelated work still in flight; round robin when every queue is busy.
 int pick_queue(Context &c) {
   enter_multi_queue(c);
-  const int q = c.next_queue;
+  int q = c.next_queue;
+  for (int i = 0; i < kQueues; ++i) {
+    const int k = (c.next_queue + i) % kQueues;
+    const cudaError_t r = cudaStreamQuery(c.queues[k]);
+    if (r == cudaSuccess) {
+      q = k;
+      break;
+    }
+    if (r != cudaErrorNotReady) {
+      cudaGetLastError();
+      break;
+    }
+  }
   c.next_queue = (q + 1) % kQueues;
   return q;
 }

@@ -224,7 +224,8 @@ int cc_launch_ptrs(cc_handle program, const uint64_t *input_ptrs, int n_inputs, 
  *      and the non-blocking enqueueWriteBuffer / enqueueReadBuffer with their events (:1206-1244,
  *      :1415-1431), as CompiledKernel.run drives them: each kernel waits for the events of the
  *      buffers it reads (Tensors.scala:1331-1381, PendingBuffer / EventBuffer :253-299).
- *      Each call takes the next stream of a pool of five (round robin), makes it wait for every
+ *      Each call takes a stream of a pool of eight (the first idle one from a round-robin position,
+ *      else the next one round robin: each stream runs its work in order), makes it wait for every
  *      event of `wait` (n_wait of them; NULL when 0), enqueues its work there and, when `event` is
  *      not NULL, returns an event that completes with it (release it with cc_event_release; it
  *      has no timing, so cc_event_elapsed refuses it).  Work without a chain of events between it
