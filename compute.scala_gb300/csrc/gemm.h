@@ -29,11 +29,16 @@ constexpr int kTcBM = 128, kTcBN = 256, kTcBK = 32;
 // 2 = 128-column tiles, one pair per tile; 3 / 4 = as 0 with accumulators restarted
 // every 8 / 16 k-blocks; 5 = 256-column tiles, hi*hi restarted every 8 k-blocks and
 // the small products over the whole K, a partial last round in column halves.
-// gemm_tc_box_n: the tile width.
+// gemm_tc_variant: the kernel a variant runs for K_padded (a kernel that sums K
+// chunks in registers hands a K that fits one chunk to a one-pair-per-tile
+// kernel); the tensor maps and the launch both take the resolved variant.
+// gemm_tc_box_n: the tile width of a resolved variant.
+int gemm_tc_variant(int variant, int K_padded);
 int gemm_tc_box_n(int variant);
 // maps: A planes 0..2 (box 32 x 128), B^T planes 0..2 (box 32 x gemm_tc_box_n), the B^T planes
 // again with box 32 x gemm_tc_box_n / 2 (6..8: column halves of split tiles), 64-byte swizzle.
-// group_m: output tiles are visited in groups of this many tile rows (1 = row-major).
+// group_m: output tiles are visited in groups of this many tile rows (1 = row-major);
+// variant: as resolved by gemm_tc_variant (any other is rejected).
 cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
                                int sm_count, int *err, int variant, int group_m, cudaStream_t stream);
 

@@ -20,7 +20,9 @@
 //               "empty" mbarrier and, after a tile's last stage, to the
 //               accumulator pair's "full";
 //   warps 2..5  epilogue: tcgen05.ld both accumulators (each warp reads its own
-//               32-lane quarter of TMEM), add, store to C, release the pair;
+//               32-lane quarter of TMEM, in the 16x256b shape so that four
+//               threads hold 32 consecutive bytes of a row and every store
+//               fills whole sectors), add, store to C, release the pair;
 //               kernels that sum K chunks in registers have a second group,
 //               warps 6..9, and each group takes half of the columns.
 // With one accumulator pair of 256 columns (TMEM holds no second pair) and K
@@ -164,34 +166,52 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+// 32 columns of the 32 TMEM lanes of this warp's subpartition, read as two
+// 16x256b.x4 loads (lanes 0-15, then 16-31).  Thread t receives, for h = 0, 1 and
+// k = 0..3: v[16h + 4k + {0,1}] = lane 16h + t/4, columns 8k + 2(t%4) + {0,1};
+// v[16h + 4k + {2,3}] = lane 16h + t/4 + 8, the same columns.  Four threads hold
+// 32 consecutive bytes of a row, so the stores below fill whole 32-byte sectors.
+__device__ __forceinline__ void tmem_ld_block32(uint32_t taddr, float (&v)[32]) {
   uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+    asm volatile(
+        "tcgen05.ld.sync.aligned.16x256b.x4.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+        "[%16];"
+        : "=r"(r[16 * h + 0]), "=r"(r[16 * h + 1]), "=r"(r[16 * h + 2]), "=r"(r[16 * h + 3]), "=r"(r[16 * h + 4]),
+          "=r"(r[16 * h + 5]), "=r"(r[16 * h + 6]), "=r"(r[16 * h + 7]), "=r"(r[16 * h + 8]), "=r"(r[16 * h + 9]),
+          "=r"(r[16 * h + 10]), "=r"(r[16 * h + 11]), "=r"(r[16 * h + 12]), "=r"(r[16 * h + 13]),
+          "=r"(r[16 * h + 14]), "=r"(r[16 * h + 15])
+        : "r"(taddr + ((uint32_t)(16 * h) << 16)));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Stores 32 consecutive values of one output row (columns col0..col0+31, masked to N).
-__device__ __forceinline__ void store_row_chunk(float *crow, int row, int M, int N, long long ldc, int col0,
-                                                const float *v) {
-  if (row >= M) return;
-  if (col0 + 32 <= N && (ldc & 3) == 0 && ((reinterpret_cast<uintptr_t>(crow) & 15) == 0)) {
+// Stores a block read by tmem_ld_block32: row0 is the output row of the
+// subpartition's lane 0, col0 the block's first column (masked to M and N).
+// vec2: C and ldc allow 8-byte stores.
+__device__ __forceinline__ void store_block32(float *C, int row0, int col0, int M, int N, long long ldc, bool vec2,
+                                              const float *v) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int j = 0; j < 32; j += 4)
-      *reinterpret_cast<float4 *>(crow + col0 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-  } else {
+  for (int h = 0; h < 2; ++h)
 #pragma unroll
-    for (int j = 0; j < 32; ++j)
-      if (col0 + j < N) crow[col0 + j] = v[j];
-  }
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int row = row0 + 16 * h + (lane >> 2) + 8 * g;
+        const int col = col0 + 8 * k + 2 * (lane & 3);
+        const float a = v[16 * h + 4 * k + 2 * g], b = v[16 * h + 4 * k + 2 * g + 1];
+        if (row >= M) continue;
+        float *p = C + (long long)row * ldc + col;
+        if (vec2 && col + 1 < N) {
+          *reinterpret_cast<float2 *>(p) = make_float2(a, b);
+        } else {
+          if (col < N) p[0] = a;
+          if (col + 1 < N) p[1] = b;
+        }
+      }
 }
 
 // Origin of output tile `tile` in tile units.  Tiles are numbered in groups of
@@ -464,10 +484,11 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
   } else {
     // Epilogue: warp w reads TMEM lanes 32*(w%4) .. 32*(w%4)+31 (one row each).
     const int quarter = warp & 3;
-    const int row_in_tile = quarter * 32 + lane;
+    const int row_block = quarter * 32;  // the tile row of this subpartition's lane 0
     int acc = 0;
     uint32_t acc_phase = 0;
     const uint32_t lane_tmem = tmem_base + ((uint32_t)(quarter * 32) << 16);
+    const bool vec2 = (ldc & 1) == 0 && (reinterpret_cast<uintptr_t>(C) & 7) == 0;
     if constexpr (kLate) {
       // hi*hi per chunk into a running sum of the row; the small products once
       // per tile, added last.
@@ -495,7 +516,7 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
           for (int c32 = 0; c32 < kCols / 32; ++c32) {
             if (c32 * 32 >= cols) break;
             float v[32];
-            tmem_ld32(lane_tmem + (uint32_t)(col0 + c32 * 32), v);
+            tmem_ld_block32(lane_tmem + (uint32_t)(col0 + c32 * 32), v);
 #pragma unroll
             for (int j = 0; j < 32; ++j) sum[c32 * 32 + j] = __fadd_rn(sum[c32 * 32 + j], v[j]);
           }
@@ -506,16 +527,14 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
         if (!mbar_wait(bar_accfull, small_phase, abort_flag, err, 4)) break;
         small_phase ^= 1u;
         tc_fence_after();
-        const int row = m0 + row_in_tile;
-        float *crow = C + (long long)row * ldc;
 #pragma unroll
         for (int c32 = 0; c32 < kCols / 32; ++c32) {
           if (c32 * 32 >= cols) break;
           float w[32];
-          tmem_ld32(lane_tmem + (uint32_t)(BN + col0 + c32 * 32), w);
+          tmem_ld_block32(lane_tmem + (uint32_t)(BN + col0 + c32 * 32), w);
 #pragma unroll
           for (int j = 0; j < 32; ++j) w[j] = __fadd_rn(sum[c32 * 32 + j], w[j]);
-          store_row_chunk(crow, row, M, N, ldc, n0 + col0 + c32 * 32, w);
+          store_block32(C, m0 + row_block, n0 + col0 + c32 * 32, M, N, ldc, vec2, w);
         }
         tc_fence_before();
         mbar_arrive(bar_accempty);
@@ -528,17 +547,15 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
         int tm, tn;
         tile_origin(tile, num_tiles / tiles_n, tiles_n, group_m, tm, tn);
         const int m0 = tm * BM, n0 = tn * BN;
-        const int row = m0 + row_in_tile;
-        float *crow = C + (long long)row * ldc;
 #pragma unroll 1
         for (int chunk = 0; chunk < BN / 32; ++chunk) {
           float v[32], w[32];
           const uint32_t t = lane_tmem + (uint32_t)(acc * 2 * BN + chunk * 32);
-          tmem_ld32(t, v);
-          tmem_ld32(t + BN, w);
+          tmem_ld_block32(t, v);
+          tmem_ld_block32(t + BN, w);
 #pragma unroll
           for (int j = 0; j < 32; ++j) v[j] = __fadd_rn(v[j], w[j]);
-          store_row_chunk(crow, row, M, N, ldc, n0 + chunk * 32, v);
+          store_block32(C, m0 + row_block, n0 + chunk * 32, M, N, ldc, vec2, v);
         }
         tc_fence_before();
         mbar_arrive(bar_accempty + 8 * acc);
@@ -569,8 +586,8 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
           for (int c32 = 0; c32 < kCols / 32; ++c32) {
             float v[32], w[32];
             const uint32_t t = lane_tmem + (uint32_t)(acc * 2 * BN + col0 + c32 * 32);
-            tmem_ld32(t, v);
-            tmem_ld32(t + BN, w);
+            tmem_ld_block32(t, v);
+            tmem_ld_block32(t + BN, w);
 #pragma unroll
             for (int j = 0; j < 32; ++j) sum[c32 * 32 + j] = __fadd_rn(sum[c32 * 32 + j], __fadd_rn(v[j], w[j]));
           }
@@ -585,11 +602,9 @@ __global__ void __launch_bounds__(threads_for(KC), 1)
         int tm, tn;
         tile_origin(tile, num_tiles / tiles_n, tiles_n, group_m, tm, tn);
         const int m0 = tm * BM, n0 = tn * BN;
-        const int row = m0 + row_in_tile;
-        float *crow = C + (long long)row * ldc;
 #pragma unroll
         for (int c32 = 0; c32 < kCols / 32; ++c32)
-          store_row_chunk(crow, row, M, N, ldc, n0 + col0 + c32 * 32, sum + c32 * 32);
+          store_block32(C, m0 + row_block, n0 + col0 + c32 * 32, M, N, ldc, vec2, sum + c32 * 32);
       }
     }
   }
@@ -631,14 +646,23 @@ cudaError_t launch_variant(const CUtensorMap *maps, float *C, int M, int N, int 
 
 int gemm_tc_box_n(int variant) { return variant == 1 || variant == 5 ? 256 : 128; }
 
+int gemm_tc_variant(int variant, int K_padded) {
+  // When K fits in one chunk the running sum only adds the pair to zero, which
+  // changes no value (at most the sign of a zero result): a one-pair-per-tile
+  // kernel computes the same without the running sum's registers.  The
+  // 128-column one holds two accumulator pairs, so the epilogue of one tile
+  // overlaps the products of the next (K = 256, 16384 x 16384: 241.7 against
+  // 208.0 TFLOP/s for the 256-column kernel with one pair).
+  const int num_kb = K_padded / BK;
+  if ((variant == 0 && num_kb <= 4) || (variant == 3 && num_kb <= 8) || (variant == 4 && num_kb <= 16)) return 2;
+  if (variant == 5 && num_kb <= 8) return 2;
+  return variant;
+}
+
 cudaError_t launch_gemm_bf16x6(const CUtensorMap *maps, float *C, int M, int N, int K_padded, long long ldc,
                                int sm_count, int *err, int variant, int group_m, cudaStream_t stream) {
-  // When K fits in one chunk the running sum only adds the pair to zero, which
-  // changes no value (at most the sign of a zero result): the one-pair-per-tile
-  // kernel computes the same without the running sum's registers.
-  const int num_kb = K_padded / BK;
-  if ((variant == 0 && num_kb <= 4) || (variant == 3 && num_kb <= 8) || (variant == 4 && num_kb <= 16)) variant = 2;
-  if (variant == 5 && num_kb <= 8) variant = 1;
+  // the maps were encoded for the resolved variant's tile width
+  if (variant != gemm_tc_variant(variant, K_padded)) return cudaErrorInvalidValue;
   if (variant == 5) return launch_variant<256, 3, 1, 8>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   if (variant == 1) return launch_variant<256, 3, 1, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);
   if (variant == 2) return launch_variant<128, 4, 2, 0>(maps, C, M, N, K_padded, ldc, sm_count, group_m, err, stream);

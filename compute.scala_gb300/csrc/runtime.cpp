@@ -720,19 +720,19 @@ void run_gemm(Context &c, const float *A, const float *B, float *C, int m, int n
   if (e == cudaSuccess) {
     CUtensorMap maps[9];
     const size_t plane_a = (size_t)Mp * Kp * 2, plane_b = (size_t)Np * Kp * 2;
+    const int variant = gemm_tc_variant(c.tc_variant, Kp);  // the kernel that runs: its tile width
     try {
       for (int p = 0; p < 3; ++p) {
         encode_plane_map(&maps[p], static_cast<char *>(pa) + p * plane_a, Mp, Kp, kTcBM);
-        encode_plane_map(&maps[3 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp, gemm_tc_box_n(c.tc_variant));
-        encode_plane_map(&maps[6 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp,
-                         gemm_tc_box_n(c.tc_variant) / 2);
+        encode_plane_map(&maps[3 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp, gemm_tc_box_n(variant));
+        encode_plane_map(&maps[6 + p], static_cast<char *>(pb) + p * plane_b, Np, Kp, gemm_tc_box_n(variant) / 2);
       }
     } catch (...) {
       release_block(c, pa, cls_a);
       release_block(c, pb, cls_b);
       throw;
     }
-    e = launch_gemm_bf16x6(maps, C, m, n, Kp, ldc, c.sm_count, c.error_flag(), c.tc_variant, c.tc_group_m, s);
+    e = launch_gemm_bf16x6(maps, C, m, n, Kp, ldc, c.sm_count, c.error_flag(), variant, c.tc_group_m, s);
   }
   // blocks of the pool are ordered on the context stream and the queues; wait for other streams
   if (s != c.stream && queue_index(c, s) < 0 && e == cudaSuccess) e = cudaStreamSynchronize(s);
