@@ -358,6 +358,14 @@ def contraction_extras(d, st):
     ms = rt.event_elapsed_ms(e0, e1) / 3
     c32 = np.stack([rt.download(out, n, offset=int(r) * n * 4) for r in rows]).astype(np.float64)
     err32 = float(np.linalg.norm(c32 - ref) / np.linalg.norm(ref))
+    # the exact fold (the default contraction mode: the reference's rounding order), timed once
+    exact_args = args[:-1] + (rt.GEMM_EXACT,)
+    rt.gemm_ptr(*exact_args)
+    e0 = rt.event()
+    rt.gemm_ptr(*exact_args)
+    e1 = rt.event()
+    rt.event_wait(e1)
+    ms_exact = rt.event_elapsed_ms(e0, e1)
     out.release()
     info = rt.device_info()
     # FP32 CUDA-core peak: 128 FP32 lanes per SM, one FMA (2 flops) each per clock, at the maximum SM clock
@@ -366,7 +374,10 @@ def contraction_extras(d, st):
     return {"rel_fro_err_vs_fp64": err, "rows_checked": int(len(rows)),
             "fp32_cuda_core_tflops": fp32, "fp32_cuda_core_rel_fro_err": err32,
             "fp32_cuda_core_peak_tflops": fp32_peak, "fp32_cuda_core_frac_of_peak": fp32 / fp32_peak,
-            "fp32_cuda_core_peak_note": "SMs x 128 FP32 lanes x 2 flops x 2070 MHz (nominal)"}
+            "fp32_cuda_core_peak_note": "SMs x 128 FP32 lanes x 2 flops x 2070 MHz (nominal)",
+            "exact_fold_tflops": 2.0 * m * n * k / (ms_exact * 1e-3) / 1e12,
+            "exact_fold_note": "the default contraction mode: per output, products and sums rounded separately "
+                               "in the reference's order (one mul and one add per term)"}
 
 
 def time_device(rt, st, steps, warmup):

@@ -26,6 +26,10 @@ constexpr int kTk = 8;      // k per smem stage
 
 // One 128x128 output tile per block of 256 threads; each thread owns an 8x8
 // sub-tile made of rows {ty*4+r, 64+ty*4+r} and columns {tx*4+c, 64+tx*4+c}.
+// The accumulators are pairs of adjacent columns.  The plain GEMM updates them
+// with the packed FP32 fused multiply-add (fma.rn.f32x2: one instruction for
+// two outputs, each lane the scalar fmaf); the exact fold keeps the scalar
+// __fmul_rn / __fadd_rn, which no compiler stage fuses.
 template <bool kExact>
 __global__ void __launch_bounds__(256) sgemm_kernel(const float *__restrict__ A, const float *__restrict__ B,
                                                     float *__restrict__ C, int M, int N, int K, long long lda,
@@ -35,11 +39,11 @@ __global__ void __launch_bounds__(256) sgemm_kernel(const float *__restrict__ A,
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int bm = blockIdx.y * kTile, bn = blockIdx.x * kTile;
-  float acc[8][8];
+  float2 acc[8][4];  // acc[i][jp]: columns 2*jp and 2*jp + 1 of the thread's eight
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.0f, 0.0f);
 
   // global -> register staging: A: row tid/2, k (tid%2)*4..+3; B: k-row tid/32, cols (tid%32)*4..+3
   const int a_r = tid >> 1, a_c = (tid & 1) * 4;
@@ -81,17 +85,23 @@ __global__ void __launch_bounds__(256) sgemm_kernel(const float *__restrict__ A,
           b[4 + r] = Bs[buf][kk][64 + tx * 4 + r];
         }
         const bool first = (t == 0 && kk == 0);
+        float2 b2[4];
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
+        for (int j = 0; j < 4; ++j) b2[j] = make_float2(b[2 * j], b[2 * j + 1]);
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
+        for (int i = 0; i < 8; ++i) {
+          const float2 a2 = make_float2(a[i], a[i]);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
             if (kExact) {
-              const float p = __fmul_rn(a[i], b[j]);
-              acc[i][j] = first ? p : __fadd_rn(acc[i][j], p);
+              const float px = __fmul_rn(a[i], b2[j].x), py = __fmul_rn(a[i], b2[j].y);
+              acc[i][j].x = first ? px : __fadd_rn(acc[i][j].x, px);
+              acc[i][j].y = first ? py : __fadd_rn(acc[i][j].y, py);
             } else {
-              acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+              acc[i][j] = __ffma2_rn(a2, b2[j], acc[i][j]);
             }
           }
+        }
       }
     }
     if (t + 1 < ntiles) store(buf ^ 1);
@@ -104,7 +114,7 @@ __global__ void __launch_bounds__(256) sgemm_kernel(const float *__restrict__ A,
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int gc = bn + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
-      if (gc < N) C[gr * ldc + gc] = acc[i][j];
+      if (gc < N) C[gr * ldc + gc] = (j & 1) ? acc[i][j >> 1].y : acc[i][j >> 1].x;
     }
   }
 }
