@@ -5,7 +5,7 @@ The reference enqueues every kernel on a queue of its CommandQueuePool with the
 events of the buffers it reads as its wait list (Kernel.enqueue, OpenCL.scala:
 787-844, dispatch :1298-1329; CompiledKernel.run, Tensors.scala:1331-1381), so
 independent subgraphs run concurrently and a kernel starts once its inputs
-exist.  Here the *_ev entry points do the same over five CUDA streams; these
+exist.  Here the *_ev entry points do the same over eight CUDA streams; these
 tests check that such graphs compute the oracle's bits, that the chains of a
 graph really overlap, and that buffers released while other streams may still
 use them are not reused too early.
